@@ -1,0 +1,329 @@
+"""bc_gb300 -- Python access to libgbc, the GB300 (sm_103a) betweenness /
+closeness library, through its C ABI (include/gbc.h) via ctypes.
+
+The library is built in-tree (``bc_gb300/libgbc.so``, see build.py).  There is
+no fallback: if the shared library is missing or a device call fails, the
+call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbc.so")
+
+BC_BRANDES, BC_REFERENCE = 0, 1
+DELTA_F32, DELTA_F64 = 0, 1
+SIGMA_AUTO, SIGMA_EXACT, SIGMA_LOG = 0, 1, 2
+ENGINE_AUTO, ENGINE_PLAIN, ENGINE_LANES = 0, 1, 2
+Q_CC, Q_BC, Q_BC_SAMPLED = 0, 1, 2
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
+
+STATUS = {0: "GBC_OK", 1: "GBC_ERR_ARG", 2: "GBC_ERR_CUDA", 3: "GBC_ERR_NOMEM", 4: "GBC_ERR_OVERFLOW",
+          5: "GBC_ERR_LIMIT", 6: "GBC_ERR_NOT_FOUND", 7: "GBC_ERR_BUSY", 8: "GBC_ERR_TIMEOUT", 9: "GBC_ERR_NO_DEVICE"}
+
+
+class GbcError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Options(C.Structure):
+    _fields_ = [("semantics", C.c_int32), ("delta_precision", C.c_int32), ("sigma_mode", C.c_int32),
+                ("engine", C.c_int32), ("lanes", C.c_int32), ("sparse_lanes", C.c_int32),
+                ("levels_per_graph", C.c_int32), ("reserved", C.c_int32 * 9)]
+
+
+class RunStats(C.Structure):
+    _fields_ = [("sources", C.c_int64), ("batches", C.c_int64), ("levels", C.c_int64),
+                ("kernel_launches", C.c_int64), ("graph_launches", C.c_int64), ("edges_traversed", C.c_int64),
+                ("frontier_entries", C.c_int64), ("sigma_overflow_lanes", C.c_int64), ("kernel_ms", C.c_double),
+                ("total_ms", C.c_double), ("lanes", C.c_int32), ("sigma_mode_used", C.c_int32),
+                ("reserved", C.c_int32 * 8)]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}
+
+
+class ReducedInfo(C.Structure):
+    _fields_ = [("n", C.c_int32), ("d1_folded", C.c_int32), ("d1_hubs", C.c_int32), ("alive", C.c_int32),
+                ("articulation_points", C.c_int32), ("blocks", C.c_int32), ("max_block", C.c_int32),
+                ("block_slots", C.c_int32), ("block_edges", C.c_int64), ("components", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_lanes", C.c_int32), ("max_inflight", C.c_int32),
+                ("reserved", C.c_int32 * 8)]
+
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+_st = C.c_int
+
+# (name, restype, argtypes) of every C-ABI entry point used from Python.
+_PROTOS = [
+    ("gbc_options_default", None, [C.POINTER(Options)]),
+    ("gbc_last_error", C.c_char_p, []),
+    ("gbc_version", C.c_char_p, []),
+    ("gbc_device_count", C.c_int, []),
+    ("gbc_graph_create", _st, [_i64p, _i32p, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_graph_create_device", _st, [_vp, _vp, C.c_int32, C.c_int64, C.POINTER(_vp)]),
+    ("gbc_graph_destroy", _st, [_vp]),
+    ("gbc_graph_info", _st, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_size_t)]),
+    ("gbc_graph_last_stats", _st, [_vp, C.POINTER(RunStats)]),
+    ("gbc_bc", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _f64p]),
+    ("gbc_bc_device", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _vp, _vp]),
+    ("gbc_cc", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _i64p]),
+    ("gbc_cc_device", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _vp, _vp]),
+    ("gbc_sssp", _st, [_vp, _i32p, C.c_int32, C.POINTER(Options), _vp, _vp, _vp]),
+    ("gbc_reduce", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_reduced_info_get", _st, [_vp, C.POINTER(ReducedInfo)]),
+    ("gbc_cc_reduced", _st, [_vp, C.POINTER(Options), _i64p]),
+    ("gbc_bc_reduced", _st, [_vp, C.POINTER(Options), _f64p]),
+    ("gbc_reduced_destroy", _st, [_vp]),
+    ("gbc_reduced_block_graph", _st, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
+    ("gbc_reduced_assemble_cc", _st, [_vp, _i64p, _i64p]),
+    ("gbc_gen_ba", _st, [C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_vp), C.POINTER(_vp)]),
+    ("gbc_gen_rmat", _st, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int32,
+                           C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
+    ("gbc_gen_grid", _st, [C.c_int32, C.c_int32, C.c_double, C.c_uint64, C.c_int32, C.POINTER(_vp),
+                           C.POINTER(_vp), C.POINTER(C.c_int32)]),
+    ("gbc_gen_er", _st, [C.c_int32, C.c_double, C.c_uint64, C.POINTER(_vp), C.POINTER(_vp)]),
+    ("gbc_add_pendants", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_vp),
+                               C.POINTER(_vp), C.POINTER(C.c_int32)]),
+    ("gbc_read_edgelist", _st, [C.c_char_p, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32)]),
+    ("gbc_free", None, [_vp]),
+    ("gbc_server_create", _st, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    ("gbc_server_destroy", _st, [_vp]),
+    ("gbc_server_add_graph", _st, [_vp, _i64p, _i32p, C.c_int32, C.POINTER(C.c_int32)]),
+    ("gbc_server_submit", _st, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(Options), C.c_double,
+                                C.POINTER(C.c_int64)]),
+    ("gbc_server_poll", _st, [_vp, C.c_int64, C.POINTER(C.c_int32)]),
+    ("gbc_server_wait", _st, [_vp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
+    ("gbc_server_fetch", _st, [_vp, C.c_int64, _vp, _vp, C.POINTER(C.c_double)]),
+    ("gbc_server_cancel", _st, [_vp, C.c_int64]),
+    ("gbc_server_counters", _st, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+]
+
+_LIB = None
+
+
+def lib():
+    """Load libgbc.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m bc_gb300.build` "
+                               "(or __graft_entry__.build()); there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in _PROTOS:
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(status: int):
+    if status != 0:
+        raise GbcError(status, lib().gbc_last_error().decode(errors="replace"))
+
+
+def options(**kw) -> Options:
+    o = Options()
+    lib().gbc_options_default(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, int(v))
+    return o
+
+
+def device_count() -> int:
+    return int(lib().gbc_device_count())
+
+
+# --------------------------------------------------------------- graphs ----
+class CSR:
+    """Host CSR: row[n+1] int64, col int32 (both directions of every edge)."""
+
+    def __init__(self, row, col, start: int = 0):
+        self.row = np.ascontiguousarray(row, dtype=np.int64)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        self.n = int(self.row.shape[0] - 1)
+        self.start = int(start)
+
+    @property
+    def m(self) -> int:
+        return int(self.row[-1])
+
+
+def _take_csr(rp, cp, n, start=0) -> CSR:
+    L = lib()
+    row = np.ctypeslib.as_array(C.cast(rp, C.POINTER(C.c_int64)), shape=(n + 1,)).copy()
+    m = int(row[-1])
+    col = np.ctypeslib.as_array(C.cast(cp, C.POINTER(C.c_int32)), shape=(max(m, 1),))[:m].copy()
+    L.gbc_free(rp)
+    L.gbc_free(cp)
+    return CSR(row, col, start)
+
+
+def gen_ba(n: int, m: int, seed: int) -> CSR:
+    rp, cp = _vp(), _vp()
+    check(lib().gbc_gen_ba(n, m, seed, C.byref(rp), C.byref(cp)))
+    return _take_csr(rp, cp, n)
+
+
+def gen_rmat(scale: int, edge_factor: int, a=0.57, b=0.19, c=0.19, seed=1, permute=True) -> CSR:
+    rp, cp, n = _vp(), _vp(), C.c_int32()
+    check(lib().gbc_gen_rmat(scale, edge_factor, a, b, c, seed, int(permute), C.byref(rp), C.byref(cp), C.byref(n)))
+    return _take_csr(rp, cp, n.value)
+
+
+def gen_grid(rows: int, cols: int, remove_frac=0.0, seed=3, largest_only=True) -> CSR:
+    rp, cp, n = _vp(), _vp(), C.c_int32()
+    check(lib().gbc_gen_grid(rows, cols, remove_frac, seed, int(largest_only), C.byref(rp), C.byref(cp), C.byref(n)))
+    return _take_csr(rp, cp, n.value)
+
+
+def gen_er(n: int, avg_degree: float, seed: int) -> CSR:
+    rp, cp = _vp(), _vp()
+    check(lib().gbc_gen_er(n, avg_degree, seed, C.byref(rp), C.byref(cp)))
+    return _take_csr(rp, cp, n)
+
+
+def add_pendants(g: CSR, trees: int, max_depth: int, seed: int) -> CSR:
+    rp, cp, n = _vp(), _vp(), C.c_int32()
+    check(lib().gbc_add_pendants(g.row, g.col, g.n, trees, max_depth, seed, C.byref(rp), C.byref(cp), C.byref(n)))
+    return _take_csr(rp, cp, n.value)
+
+
+def read_edgelist(path: str) -> CSR:
+    rp, cp, n, st = _vp(), _vp(), C.c_int32(), C.c_int32()
+    check(lib().gbc_read_edgelist(path.encode(), C.byref(rp), C.byref(cp), C.byref(n), C.byref(st)))
+    return _take_csr(rp, cp, n.value, st.value)
+
+
+class Graph:
+    """A device-resident graph (gbc_graph handle)."""
+
+    def __init__(self, csr: CSR):
+        self.csr = csr
+        self.n = csr.n
+        h = _vp()
+        check(lib().gbc_graph_create(csr.row, csr.col, csr.n, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbc_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _src(self, sources):
+        if sources is None:
+            return None, 0, None
+        s = np.ascontiguousarray(sources, dtype=np.int32)
+        return s.ctypes.data_as(_vp), len(s), s
+
+    def bc(self, sources=None, **opt) -> np.ndarray:
+        out = np.zeros(self.n, np.float64)
+        p, k, keep = self._src(sources)
+        check(lib().gbc_bc(self.h, p, k, C.byref(options(**opt)), out))
+        return out
+
+    def cc(self, sources=None, **opt) -> np.ndarray:
+        p, k, keep = self._src(sources)
+        out = np.zeros(k if k else self.n, np.int64)
+        check(lib().gbc_cc(self.h, p, k, C.byref(options(**opt)), out))
+        return out
+
+    def sssp(self, sources, **opt):
+        s = np.ascontiguousarray(sources, dtype=np.int32)
+        dist = np.empty((len(s), self.n), np.int32)
+        sig = np.empty((len(s), self.n), np.uint64)
+        ovf = np.empty(len(s), np.uint8)
+        check(lib().gbc_sssp(self.h, s, len(s), C.byref(options(**opt)), dist.ctypes.data_as(_vp),
+                             sig.ctypes.data_as(_vp), ovf.ctypes.data_as(_vp)))
+        return dist, sig, ovf.astype(bool)
+
+    def stats(self) -> dict:
+        st = RunStats()
+        check(lib().gbc_graph_last_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+
+class Reduced:
+    """D1-folded, block-split form of a host CSR (gbc_reduced handle)."""
+
+    def __init__(self, csr: CSR):
+        self.csr = csr
+        h = _vp()
+        check(lib().gbc_reduce(csr.row, csr.col, csr.n, csr.start, C.byref(h)))
+        self.h = h
+
+    def info(self) -> dict:
+        i = ReducedInfo()
+        check(lib().gbc_reduced_info_get(self.h, C.byref(i)))
+        return i.as_dict()
+
+    def cc(self, **opt) -> np.ndarray:
+        out = np.zeros(self.csr.n, np.int64)
+        check(lib().gbc_cc_reduced(self.h, C.byref(options(**opt)), out))
+        return out
+
+    def bc(self, **opt) -> np.ndarray:
+        out = np.zeros(self.csr.n, np.float64)
+        check(lib().gbc_bc_reduced(self.h, C.byref(options(**opt)), out))
+        return out
+
+    def block_graph(self):
+        """(CSR over block slots, per-slot clone weights)."""
+        rp, cp, wp, ns = _vp(), _vp(), _vp(), C.c_int32()
+        check(lib().gbc_reduced_block_graph(self.h, C.byref(rp), C.byref(cp), C.byref(wp), C.byref(ns)))
+        w = np.ctypeslib.as_array(C.cast(wp, C.POINTER(C.c_int32)), shape=(max(ns.value, 1),))[: ns.value].copy()
+        lib().gbc_free(wp)
+        return _take_csr(rp, cp, ns.value), w
+
+    def assemble_cc(self, D) -> np.ndarray:
+        out = np.zeros(self.csr.n, np.int64)
+        check(lib().gbc_reduced_assemble_cc(self.h, np.ascontiguousarray(D, dtype=np.int64), out))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbc_reduced_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,469 @@
+// C ABI of libgbc: device-resident graphs, betweenness / closeness / per-source
+// counts through the lane or plain engine, with status codes and stats.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "engine.h"
+
+using namespace gbc;
+
+struct gbc_graph_s {
+    DevGraph g;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::unique_ptr<LaneEngine> eng;
+    gbc_run_stats last{};
+    int32_t* d_src = nullptr;
+    int64_t src_cap = 0;
+    unsigned long long* d_ccb = nullptr;
+    int64_t ccb_cap = 0;
+    double* d_bc = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ~gbc_graph_s() {
+        eng.reset();
+        cudaFree(g.row);
+        cudaFree(g.col);
+        cudaFree(d_src);
+        cudaFree(d_ccb);
+        cudaFree(d_bc);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace gbc {
+
+// Component ids and per-component undirected edge counts of a host CSR.
+static void host_components(const int64_t* row, const int32_t* col, int32_t n, DevGraph& g) {
+    HostCSR h;
+    h.n = n;
+    h.row.assign(row, row + n + 1);
+    h.col.assign(col, col + row[n]);
+    std::vector<int64_t> sizes;
+    const int32_t nc = components(h, g.comp, sizes);
+    g.comp_edges.assign(nc, 0);
+    int32_t md = 0;
+    for (int32_t v = 0; v < n; v++) {
+        g.comp_edges[g.comp[v]] += row[v + 1] - row[v];
+        md = std::max<int32_t>(md, (int32_t)(row[v + 1] - row[v]));
+    }
+    for (auto& e : g.comp_edges) e /= 2;
+    g.max_degree = md;
+}
+
+gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_graph_s* G) {
+    DevGraph& g = G->g;
+    g.n = n;
+    g.m = row[n];
+    GBC_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    GBC_CUDA(cudaEventCreate(&G->ev0));
+    GBC_CUDA(cudaEventCreate(&G->ev1));
+    if (cudaMalloc(&g.row, sizeof(int64_t) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&g.col, sizeof(int32_t) * std::max<int64_t>(g.m, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation for the CSR failed");
+        return GBC_ERR_NOMEM;
+    }
+    GBC_CUDA(cudaMemcpyAsync(g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, G->stream));
+    if (g.m) GBC_CUDA(cudaMemcpyAsync(g.col, col, sizeof(int32_t) * g.m, cudaMemcpyHostToDevice, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    host_components(row, col, n, g);
+    return GBC_OK;
+}
+
+static gbc_status ensure_device() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device available (%s)", cudaGetErrorString(e));
+        return GBC_ERR_NO_DEVICE;
+    }
+    return GBC_OK;
+}
+
+static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
+    gbc_options_default(&o);
+    if (opt) o = *opt;
+    if (o.semantics != GBC_BC_BRANDES && o.semantics != GBC_BC_REFERENCE) { set_error("bad semantics"); return GBC_ERR_ARG; }
+    if (o.delta_precision != GBC_DELTA_F32 && o.delta_precision != GBC_DELTA_F64) { set_error("bad delta precision"); return GBC_ERR_ARG; }
+    if (o.sigma_mode < GBC_SIGMA_AUTO || o.sigma_mode > GBC_SIGMA_LOG) { set_error("bad sigma mode"); return GBC_ERR_ARG; }
+    if (o.engine < GBC_ENGINE_AUTO || o.engine > GBC_ENGINE_LANES) { set_error("bad engine"); return GBC_ERR_ARG; }
+    if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("lanes must be 0 or a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
+    return GBC_OK;
+}
+
+// Autotune lanes: as wide as the sources and the memory budget allow.
+static int32_t pick_lanes(const DevGraph& g, int64_t k, bool bc, int32_t requested) {
+    if (requested) return requested;
+    int32_t lanes = (int32_t)std::min<int64_t>(1024, ((k + 31) / 32) * 32);
+    lanes = std::max(lanes, 32);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    const size_t budget = fr / 2;
+    while (lanes > 32 && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= 32;
+    return lanes;
+}
+
+static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
+    if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc)) { *out = G->eng.get(); return GBC_OK; }
+    G->eng.reset();
+    auto e = std::make_unique<LaneEngine>();
+    GBC_TRY(e->init(&G->g, lanes, bc, o.sparse_lanes, o.levels_per_graph, G->stream));
+    G->eng = std::move(e);
+    *out = G->eng.get();
+    return GBC_OK;
+}
+
+static gbc_status stage_sources(gbc_graph_s* G, const int32_t* sources, int32_t k, std::vector<int32_t>& hsrc) {
+    const DevGraph& g = G->g;
+    if (k < 0) { set_error("k < 0"); return GBC_ERR_ARG; }
+    if (k == 0) {
+        if (sources) { set_error("k = 0 with a non-NULL source list"); return GBC_ERR_ARG; }
+        hsrc.resize(g.n);
+        for (int32_t i = 0; i < g.n; i++) hsrc[i] = i;
+    } else {
+        if (!sources) { set_error("sources is NULL"); return GBC_ERR_ARG; }
+        hsrc.assign(sources, sources + k);
+        for (int32_t i = 0; i < k; i++)
+            if (hsrc[i] < 0 || hsrc[i] >= g.n) { set_error("source %d out of range [0,%d)", hsrc[i], g.n); return GBC_ERR_ARG; }
+    }
+    if ((int64_t)hsrc.size() > G->src_cap) {
+        cudaFree(G->d_src);
+        G->d_src = nullptr;
+        if (cudaMalloc(&G->d_src, sizeof(int32_t) * hsrc.size()) != cudaSuccess) { cudaGetLastError(); set_error("source buffer"); return GBC_ERR_NOMEM; }
+        G->src_cap = (int64_t)hsrc.size();
+    }
+    GBC_CUDA(cudaMemcpyAsync(G->d_src, hsrc.data(), sizeof(int32_t) * hsrc.size(), cudaMemcpyHostToDevice, G->stream));
+    return GBC_OK;
+}
+
+static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t batches, int32_t lanes, int sigma_used,
+                         const std::vector<int32_t>& hsrc, double ms_kernel, double ms_total) {
+    gbc_run_stats& s = G->last;
+    std::memset(&s, 0, sizeof s);
+    s.sources = k;
+    s.batches = batches;
+    s.levels = r.levels;
+    s.kernel_launches = r.kernel_launches;
+    s.graph_launches = r.graph_launches;
+    s.frontier_entries = r.frontier_entries;
+    s.sigma_overflow_lanes = r.overflow_count;
+    s.kernel_ms = ms_kernel;
+    s.total_ms = ms_total;
+    s.lanes = lanes;
+    s.sigma_mode_used = sigma_used;
+    int64_t e = 0;
+    for (int32_t x : hsrc) e += G->g.comp_edges[G->g.comp[x]];
+    s.edges_traversed = e;
+}
+
+// Betweenness over device-staged sources d_src[0..k) into d_bc[n].
+static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const gbc_options& o, double* d_bc,
+                          LaneResult& res, int32_t& lanes_used, int& sigma_used, int64_t& batches) {
+    const DevGraph& g = G->g;
+    if (o.engine == GBC_ENGINE_PLAIN) {
+        std::vector<int32_t> h(k);
+        GBC_CUDA(cudaMemcpyAsync(h.data(), d_src, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, G->stream));
+        GBC_CUDA(cudaStreamSynchronize(G->stream));
+        GBC_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * g.n, G->stream));
+        GBC_TRY(plain_bc(&g, h.data(), k, o.semantics, o.delta_precision == GBC_DELTA_F64, d_bc, G->stream, res));
+        lanes_used = 1;
+        sigma_used = GBC_SIGMA_EXACT;
+        batches = k;
+        if (res.overflow_count && o.sigma_mode != GBC_SIGMA_LOG) {
+            set_error("exact path counts overflowed uint64 for %d sources (plain engine has no log form)", res.overflow_count);
+            return GBC_ERR_OVERFLOW;
+        }
+        return GBC_OK;
+    }
+    const int32_t lanes = pick_lanes(g, k, true, o.lanes);
+    LaneEngine* E = nullptr;
+    GBC_TRY(get_engine(G, lanes, true, o, &E));
+    lanes_used = lanes;
+    GBC_TRY(E->bc_begin());
+    sigma_used = o.sigma_mode == GBC_SIGMA_LOG ? GBC_SIGMA_LOG : GBC_SIGMA_EXACT;
+    batches = 0;
+    for (int32_t b0 = 0; b0 < k; b0 += lanes) {
+        LaneRequest rq;
+        rq.job = LaneJob::BC;
+        rq.d_src = d_src + b0;
+        rq.kb = std::min(lanes, k - b0);
+        rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
+        rq.semantics = o.semantics;
+        rq.sigma_log = (o.sigma_mode == GBC_SIGMA_LOG);
+        rq.abort_on_overflow = !rq.sigma_log;
+        gbc_status st = E->run(rq, res);
+        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO) {
+            rq.sigma_log = 1;
+            rq.abort_on_overflow = false;
+            sigma_used = GBC_SIGMA_LOG;
+            st = E->run(rq, res);
+        }
+        if (st != GBC_OK) return st;
+        batches++;
+    }
+    return E->bc_finish(d_bc);
+}
+
+static gbc_status cc_core(gbc_graph_s* G, const int32_t* d_src, const int32_t* h_src, int32_t k, const gbc_options& o,
+                          unsigned long long* d_cc, int64_t* h_cc_plain, LaneResult& res, int32_t& lanes_used,
+                          int64_t& batches) {
+    const DevGraph& g = G->g;
+    if (o.engine == GBC_ENGINE_PLAIN) {
+        GBC_TRY(plain_cc(&g, h_src, k, h_cc_plain, G->stream, res));
+        lanes_used = 1;
+        batches = k;
+        return GBC_OK;
+    }
+    const int32_t lanes = pick_lanes(g, k, false, o.lanes);
+    LaneEngine* E = nullptr;
+    GBC_TRY(get_engine(G, lanes, false, o, &E));
+    lanes_used = lanes;
+    batches = 0;
+    for (int32_t b0 = 0; b0 < k; b0 += lanes) {
+        LaneRequest rq;
+        rq.job = LaneJob::CC;
+        rq.d_src = d_src + b0;
+        rq.kb = std::min(lanes, k - b0);
+        rq.d_cc = d_cc + b0;
+        GBC_TRY(E->run(rq, res));
+        batches++;
+    }
+    return GBC_OK;
+}
+
+}  // namespace gbc
+
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+extern "C" {
+
+const char* gbc_version(void) { return "gbc 0.1 (sm_103a)"; }
+
+int gbc_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return n;
+}
+
+void gbc_options_default(gbc_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->semantics = GBC_BC_BRANDES;
+    o->delta_precision = GBC_DELTA_F64;
+    o->sigma_mode = GBC_SIGMA_AUTO;
+    o->engine = GBC_ENGINE_AUTO;
+    o->lanes = 0;
+    o->sparse_lanes = -1;
+    o->levels_per_graph = 0;
+}
+
+gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, gbc_graph* out) {
+    if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    GBC_TRY(validate_csr(row, col, n));
+    GBC_TRY(ensure_device());
+    auto G = std::make_unique<gbc_graph_s>();
+    GBC_TRY(graph_upload(row, col, n, G.get()));
+    *out = G.release();
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t m, gbc_graph* out) {
+    if (!out || !d_row || (m > 0 && !d_col) || n <= 0 || m < 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    GBC_TRY(ensure_device());
+    std::vector<int64_t> row(n + 1);
+    std::vector<int32_t> col(std::max<int64_t>(m, 1));
+    GBC_CUDA(cudaMemcpy(row.data(), d_row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+    if (m) GBC_CUDA(cudaMemcpy(col.data(), d_col, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
+    if (row[n] != m) { set_error("row[n] != m"); return GBC_ERR_ARG; }
+    GBC_TRY(validate_csr(row.data(), col.data(), n));
+    auto G = std::make_unique<gbc_graph_s>();
+    GBC_TRY(graph_upload(row.data(), col.data(), n, G.get()));
+    *out = G.release();
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_destroy(gbc_graph g) {
+    if (!g) { set_error("graph is NULL"); return GBC_ERR_ARG; }
+    delete g;
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_info(gbc_graph G, int32_t* n, int64_t* m, size_t* bytes) {
+    if (!G) { set_error("graph is NULL"); return GBC_ERR_ARG; }
+    if (n) *n = G->g.n;
+    if (m) *m = G->g.m;
+    if (bytes) *bytes = sizeof(int64_t) * (G->g.n + 1) + sizeof(int32_t) * G->g.m + (G->eng ? G->eng->device_bytes() : 0);
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_last_stats(gbc_graph G, gbc_run_stats* st) {
+    if (!G || !st) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    *st = G->last;
+    return GBC_OK;
+}
+
+gbc_status gbc_bc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_options* opt, double* bc) {
+    if (!G || !bc) { set_error("NULL graph or output"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const double t0 = now_ms();
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    std::vector<int32_t> hsrc;
+    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    const int32_t kk = (int32_t)hsrc.size();
+    if (!G->d_bc) {
+        if (cudaMalloc(&G->d_bc, sizeof(double) * G->g.n) != cudaSuccess) { cudaGetLastError(); set_error("bc buffer"); return GBC_ERR_NOMEM; }
+    }
+    LaneResult res;
+    int32_t lanes = 0;
+    int sig = 0;
+    int64_t batches = 0;
+    GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
+    GBC_TRY(bc_core(G, G->d_src, kk, o, G->d_bc, res, lanes, sig, batches));
+    GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
+    GBC_CUDA(cudaMemcpyAsync(bc, G->d_bc, sizeof(double) * G->g.n, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+    finish_stats(G, res, kk, batches, lanes, sig, hsrc, ms, now_ms() - t0);
+    return GBC_OK;
+}
+
+gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const gbc_options* opt, double* d_bc,
+                         void* stream) {
+    if (!G || !d_bc || !d_sources || k <= 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const double t0 = now_ms();
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    cudaStream_t us = (cudaStream_t)stream;
+    GBC_CUDA(cudaEventRecord(G->ev0, us));
+    GBC_CUDA(cudaStreamWaitEvent(G->stream, G->ev0, 0));
+    LaneResult res;
+    int32_t lanes = 0;
+    int sig = 0;
+    int64_t batches = 0;
+    GBC_TRY(bc_core(G, d_sources, k, o, d_bc, res, lanes, sig, batches));
+    GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
+    GBC_CUDA(cudaStreamWaitEvent(us, G->ev1, 0));
+    GBC_CUDA(cudaEventSynchronize(G->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+    std::vector<int32_t> hsrc(k);
+    GBC_CUDA(cudaMemcpy(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
+    finish_stats(G, res, k, batches, lanes, sig, hsrc, ms, now_ms() - t0);
+    return GBC_OK;
+}
+
+gbc_status gbc_cc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_options* opt, int64_t* cc) {
+    if (!G || !cc) { set_error("NULL graph or output"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const double t0 = now_ms();
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    std::vector<int32_t> hsrc;
+    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    const int32_t kk = (int32_t)hsrc.size();
+    if (kk > G->ccb_cap) {
+        cudaFree(G->d_ccb);
+        G->d_ccb = nullptr;
+        if (cudaMalloc(&G->d_ccb, sizeof(unsigned long long) * kk) != cudaSuccess) { cudaGetLastError(); set_error("cc buffer"); return GBC_ERR_NOMEM; }
+        G->ccb_cap = kk;
+    }
+    LaneResult res;
+    int32_t lanes = 0;
+    int64_t batches = 0;
+    GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
+    GBC_TRY(cc_core(G, G->d_src, hsrc.data(), kk, o, G->d_ccb, cc, res, lanes, batches));
+    GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
+    if (o.engine != GBC_ENGINE_PLAIN)
+        GBC_CUDA(cudaMemcpyAsync(cc, G->d_ccb, sizeof(int64_t) * kk, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+    finish_stats(G, res, kk, batches, lanes, GBC_SIGMA_EXACT, hsrc, ms, now_ms() - t0);
+    return GBC_OK;
+}
+
+gbc_status gbc_cc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const gbc_options* opt, int64_t* d_cc,
+                         void* stream) {
+    if (!G || !d_cc || !d_sources || k <= 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const double t0 = now_ms();
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    if (o.engine == GBC_ENGINE_PLAIN) { set_error("gbc_cc_device runs the lane engine only"); return GBC_ERR_ARG; }
+    cudaStream_t us = (cudaStream_t)stream;
+    GBC_CUDA(cudaEventRecord(G->ev0, us));
+    GBC_CUDA(cudaStreamWaitEvent(G->stream, G->ev0, 0));
+    LaneResult res;
+    int32_t lanes = 0;
+    int64_t batches = 0;
+    GBC_TRY(cc_core(G, d_sources, nullptr, k, o, (unsigned long long*)d_cc, nullptr, res, lanes, batches));
+    GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
+    GBC_CUDA(cudaStreamWaitEvent(us, G->ev1, 0));
+    GBC_CUDA(cudaEventSynchronize(G->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, G->ev0, G->ev1);
+    std::vector<int32_t> hsrc(k);
+    GBC_CUDA(cudaMemcpy(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
+    finish_stats(G, res, k, batches, lanes, GBC_SIGMA_EXACT, hsrc, ms, now_ms() - t0);
+    return GBC_OK;
+}
+
+gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_options* opt, int32_t* dist,
+                    uint64_t* sigma, uint8_t* ovf) {
+    if (!G || !sources || k <= 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    std::vector<int32_t> hsrc;
+    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    const int32_t n = G->g.n;
+    const int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((k + 31) / 32) * 32);
+    LaneEngine* E = nullptr;
+    GBC_TRY(get_engine(G, lanes, true, o, &E));
+    int32_t* d_dist = nullptr;
+    uint64_t* d_sig = nullptr;
+    const size_t cells = (size_t)std::min(lanes, k) * n;
+    if (cudaMalloc(&d_dist, cells * sizeof(int32_t)) != cudaSuccess || cudaMalloc(&d_sig, cells * sizeof(uint64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_dist);
+        set_error("sssp output buffers");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<void, void (*)(void*)> f1(d_dist, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_sig, [](void* p) { cudaFree(p); });
+    LaneResult res;
+    for (int32_t b0 = 0; b0 < k; b0 += lanes) {
+        LaneRequest rq;
+        rq.job = LaneJob::SSSP;
+        rq.d_src = G->d_src + b0;
+        rq.kb = std::min(lanes, k - b0);
+        rq.d_dist = d_dist;
+        rq.d_sigma = d_sig;
+        GBC_TRY(E->run(rq, res));
+        const size_t c = (size_t)rq.kb * n;
+        if (dist) GBC_CUDA(cudaMemcpyAsync(dist + (size_t)b0 * n, d_dist, c * sizeof(int32_t), cudaMemcpyDeviceToHost, G->stream));
+        if (sigma) GBC_CUDA(cudaMemcpyAsync(sigma + (size_t)b0 * n, d_sig, c * sizeof(uint64_t), cudaMemcpyDeviceToHost, G->stream));
+        GBC_CUDA(cudaStreamSynchronize(G->stream));
+        if (ovf)
+            for (int32_t l = 0; l < rq.kb; l++) ovf[b0 + l] = (res.ovf_bits[l >> 5] >> (l & 31)) & 1u;
+    }
+    return GBC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Engines behind the C ABI: the batched multi-source lane engine and the
+// plain one-source-at-a-time engine.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "gbc_internal.h"
+
+namespace gbc {
+
+#define GBC_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess) {                                                               \
+            gbc::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return GBC_ERR_CUDA;                                                               \
+        }                                                                                      \
+    } while (0)
+
+#define GBC_TRY(expr)                         \
+    do {                                      \
+        gbc_status s_ = (expr);               \
+        if (s_ != GBC_OK) return s_;          \
+    } while (0)
+
+// Device CSR (+ host-side component information for the GTEPS numerator).
+struct DevGraph {
+    int32_t n = 0;
+    int64_t m = 0;             // directed entries
+    int64_t* row = nullptr;    // device [n+1]
+    int32_t* col = nullptr;    // device [m]
+    const int32_t* w = nullptr;   // device per-vertex weights (reduced graphs), nullable
+    const int64_t* ff = nullptr;  // device per-vertex folded distance sums, nullable
+    std::vector<int32_t> comp;         // host, per vertex
+    std::vector<int64_t> comp_edges;   // host, undirected edges per component
+    int32_t max_degree = 0;
+};
+
+// Which computation a lane batch performs.
+enum class LaneJob { CC, BC, SSSP };
+
+struct LaneRequest {
+    LaneJob job = LaneJob::CC;
+    const int32_t* d_src = nullptr;  // device sources of this batch
+    int32_t kb = 0;                  // sources in this batch (<= lanes)
+    int sigma_log = 0;               // 1: log2-domain path counts
+    int delta_f64 = 1;
+    int semantics = GBC_BC_BRANDES;
+    unsigned long long* d_cc = nullptr;  // [kb] per-lane distance sums (CC)
+    double* d_bcg = nullptr;             // [ng][n] per-group BC partials (BC)
+    int32_t* d_dist = nullptr;           // [kb][n] (SSSP) nullable
+    uint64_t* d_sigma = nullptr;         // [kb][n] (SSSP) nullable
+    bool abort_on_overflow = false;      // exact sigma: stop before the backward sweep if a lane overflowed
+};
+
+struct LaneResult {
+    int64_t levels = 0;
+    uint32_t ovf_bits[32] = {};    // per lane group: lanes whose exact sigma overflowed (last batch)
+    int32_t overflow_count = 0;    // overflowed lanes, summed over batches
+    int64_t frontier_entries = 0;
+    int64_t kernel_launches = 0;
+    int64_t graph_launches = 0;
+};
+
+class LaneEngine {
+public:
+    LaneEngine() = default;
+    ~LaneEngine();
+    LaneEngine(const LaneEngine&) = delete;
+    LaneEngine& operator=(const LaneEngine&) = delete;
+    // Allocate lane state for `lanes` (multiple of 32, <= 1024) on graph g.
+    gbc_status init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
+                    cudaStream_t stream);
+    // One batch of rq.kb <= lanes sources (forward, then backward for BC).
+    gbc_status run(const LaneRequest& rq, LaneResult& res);
+    // BC accumulation across batches: zero the per-group partials / reduce them into d_bc[n].
+    gbc_status bc_begin();
+    gbc_status bc_finish(double* d_bc);
+    int32_t lanes() const { return lanes_; }
+    bool has_bc() const { return need_bc_; }
+    const DevGraph* graph() const { return g_; }
+    cudaStream_t stream() const { return stream_; }
+    size_t device_bytes() const { return bytes_; }
+    static size_t bytes_needed(int32_t n, int32_t lanes, bool need_bc);
+
+private:
+    friend struct LaneAccess;
+    gbc_status get_graph(int key, cudaGraphExec_t* out);
+    gbc_status alloc_queue(unsigned long long cap);
+    void release();
+
+    const DevGraph* g_ = nullptr;
+    int32_t lanes_ = 0, ng_ = 0;
+    bool need_bc_ = false;
+    int sparse_ = 2;
+    int lpg_ = 16;
+    int grid_ = 0;
+    cudaStream_t stream_ = nullptr;
+    size_t bytes_ = 0;
+    uint16_t* lvl_ = nullptr;
+    uint64_t* sig_ = nullptr;
+    void* rho_ = nullptr;
+    int32_t* vmark_ = nullptr;
+    uint32_t* fq_ = nullptr;
+    unsigned long long fcap_ = 0;
+    unsigned long long* foff_ = nullptr;
+    void* ctl_ = nullptr;
+    void* ctl_host_ = nullptr;
+    uint32_t* ovf_ = nullptr;
+    double* bcg_ = nullptr;
+    unsigned long long* ccbuf_ = nullptr;
+    struct Captured { int key = -1; cudaGraphExec_t exec = nullptr; };
+    std::vector<Captured> graphs_;
+    int sm_count_ = 0;
+};
+
+// Plain engine: one source at a time, int32 distances, uint64 sigma, the
+// level loop driven from the host with one device->host read per level.
+gbc_status plain_bc(const DevGraph* g, const int32_t* h_src, int32_t k, int semantics, int delta_f64,
+                    double* d_bc, cudaStream_t st, LaneResult& res);
+gbc_status plain_cc(const DevGraph* g, const int32_t* h_src, int32_t k, int64_t* h_cc, cudaStream_t st,
+                    LaneResult& res);
+
+}  // namespace gbc

@@ -1,0 +1,519 @@
+// D1 folding + articulation-point (block) reduction for closeness, and D1
+// folding for betweenness.
+//
+// Folding (as Lib/D1Process/D1Process.c:32-73): degree-1 vertices are peeled
+// repeatedly into their neighbour, which accumulates reach r (vertices it
+// stands for) and ff (sum of distances from it to the vertices folded into
+// it).  A vertex whose last neighbour was folded into it is the root of a
+// tree component and stays.
+//
+// Splitting: the folded graph is cut into biconnected blocks (Hopcroft-Tarjan
+// with an edge stack).  For a block B and a vertex b of B that is an
+// articulation point, the clone weight w'_B(b) = r(b) + reach of every vertex
+// separated from B by b (the AP clones of Lib/AP_Process/AP_Process.c:916-1020
+// carry the same reach).  Then for every vertex v and any block B holding v
+//     CC(v) = FF_B + D_B(v),   D_B(v) = sum_{u in B} d_B(v,u) * w'_B(u)
+// where FF_B = sum_{u in B} ff'_B(u) and ff'_B(b) folds the distance sums of
+// everything behind b.  D_B is a weighted distance sum computed for every
+// (block, vertex) slot by the lane engine on the disjoint union of the
+// blocks; FF_B follows from two passes over the block-cut tree on the host.
+// Folded vertices are recovered in reverse folding order with
+//     CC(d1) = CC(parent) + N_c - 2 r(d1)
+// (Seq_CC/CC.cpp:2037-2049) where N_c is the size of d1's connected
+// component (the reference uses the global vertex count, which is only right
+// for connected graphs).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "engine.h"
+
+namespace gbc {
+
+struct Reduction {
+    int32_t n = 0, start = 0;
+    // folding
+    std::vector<int64_t> r, ff;       // reach and folded distance sums
+    std::vector<int32_t> parent;      // folded vertex -> vertex it was folded into
+    std::vector<int32_t> fold_order;
+    std::vector<uint8_t> folded, is_ap;
+    int32_t n_hub = 0;
+    // connected components of the folded graph (alive vertices)
+    std::vector<int32_t> comp;        // per vertex slot (-1 for the phantom slot)
+    std::vector<int64_t> comp_w;      // total reach per component
+    int32_t n_comp = 0;
+    // blocks
+    int32_t n_blocks = 0;
+    std::vector<int64_t> bvoff;       // block -> first slot
+    std::vector<int32_t> slot_v;      // slot -> vertex
+    std::vector<int32_t> slot_w;      // slot -> clone weight w'
+    std::vector<int32_t> vslot;       // vertex -> one slot holding it (its only slot unless AP)
+    HostCSR bg;                       // block graph over slots
+    // block-cut tree
+    std::vector<int32_t> bparent_ap;  // block -> parent AP vertex (-1 for a root block)
+    std::vector<int32_t> ap_parent_block;  // vertex -> parent block (APs only)
+    std::vector<std::vector<int32_t>> ap_child_blocks;  // per AP vertex (index by vertex via map)
+    std::vector<int32_t> ap_index;    // vertex -> index into ap_child_blocks (-1 if not AP)
+    std::vector<int32_t> border;      // blocks in BFS order from the roots
+    int32_t max_block = 0;
+    // device copy of the block graph
+    std::unique_ptr<DevGraph> dg;
+    int32_t* d_w = nullptr;
+    cudaStream_t stream = nullptr;
+    std::unique_ptr<LaneEngine> eng;
+    std::mutex mu;
+    ~Reduction() {
+        eng.reset();
+        if (dg) { cudaFree(dg->row); cudaFree(dg->col); }
+        cudaFree(d_w);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+// ---------------------------------------------------------------- fold ----
+static void fold(const int64_t* row, const int32_t* col, Reduction& R, std::vector<int32_t>& livecol,
+                 std::vector<int64_t>& lo) {
+    const int32_t n = R.n;
+    livecol.assign(col, col + row[n]);
+    lo.assign(row, row + n);
+    std::vector<int64_t> deg(n);
+    R.r.assign(n, 1);
+    R.ff.assign(n, 0);
+    R.parent.assign(n, -1);
+    R.folded.assign(n, 0);
+    std::vector<uint8_t> hub(n, 0);
+    std::vector<int32_t> q;
+    q.reserve(n);
+    for (int32_t v = 0; v < n; v++) {
+        deg[v] = row[v + 1] - row[v];
+        if (v >= R.start && deg[v] == 1) q.push_back(v);
+    }
+    for (size_t h = 0; h < q.size(); h++) {
+        const int32_t d1 = q[h];
+        if (deg[d1] != 1) continue;           // root of a tree component
+        const int32_t p = livecol[lo[d1]];
+        R.folded[d1] = 1;
+        R.parent[d1] = p;
+        hub[p] = 1;
+        R.r[p] += R.r[d1];
+        R.ff[p] += R.r[d1] + R.ff[d1];
+        for (int64_t e = lo[p]; e < row[p + 1]; e++)
+            if (livecol[e] == d1) { std::swap(livecol[e], livecol[lo[p]]); break; }
+        lo[p]++;
+        deg[d1] = 0;
+        if (--deg[p] == 1) q.push_back(p);
+        R.fold_order.push_back(d1);
+    }
+    R.n_hub = 0;
+    for (int32_t v = R.start; v < n; v++) R.n_hub += (hub[v] && !R.folded[v]);
+}
+
+// ----------------------------------------------------- blocks (Tarjan) ----
+static gbc_status split(const int64_t* row, Reduction& R, const std::vector<int32_t>& lc, const std::vector<int64_t>& lo) {
+    const int32_t n = R.n;
+    std::vector<int32_t> disc(n, 0), low(n, 0), nchild(n, 0);
+    std::vector<int64_t> it(n), pedge(n, -1);
+    std::vector<int32_t> par(n, -1), stk;
+    std::vector<std::pair<int32_t, int32_t>> es;   // edge stack
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> block_edges;
+    std::vector<std::vector<int32_t>> block_verts;
+    R.is_ap.assign(n, 0);
+    R.comp.assign(n, -1);
+    std::vector<int32_t> mark(n, -1);
+    int32_t timer = 0;
+    auto close_block = [&](int32_t v, int32_t u) {
+        std::vector<std::pair<int32_t, int32_t>> edges;
+        std::vector<int32_t> verts;
+        const int32_t b = (int32_t)block_edges.size();
+        while (!es.empty()) {
+            auto e = es.back();
+            es.pop_back();
+            edges.push_back(e);
+            for (int32_t x : {e.first, e.second})
+                if (mark[x] != b) { mark[x] = b; verts.push_back(x); }
+            if (e.first == v && e.second == u) break;
+        }
+        std::sort(verts.begin(), verts.end());
+        block_edges.push_back(std::move(edges));
+        block_verts.push_back(std::move(verts));
+    };
+    for (int32_t rt = R.start; rt < n; rt++) {
+        if (R.folded[rt] || disc[rt]) continue;
+        const int32_t c = R.n_comp++;
+        R.comp_w.push_back(0);
+        if (lo[rt] == row[rt + 1]) {   // isolated alive vertex: a block of its own
+            disc[rt] = ++timer;
+            R.comp[rt] = c;
+            R.comp_w[c] += R.r[rt];
+            block_edges.emplace_back();
+            block_verts.push_back({rt});
+            mark[rt] = (int32_t)block_verts.size() - 1;
+            continue;
+        }
+        stk.clear();
+        stk.push_back(rt);
+        disc[rt] = low[rt] = ++timer;
+        it[rt] = lo[rt];
+        R.comp[rt] = c;
+        R.comp_w[c] += R.r[rt];
+        while (!stk.empty()) {
+            const int32_t v = stk.back();
+            if (it[v] < row[v + 1]) {
+                const int64_t e = it[v]++;
+                const int32_t u = lc[e];
+                if (u == v) continue;
+                if (!disc[u]) {
+                    par[u] = v;
+                    pedge[u] = e;
+                    disc[u] = low[u] = ++timer;
+                    it[u] = lo[u];
+                    R.comp[u] = c;
+                    R.comp_w[c] += R.r[u];
+                    nchild[v]++;
+                    es.push_back({v, u});
+                    stk.push_back(u);
+                } else if (disc[u] < disc[v]) {
+                    // back edge (the tree edge to the parent is skipped by position,
+                    // so a parallel edge to the parent counts as a back edge)
+                    bool is_tree = (u == par[v]);
+                    if (is_tree) {
+                        // find whether e is the reverse of the tree edge: the first
+                        // occurrence of par[v] in v's live list is treated as it
+                        int64_t first = -1;
+                        for (int64_t f = lo[v]; f < row[v + 1]; f++) if (lc[f] == u) { first = f; break; }
+                        is_tree = (first == e);
+                    }
+                    if (!is_tree) {
+                        es.push_back({v, u});
+                        low[v] = std::min(low[v], disc[u]);
+                    }
+                }
+            } else {
+                stk.pop_back();
+                const int32_t p = par[v];
+                if (p >= 0) {
+                    low[p] = std::min(low[p], low[v]);
+                    if (low[v] >= disc[p]) {
+                        if (par[p] >= 0 || nchild[p] > 1) R.is_ap[p] = 1;
+                        close_block(p, v);
+                    }
+                }
+            }
+        }
+    }
+    // slots: blocks in order, vertices sorted within a block
+    R.n_blocks = (int32_t)block_verts.size();
+    R.bvoff.assign(R.n_blocks + 1, 0);
+    for (int32_t b = 0; b < R.n_blocks; b++) R.bvoff[b + 1] = R.bvoff[b] + (int64_t)block_verts[b].size();
+    const int64_t ns = R.bvoff[R.n_blocks];
+    if (ns >= ((int64_t)1 << 27)) { set_error("block graph too large (%lld slots)", (long long)ns); return GBC_ERR_ARG; }
+    R.slot_v.resize(ns);
+    R.vslot.assign(n, -1);
+    R.max_block = 0;
+    for (int32_t b = 0; b < R.n_blocks; b++) {
+        R.max_block = std::max<int32_t>(R.max_block, (int32_t)block_verts[b].size());
+        for (size_t i = 0; i < block_verts[b].size(); i++) {
+            const int32_t v = block_verts[b][i];
+            R.slot_v[R.bvoff[b] + i] = v;
+            if (R.vslot[v] < 0) R.vslot[v] = (int32_t)(R.bvoff[b] + i);
+        }
+    }
+    // block graph CSR over slots
+    auto slot_of = [&](int32_t b, int32_t v) -> int32_t {
+        const auto& V = block_verts[b];
+        return (int32_t)(R.bvoff[b] + (std::lower_bound(V.begin(), V.end(), v) - V.begin()));
+    };
+    std::vector<int64_t> deg(ns + 1, 0);
+    for (int32_t b = 0; b < R.n_blocks; b++)
+        for (auto& e : block_edges[b]) { deg[slot_of(b, e.first)]++; deg[slot_of(b, e.second)]++; }
+    R.bg.n = (int32_t)ns;
+    R.bg.row.assign(ns + 1, 0);
+    for (int64_t s = 0; s < ns; s++) R.bg.row[s + 1] = R.bg.row[s] + deg[s];
+    R.bg.col.resize(R.bg.row[ns]);
+    std::vector<int64_t> fill(R.bg.row.begin(), R.bg.row.end() - 1);
+    for (int32_t b = 0; b < R.n_blocks; b++)
+        for (auto& e : block_edges[b]) {
+            const int32_t x = slot_of(b, e.first), y = slot_of(b, e.second);
+            R.bg.col[fill[x]++] = y;
+            R.bg.col[fill[y]++] = x;
+        }
+    // block-cut tree: BFS over blocks / APs from the first block of each component
+    R.ap_index.assign(n, -1);
+    int32_t nap = 0;
+    for (int32_t v = 0; v < n; v++) if (R.is_ap[v]) R.ap_index[v] = nap++;
+    std::vector<std::vector<int32_t>> ap_blocks(nap);
+    for (int32_t b = 0; b < R.n_blocks; b++)
+        for (int32_t v : block_verts[b]) if (R.is_ap[v]) ap_blocks[R.ap_index[v]].push_back(b);
+    R.bparent_ap.assign(R.n_blocks, -2);
+    R.ap_parent_block.assign(n, -1);
+    R.ap_child_blocks.assign(nap, {});
+    R.border.clear();
+    for (int32_t b0 = 0; b0 < R.n_blocks; b0++) {
+        if (R.bparent_ap[b0] != -2) continue;
+        R.bparent_ap[b0] = -1;
+        size_t h = R.border.size();
+        R.border.push_back(b0);
+        while (h < R.border.size()) {
+            const int32_t b = R.border[h++];
+            for (int32_t v : block_verts[b]) {
+                if (!R.is_ap[v] || v == R.bparent_ap[b]) continue;
+                R.ap_parent_block[v] = b;
+                for (int32_t b2 : ap_blocks[R.ap_index[v]]) {
+                    if (b2 == b) continue;
+                    R.bparent_ap[b2] = v;
+                    R.ap_child_blocks[R.ap_index[v]].push_back(b2);
+                    R.border.push_back(b2);
+                }
+            }
+        }
+    }
+    // clone weights: W_sub bottom-up, then w' per slot
+    std::vector<int64_t> wsub(R.n_blocks, 0);
+    for (int64_t h = (int64_t)R.border.size() - 1; h >= 0; h--) {
+        const int32_t b = R.border[h];
+        int64_t s = 0;
+        for (int32_t v : block_verts[b]) {
+            if (v == R.bparent_ap[b]) continue;
+            s += R.r[v];
+            if (R.is_ap[v]) for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) s += wsub[b2];
+        }
+        wsub[b] = s;
+    }
+    R.slot_w.resize(ns);
+    for (int32_t b = 0; b < R.n_blocks; b++) {
+        for (size_t i = 0; i < block_verts[b].size(); i++) {
+            const int32_t v = block_verts[b][i];
+            int64_t w = R.r[v];
+            if (R.is_ap[v]) {
+                if (v == R.bparent_ap[b]) w = R.comp_w[R.comp[v]] - wsub[b];
+                else for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) w += wsub[b2];
+            }
+            if (w > INT32_MAX) { set_error("clone weight exceeds int32"); return GBC_ERR_ARG; }
+            R.slot_w[R.bvoff[b] + i] = (int32_t)w;
+        }
+    }
+    return GBC_OK;
+}
+
+static gbc_status upload(Reduction& R) {
+    if (R.dg) return GBC_OK;
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+    auto g = std::make_unique<DevGraph>();
+    g->n = R.bg.n;
+    g->m = R.bg.m();
+    bool ok = cudaMalloc(&g->row, sizeof(int64_t) * (g->n + 1)) == cudaSuccess;
+    ok &= cudaMalloc(&g->col, sizeof(int32_t) * std::max<int64_t>(g->m, 1)) == cudaSuccess;
+    ok &= cudaMalloc(&R.d_w, sizeof(int32_t) * std::max<int32_t>(g->n, 1)) == cudaSuccess;
+    if (!ok) { cudaGetLastError(); set_error("block graph allocation"); cudaFree(g->row); cudaFree(g->col); return GBC_ERR_NOMEM; }
+    GBC_CUDA(cudaMemcpy(g->row, R.bg.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
+    if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.bg.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
+    GBC_CUDA(cudaMemcpy(R.d_w, R.slot_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
+    g->w = R.d_w;
+    g->ff = nullptr;
+    R.dg = std::move(g);
+    return GBC_OK;
+}
+
+// D_B(slot) for every slot, by the lane engine over the block graph.
+static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<int64_t>& D) {
+    GBC_TRY(upload(R));
+    const int32_t ns = R.bg.n;
+    D.assign(ns, 0);
+    if (ns == 0) return GBC_OK;
+    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + 31) / 32) * 32);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(ns, lanes, false) > fr / 2) lanes -= 32;
+    if (!R.eng || R.eng->lanes() != lanes) {
+        R.eng = std::make_unique<LaneEngine>();
+        GBC_TRY(R.eng->init(R.dg.get(), lanes, false, o.sparse_lanes, o.levels_per_graph, R.stream));
+    }
+    int32_t* d_src = nullptr;
+    unsigned long long* d_cc = nullptr;
+    if (cudaMalloc(&d_src, sizeof(int32_t) * ns) != cudaSuccess || cudaMalloc(&d_cc, sizeof(unsigned long long) * ns) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_src);
+        set_error("slot buffers");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_cc, [](void* p) { cudaFree(p); });
+    std::vector<int32_t> src(ns);
+    for (int32_t i = 0; i < ns; i++) src[i] = i;
+    GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, R.stream));
+    LaneResult res;
+    for (int32_t b0 = 0; b0 < ns; b0 += lanes) {
+        LaneRequest rq;
+        rq.job = LaneJob::CC;
+        rq.d_src = d_src + b0;
+        rq.kb = std::min(lanes, ns - b0);
+        rq.d_cc = d_cc + b0;
+        GBC_TRY(R.eng->run(rq, res));
+    }
+    GBC_CUDA(cudaMemcpyAsync(D.data(), d_cc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, R.stream));
+    GBC_CUDA(cudaStreamSynchronize(R.stream));
+    return GBC_OK;
+}
+
+// Host DP over the block-cut tree, then recovery of the folded vertices.
+static gbc_status assemble_cc(Reduction& R, const std::vector<int64_t>& D, int64_t* cc) {
+    const int32_t n = R.n, nb = R.n_blocks;
+    auto slot_of = [&](int32_t b, int32_t v) -> int64_t {
+        auto first = R.slot_v.begin() + R.bvoff[b], last = R.slot_v.begin() + R.bvoff[b + 1];
+        return std::lower_bound(first, last, v) - R.slot_v.begin();
+    };
+    const int32_t nap = (int32_t)R.ap_child_blocks.size();
+    std::vector<int64_t> base(nb, 0), xdown(nap, 0), sdown(nb, 0), xup(nb, 0), FF(nb, 0);
+    for (int32_t b = 0; b < nb; b++)
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) base[b] += R.ff[R.slot_v[s]];
+    // down: S_B(p) = base(B) - ff[p] + sum_{child APs c of B} X_down(c) + D_B(p)
+    for (int64_t h = (int64_t)R.border.size() - 1; h >= 0; h--) {
+        const int32_t b = R.border[h];
+        int64_t xs = 0;
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) {
+            const int32_t v = R.slot_v[s];
+            if (R.is_ap[v] && v != R.bparent_ap[b]) xs += xdown[R.ap_index[v]];
+        }
+        const int32_t p = R.bparent_ap[b];
+        if (p >= 0) {
+            sdown[b] = base[b] - R.ff[p] + xs + D[slot_of(b, p)];
+            xdown[R.ap_index[p]] += sdown[b];
+        }
+        FF[b] = base[b] + xs;   // completed with the up term below
+    }
+    // up: X_up(B) = S_P(p) + X_down(p) - S_B(p) with S_P(p) = FF_P - ff[p] - X_down(p) + D_P(p)
+    for (size_t h = 0; h < R.border.size(); h++) {
+        const int32_t b = R.border[h];
+        const int32_t p = R.bparent_ap[b];
+        if (p >= 0) {
+            const int32_t P = R.ap_parent_block[p];
+            const int64_t xd = xdown[R.ap_index[p]];
+            const int64_t sP = FF[P] - R.ff[p] - xd + D[slot_of(P, p)];
+            xup[b] = sP + xd - sdown[b];
+            FF[b] += xup[b];
+        }
+    }
+    for (int32_t v = 0; v < n; v++) cc[v] = 0;
+    for (int32_t b = 0; b < nb; b++)
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) {
+            const int32_t v = R.slot_v[s];
+            const int64_t val = FF[b] + D[s];
+            if (R.vslot[v] == s) cc[v] = val;
+            else if (cc[v] != val) {
+                set_error("internal: closeness of articulation point %d differs between blocks (%lld vs %lld)", v,
+                          (long long)cc[v], (long long)val);
+                return GBC_ERR_LIMIT;
+            }
+        }
+    // folded vertices, reverse folding order
+    for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
+        const int32_t d1 = R.fold_order[i];
+        const int64_t Nc = R.comp_w[R.comp[d1]];
+        cc[d1] = cc[R.parent[d1]] + Nc - 2 * R.r[d1];
+    }
+    return GBC_OK;
+}
+
+}  // namespace gbc
+
+using namespace gbc;
+
+struct gbc_reduced_s {
+    Reduction R;
+};
+
+extern "C" {
+
+gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out) {
+    if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    GBC_TRY(validate_csr(row, col, n));
+    if (start < 0 || start > 1 || start >= n) { set_error("start must be 0 or 1"); return GBC_ERR_ARG; }
+    if (start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
+    for (int32_t v = 0; v < n; v++)
+        for (int64_t e = row[v]; e < row[v + 1]; e++)
+            if (col[e] == v) { set_error("self-loop at vertex %d", v); return GBC_ERR_ARG; }
+    auto H = std::make_unique<gbc_reduced_s>();
+    Reduction& R = H->R;
+    R.n = n;
+    R.start = start;
+    std::vector<int32_t> lc;
+    std::vector<int64_t> lo;
+    fold(row, col, R, lc, lo);
+    GBC_TRY(split(row, R, lc, lo));
+    // components of folded vertices follow their root
+    for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
+        const int32_t d1 = R.fold_order[i];
+        R.comp[d1] = R.comp[R.parent[d1]];
+    }
+    *out = H.release();
+    return GBC_OK;
+}
+
+gbc_status gbc_reduced_info_get(gbc_reduced h, gbc_reduced_info* info) {
+    if (!h || !info) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    const Reduction& R = h->R;
+    std::memset(info, 0, sizeof *info);
+    info->n = R.n;
+    info->d1_folded = (int32_t)R.fold_order.size();
+    info->d1_hubs = R.n_hub;
+    info->alive = (R.n - R.start) - info->d1_folded;
+    int32_t ap = 0;
+    for (uint8_t a : R.is_ap) ap += a;
+    info->articulation_points = ap;
+    info->blocks = R.n_blocks;
+    info->max_block = R.max_block;
+    info->block_slots = R.bg.n;
+    info->block_edges = R.bg.m();
+    info->components = R.n_comp;
+    return GBC_OK;
+}
+
+gbc_status gbc_cc_reduced(gbc_reduced h, const gbc_options* opt, int64_t* cc) {
+    if (!h || !cc) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(h->R.mu);
+    gbc_options o;
+    gbc_options_default(&o);
+    if (opt) o = *opt;
+    if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("bad lanes"); return GBC_ERR_ARG; }
+    std::vector<int64_t> D;
+    GBC_TRY(weighted_sums(h->R, o, D));
+    return assemble_cc(h->R, D, cc);
+}
+
+gbc_status gbc_bc_reduced(gbc_reduced h, const gbc_options* opt, double* bc) {
+    (void)opt;
+    if (!h || !bc) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    set_error("betweenness through the reduction is not available yet");
+    return GBC_ERR_ARG;
+}
+
+gbc_status gbc_reduced_block_graph(gbc_reduced h, int64_t** row, int32_t** col, int32_t** weight, int32_t* n_slots) {
+    if (!h || !row || !col || !weight || !n_slots) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    const Reduction& R = h->R;
+    GBC_TRY(export_csr(R.bg, row, col));
+    *weight = (int32_t*)malloc(sizeof(int32_t) * std::max<int32_t>(R.bg.n, 1));
+    if (!*weight) { free(*row); free(*col); set_error("host allocation"); return GBC_ERR_NOMEM; }
+    if (R.bg.n) std::memcpy(*weight, R.slot_w.data(), sizeof(int32_t) * R.bg.n);
+    *n_slots = R.bg.n;
+    return GBC_OK;
+}
+
+gbc_status gbc_reduced_assemble_cc(gbc_reduced h, const int64_t* D, int64_t* cc) {
+    if (!h || (!D && h->R.bg.n) || !cc) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::vector<int64_t> d(D, D + h->R.bg.n);
+    return assemble_cc(h->R, d, cc);
+}
+
+gbc_status gbc_reduced_destroy(gbc_reduced h) {
+    if (!h) { set_error("NULL handle"); return GBC_ERR_ARG; }
+    delete h;
+    return GBC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,231 @@
+/*
+ * gbc.h -- native C ABI of libgbc, a GB300 (sm_103a) implementation of the
+ * XPPGX/BC centrality path: Brandes betweenness centrality and closeness
+ * (distance-sum) centrality on undirected, unweighted graphs, with the
+ * degree-1 folding and articulation-point reductions.
+ *
+ * Plain pointers and sizes only.  Every call returns a gbc_status; on error
+ * gbc_last_error() gives a message for the calling thread.  Host-buffer
+ * entry points copy inputs to the device and results back; *_device entry
+ * points take device pointers and a cudaStream_t (passed as void*).
+ *
+ * Reference interfaces replaced (paths within the XPPGX/BC project):
+ *   gbc_bc          <- void computeBC(struct CSR*, float*)       Seq_Brandes/Brandes.c:224
+ *   gbc_cc          <- int* computeCC(struct CSR*, int*)         Seq_CC/CC.cpp:37
+ *   gbc_cc_reduced  <- void compute_D1_AP_CC_shareBased_DegreeOrder(struct CSR*, int*)
+ *                                                                Seq_CC/CC.cpp:1728
+ *   gbc_reduce_*    <- D1Folding (Lib/D1Process/D1Process.c:5), AP_detection /
+ *                      AP_Copy_And_Split / rebuildGraph (Lib/AP_Process/AP_Process.c:6,468,1141)
+ *   gbc_bc_plain / gbc_cc_plain (one source at a time) <- the reference's GPU
+ *                      programs' per-source level loop (GPU_FAN/gpu_fan.cu:59,
+ *                      parallel_CC/para_CC.cu:61)
+ * The struct-CSR drop-in names themselves are declared in gbc_compat.h.
+ */
+#ifndef GBC_H
+#define GBC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBC_OK = 0,
+    GBC_ERR_ARG = 1,        /* invalid argument (size, index, pointer, option) */
+    GBC_ERR_CUDA = 2,       /* CUDA runtime error */
+    GBC_ERR_NOMEM = 3,      /* device or host allocation failed / over budget */
+    GBC_ERR_OVERFLOW = 4,   /* exact uint64 path counts overflowed (GBC_SIGMA_EXACT) */
+    GBC_ERR_LIMIT = 5,      /* a device-side cap was hit (levels, queue capacity) */
+    GBC_ERR_NOT_FOUND = 6,  /* unknown handle / graph id */
+    GBC_ERR_BUSY = 7,       /* admission refused: no room for the request now */
+    GBC_ERR_TIMEOUT = 8,    /* request deadline passed */
+    GBC_ERR_NO_DEVICE = 9   /* no usable CUDA device */
+} gbc_status;
+
+/* Betweenness semantics. */
+enum {
+    GBC_BC_BRANDES = 0,     /* textbook: delta_s(w) added once per source */
+    GBC_BC_REFERENCE = 1    /* XPPGX/BC: delta_s(w) added once per shortest-path
+                               predecessor of w (Seq_Brandes/Brandes.c:319-326) */
+};
+/* Precision of the dependency (delta) sweep; BC sums across sources are FP64. */
+enum { GBC_DELTA_F32 = 0, GBC_DELTA_F64 = 1 };
+/* Path-count (sigma) representation. */
+enum {
+    GBC_SIGMA_AUTO = 0,     /* exact uint64; on overflow re-run the batch in LOG form */
+    GBC_SIGMA_EXACT = 1,    /* exact uint64; overflow is an error (GBC_ERR_OVERFLOW) */
+    GBC_SIGMA_LOG = 2       /* log2(sigma) in FP64: any magnitude, ~1e-13 relative */
+};
+/* Engine. */
+enum {
+    GBC_ENGINE_AUTO = 0,
+    GBC_ENGINE_PLAIN = 1,   /* one source at a time, host-driven level loop */
+    GBC_ENGINE_LANES = 2    /* batched multi-source lanes, graph-captured level loop */
+};
+
+typedef struct {
+    int32_t semantics;        /* GBC_BC_* (default GBC_BC_BRANDES) */
+    int32_t delta_precision;  /* GBC_DELTA_* (default GBC_DELTA_F64) */
+    int32_t sigma_mode;       /* GBC_SIGMA_* (default AUTO) */
+    int32_t engine;           /* GBC_ENGINE_* (default AUTO = LANES) */
+    int32_t lanes;            /* sources per batch, multiple of 32 in [32,1024]; 0 = autotune */
+    int32_t sparse_lanes;     /* a frontier task with <= this many active lanes expands
+                                 edge-parallel, otherwise lane-parallel; -1 = autotune */
+    int32_t levels_per_graph; /* level kernels per captured CUDA graph; 0 = default */
+    int32_t reserved[9];
+} gbc_options;
+
+typedef struct {
+    int64_t sources;          /* sources processed by the last call */
+    int64_t batches;          /* lane batches */
+    int64_t levels;           /* BFS levels summed over batches (forward) */
+    int64_t kernel_launches;  /* kernels launched by the library in the last call */
+    int64_t graph_launches;   /* CUDA graph launches in the last call */
+    int64_t edges_traversed;  /* sum over sources of undirected edges in the source's component */
+    int64_t frontier_entries; /* (vertex, lane-group) frontier entries over all levels */
+    int64_t sigma_overflow_lanes; /* lanes whose exact sigma overflowed (before any LOG re-run) */
+    double  kernel_ms;        /* device time of the traversal kernels (CUDA events) */
+    double  total_ms;         /* wall time of the call */
+    int32_t lanes;            /* lanes per batch actually used */
+    int32_t sigma_mode_used;  /* GBC_SIGMA_EXACT or GBC_SIGMA_LOG */
+    int32_t reserved[8];
+} gbc_run_stats;
+
+typedef struct gbc_graph_s* gbc_graph;
+
+void gbc_options_default(gbc_options* opt);
+const char* gbc_last_error(void);
+const char* gbc_version(void);
+/* Number of CUDA devices visible (0 when none; never fails). */
+int gbc_device_count(void);
+
+/* ---- device-resident graphs ------------------------------------------- */
+/* Upload an undirected CSR (both directions of every edge present):
+ * row[n+1] int64 offsets, col[row[n]] int32 neighbour ids in [0,n).
+ * No self-loops are expected; duplicates count as parallel edges. */
+gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, gbc_graph* out);
+/* Same, from device pointers (copied; the caller keeps ownership). */
+gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, int32_t n,
+                                   int64_t m_directed, gbc_graph* out);
+gbc_status gbc_graph_destroy(gbc_graph g);
+gbc_status gbc_graph_info(gbc_graph g, int32_t* n, int64_t* m_directed, size_t* device_bytes);
+/* Statistics of the last compute call on this graph. */
+gbc_status gbc_graph_last_stats(gbc_graph g, gbc_run_stats* st);
+
+/* ---- betweenness --------------------------------------------------------
+ * bc[n] (host) receives sum over the k sources of the per-source
+ * dependencies, under opt->semantics; k = 0 with sources = NULL means all
+ * n vertices.  Unnormalised: ordered source/target pairs, as the reference. */
+gbc_status gbc_bc(gbc_graph g, const int32_t* sources, int32_t k, const gbc_options* opt, double* bc);
+gbc_status gbc_bc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const gbc_options* opt,
+                         double* d_bc, void* stream);
+
+/* ---- closeness (distance sums) -----------------------------------------
+ * cc[i] = sum of hop distances from sources[i] to every vertex it reaches
+ * (Seq_CC/CC.cpp:76-100); k = 0 with sources = NULL means all n vertices. */
+gbc_status gbc_cc(gbc_graph g, const int32_t* sources, int32_t k, const gbc_options* opt, int64_t* cc);
+gbc_status gbc_cc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const gbc_options* opt,
+                         int64_t* d_cc, void* stream);
+
+/* ---- per-source distances and exact path counts (parity surface) -------
+ * dist[k*n] int32 (-1 unreachable), sigma[k*n] uint64 exact, ovf[k] = 1
+ * when that source's counts overflowed uint64 (its sigma row is then
+ * invalid).  Any pointer may be NULL. */
+gbc_status gbc_sssp(gbc_graph g, const int32_t* sources, int32_t k, const gbc_options* opt,
+                    int32_t* dist, uint64_t* sigma, uint8_t* ovf);
+
+/* ---- D1 folding + articulation-point (block) reduction ---------------- */
+typedef struct gbc_reduced_s* gbc_reduced;
+typedef struct {
+    int32_t n;                 /* vertex slots of the input */
+    int32_t d1_folded;         /* degree-1 vertices folded (D1Process.c:71) */
+    int32_t d1_hubs;           /* unfolded vertices that absorbed a folded vertex */
+    int32_t alive;             /* vertices left after folding */
+    int32_t articulation_points;
+    int32_t blocks;            /* biconnected blocks (incl. bridges) of the folded graph */
+    int32_t max_block;         /* vertices in the largest block */
+    int32_t block_slots;       /* vertex slots of the block graph (APs counted once per block) */
+    int64_t block_edges;       /* directed CSR entries of the block graph */
+    int32_t components;        /* connected components of the input (isolated slots included) */
+    int32_t reserved[7];
+} gbc_reduced_info;
+
+/* Fold and split a host CSR (vertex slots [start, n) are real vertices;
+ * start = 1 marks the reference's phantom slot 0 of 1-based inputs). */
+gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out);
+gbc_status gbc_reduced_info_get(gbc_reduced r, gbc_reduced_info* info);
+/* Closeness of every vertex slot through the reduction: cc[n] (host).
+ * Equal to gbc_cc over all vertices of the unreduced graph. */
+gbc_status gbc_cc_reduced(gbc_reduced r, const gbc_options* opt, int64_t* cc);
+/* Betweenness of every vertex slot through D1 folding (GBC_BC_BRANDES only):
+ * sources are the unfolded vertices weighted by their reach. */
+gbc_status gbc_bc_reduced(gbc_reduced r, const gbc_options* opt, double* bc);
+gbc_status gbc_reduced_destroy(gbc_reduced r);
+/* The block graph the reduction hands to the device: slot CSR (malloc'd,
+ * free with gbc_free) and per-slot clone weights w'. */
+gbc_status gbc_reduced_block_graph(gbc_reduced r, int64_t** row, int32_t** col, int32_t** weight, int32_t* n_slots);
+/* Host assembly step: given D[s] = sum_u d(s,u) * w'(u) for every slot s of
+ * the block graph, write the closeness of every vertex slot to cc[n]. */
+gbc_status gbc_reduced_assemble_cc(gbc_reduced r, const int64_t* D, int64_t* cc);
+
+/* ---- synthetic graphs (host CSR, malloc'd; free with gbc_free) --------
+ * All generators are deterministic for a seed on any host. */
+gbc_status gbc_gen_ba(int32_t n, int32_t m, uint64_t seed, int64_t** row, int32_t** col);
+gbc_status gbc_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed,
+                        int32_t permute, int64_t** row, int32_t** col, int32_t* n);
+gbc_status gbc_gen_grid(int32_t rows, int32_t cols, double remove_frac, uint64_t seed, int32_t largest_only,
+                        int64_t** row, int32_t** col, int32_t* n);
+gbc_status gbc_gen_er(int32_t n, double avg_degree, uint64_t seed, int64_t** row, int32_t** col);
+/* Attach `trees` pendant paths of length 1..max_depth (uniform) to uniformly
+ * chosen vertices of a CSR; returns a new CSR. */
+gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, int32_t trees, int32_t max_depth,
+                            uint64_t seed, int64_t** row_out, int32_t** col_out, int32_t* n_out);
+/* Edge-list text file (header "n m", then "u v" lines; 0- or 1-based as in
+ * Lib/AdjList/AdjList.c:13) -> CSR over n (0-based) or n+1 (1-based) slots;
+ * *start = 0 or 1.  Neighbours ordered by neighbour degree ascending. */
+gbc_status gbc_read_edgelist(const char* path, int64_t** row, int32_t** col, int32_t* n, int32_t* start);
+void gbc_free(void* p);
+
+/* ---- serving: continuous batching over device-resident graphs ---------
+ * A server owns a set of registered graphs and a worker thread.  Requests
+ * (exact CC, exact BC, or k-source sampled BC) are admitted while their lane
+ * state fits the HBM budget; sources of concurrent requests on the same graph
+ * share lane batches.  Results are identical (FP64 tolerance) alone and
+ * mixed. */
+typedef struct gbc_server_s* gbc_server;
+enum { GBC_Q_CC = 0, GBC_Q_BC = 1, GBC_Q_BC_SAMPLED = 2 };
+enum { GBC_REQ_QUEUED = 0, GBC_REQ_RUNNING = 1, GBC_REQ_DONE = 2, GBC_REQ_FAILED = 3, GBC_REQ_CANCELLED = 4 };
+
+typedef struct {
+    size_t  hbm_budget_bytes;   /* lane-state budget; 0 = 50% of free device memory */
+    int32_t max_lanes;          /* lanes per shared batch (multiple of 32), 0 = 1024 */
+    int32_t max_inflight;       /* requests admitted at once, 0 = 64 */
+    int32_t reserved[8];
+} gbc_server_config;
+
+gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out);
+gbc_status gbc_server_destroy(gbc_server s);
+/* Register a host CSR; the server keeps it resident.  *graph_id out. */
+gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t* col, int32_t n, int32_t* graph_id);
+/* Submit a query.  kind GBC_Q_*; for GBC_Q_BC_SAMPLED, k sources drawn
+ * uniformly with the seed.  deadline_ms <= 0 means none.  *req_id out. */
+gbc_status gbc_server_submit(gbc_server s, int32_t graph_id, int32_t kind, int32_t k, uint64_t seed,
+                             const gbc_options* opt, double deadline_ms, int64_t* req_id);
+/* Poll: *state = GBC_REQ_*; when DONE, result buffers may be fetched. */
+gbc_status gbc_server_poll(gbc_server s, int64_t req_id, int32_t* state);
+/* Block until the request finishes (timeout_ms <= 0: no timeout). */
+gbc_status gbc_server_wait(gbc_server s, int64_t req_id, double timeout_ms, int32_t* state);
+/* Copy the result: BC kinds fill bc[n]; CC fills cc[n]. Latency in ms
+ * from submit to completion goes to *latency_ms. Frees the request. */
+gbc_status gbc_server_fetch(gbc_server s, int64_t req_id, double* bc, int64_t* cc, double* latency_ms);
+gbc_status gbc_server_cancel(gbc_server s, int64_t req_id);
+/* Aggregate counters: completed requests, lane batches, shared batches
+ * (batches that carried sources of more than one request), edges traversed. */
+gbc_status gbc_server_counters(gbc_server s, int64_t* completed, int64_t* batches, int64_t* shared_batches,
+                               int64_t* edges_traversed, double* busy_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

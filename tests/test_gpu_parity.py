@@ -1,0 +1,138 @@
+"""GPU parity: the CUDA engines (through the C ABI) against the CPU oracle.
+
+Bars: distances, exact uint64 path counts and closeness sums bit-exact;
+betweenness within 1e-9 relative (FP64 delta) or 1e-6 relative (FP32 delta)
+of the FP64 oracle, measured as max |a-b| / max(|b|, 1) over vertices.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64 = 1e-9
+TOL_F32 = 1e-6
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0))) if len(b) else 0.0
+
+
+def to_orc(orc, csr):
+    return orc.Graph(csr.row, csr.col, csr.start)
+
+
+@pytest.fixture(scope="module")
+def graphs(gpu, datasets):
+    g = {}
+    g["ba4096"] = gpu.gen_ba(4096, 4, 1)
+    g["rmat12"] = gpu.gen_rmat(12, 8, seed=2)
+    g["grid24"] = gpu.gen_grid(24, 24, 0.05, seed=3)
+    g["er2k"] = gpu.gen_er(2000, 3.0, seed=4)          # disconnected
+    g["karate"] = gpu.read_edgelist(datasets["karate.txt"])
+    g["ia-fb"] = gpu.read_edgelist(datasets["ia-fb-messages.mtx"])
+    return g
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "grid24", "er2k", "karate"])
+@pytest.mark.parametrize("lanes", [32, 128])
+def test_sssp_bit_exact(gpu, orc, graphs, name, lanes):
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    rng = np.random.default_rng(7)
+    src = rng.integers(csr.start, csr.n, size=min(70, csr.n - csr.start)).astype(np.int32)
+    with gpu.Graph(csr) as G:
+        dist, sig, ovf = G.sssp(src, lanes=lanes)
+    for i, s in enumerate(src):
+        d0, s0, o0, _ = orc.sssp(og, int(s))
+        assert np.array_equal(dist[i], d0), f"dist mismatch for source {s}"
+        assert bool(ovf[i]) == bool(o0.any())
+        if not o0.any():
+            assert np.array_equal(sig[i], s0), f"sigma mismatch for source {s}"
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "ia-fb"])
+def test_cc_bit_exact(gpu, orc, graphs, name):
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    ref = orc.cc(og, src, nthreads=4)
+    with gpu.Graph(csr) as G:
+        got = G.cc(src)
+        assert np.array_equal(got, ref)
+        got_plain = G.cc(src[:50], engine=gpu.ENGINE_PLAIN)
+        assert np.array_equal(got_plain, ref[:50])
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate"])
+@pytest.mark.parametrize("sem", [0, 1])
+def test_bc_fp64(gpu, orc, graphs, name, sem):
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    ref, novf = orc.bc(og, src, semantics=sem, nthreads=4)
+    assert novf == 0
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, semantics=sem, delta_precision=gpu.DELTA_F64, sigma_mode=gpu.SIGMA_EXACT)
+        assert relerr(got, ref) < TOL_F64
+        st = G.stats()
+        assert st["sources"] == len(src) and st["sigma_mode_used"] == gpu.SIGMA_EXACT
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12"])
+def test_bc_fp32_delta(gpu, orc, graphs, name):
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    ref, _ = orc.bc(og, src, nthreads=4)
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, delta_precision=gpu.DELTA_F32)
+    assert relerr(got, ref) < TOL_F32
+
+
+def test_bc_plain_engine(gpu, orc, graphs):
+    csr = graphs["rmat12"]
+    og = to_orc(orc, csr)
+    src = np.arange(0, 64, dtype=np.int32)
+    ref, _ = orc.bc(og, src)
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, engine=gpu.ENGINE_PLAIN)
+    assert relerr(got, ref) < TOL_F64
+
+
+def test_bc_sampled_sources_and_duplicates(gpu, orc, graphs):
+    csr = graphs["ba4096"]
+    og = to_orc(orc, csr)
+    rng = np.random.default_rng(3)
+    src = rng.integers(0, csr.n, size=300).astype(np.int32)   # with repeats
+    ref, _ = orc.bc(og, src, semantics=1)
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, semantics=1, lanes=64)
+    assert relerr(got, ref) < TOL_F64
+
+
+def test_bc_reference_golden_karate(gpu, graphs):
+    gold = np.loadtxt(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden",
+                                                  "karate_BC_Score.txt"), skiprows=1)
+    csr = graphs["karate"]
+    with gpu.Graph(csr) as G:
+        got = G.bc(np.arange(1, csr.n, dtype=np.int32), semantics=gpu.BC_REFERENCE)
+    # the golden file holds FP32 values printed with %f
+    assert np.max(np.abs(got[1:] - gold) / np.maximum(gold, 1.0)) < 2e-6
+
+
+def test_sigma_overflow_log_mode(gpu, orc):
+    # a full 80x80 grid: corner-to-corner path counts ~C(158,79) > 2^64
+    csr = gpu.gen_grid(80, 80, 0.0, seed=1)
+    og = to_orc(orc, csr)
+    src = np.array([0, 79, 3200, 6399], dtype=np.int32)
+    ref, novf = orc.bc(og, src, scaled=True)
+    assert novf > 0
+    with gpu.Graph(csr) as G:
+        with pytest.raises(gpu.GbcError):
+            G.bc(src, sigma_mode=gpu.SIGMA_EXACT)
+        got = G.bc(src)   # AUTO: exact, then log2 form for overflowing batches
+        st = G.stats()
+        assert st["sigma_mode_used"] == gpu.SIGMA_LOG
+        assert relerr(got, ref) < TOL_F64
+        dist, sig, ovf = G.sssp(src)
+        assert ovf.all()
