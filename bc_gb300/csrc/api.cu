@@ -24,6 +24,7 @@ struct gbc_graph_s {
     int64_t ccb_cap = 0;
     double* d_bc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<int32_t> last_src;
     ~gbc_graph_s() {
         eng.reset();
         cudaFree(g.row);
@@ -73,7 +74,20 @@ gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_g
     GBC_CUDA(cudaMemcpyAsync(g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, G->stream));
     if (g.m) GBC_CUDA(cudaMemcpyAsync(g.col, col, sizeof(int32_t) * g.m, cudaMemcpyHostToDevice, G->stream));
     GBC_CUDA(cudaStreamSynchronize(G->stream));
-    host_components(row, col, n, g);
+    return GBC_OK;
+}
+
+// Component information is needed only for the statistics (edges per
+// source's component); it is computed on first request from a copy of the
+// device CSR, outside the compute calls.
+static gbc_status ensure_components(gbc_graph_s* G) {
+    DevGraph& g = G->g;
+    if (!g.comp.empty()) return GBC_OK;
+    std::vector<int64_t> row(g.n + 1);
+    std::vector<int32_t> col(std::max<int64_t>(g.m, 1));
+    GBC_CUDA(cudaMemcpy(row.data(), g.row, sizeof(int64_t) * (g.n + 1), cudaMemcpyDeviceToHost));
+    if (g.m) GBC_CUDA(cudaMemcpy(col.data(), g.col, sizeof(int32_t) * g.m, cudaMemcpyDeviceToHost));
+    host_components(row.data(), col.data(), g.n, g);
     return GBC_OK;
 }
 
@@ -159,9 +173,12 @@ static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t
     s.total_ms = ms_total;
     s.lanes = lanes;
     s.sigma_mode_used = sigma_used;
-    int64_t e = 0;
-    for (int32_t x : hsrc) e += G->g.comp_edges[G->g.comp[x]];
-    s.edges_traversed = e;
+    s.fwd_ms = r.fwd_ms;
+    s.bwd_ms = r.bwd_ms;
+    s.fwd_kernels = r.fwd_kernels;
+    s.bwd_kernels = r.bwd_kernels;
+    s.edges_traversed = -1;   // filled in lazily by gbc_graph_last_stats
+    G->last_src = hsrc;
 }
 
 // Betweenness over device-staged sources d_src[0..k) into d_bc[n].
@@ -311,6 +328,12 @@ gbc_status gbc_graph_info(gbc_graph G, int32_t* n, int64_t* m, size_t* bytes) {
 gbc_status gbc_graph_last_stats(gbc_graph G, gbc_run_stats* st) {
     if (!G || !st) { set_error("NULL argument"); return GBC_ERR_ARG; }
     std::lock_guard<std::mutex> lk(G->mu);
+    if (G->last.edges_traversed < 0) {
+        GBC_TRY(ensure_components(G));
+        int64_t e = 0;
+        for (int32_t x : G->last_src) e += G->g.comp_edges[G->g.comp[x]];
+        G->last.edges_traversed = e;
+    }
     *st = G->last;
     return GBC_OK;
 }

@@ -62,6 +62,8 @@ struct LaneResult {
     int64_t frontier_entries = 0;
     int64_t kernel_launches = 0;
     int64_t graph_launches = 0;
+    double fwd_ms = 0, bwd_ms = 0;      // device time inside the level-loop graphs
+    int64_t fwd_kernels = 0, bwd_kernels = 0;
 };
 
 class LaneEngine {
@@ -78,6 +80,10 @@ public:
     // BC accumulation across batches: zero the per-group partials / reduce them into d_bc[n].
     gbc_status bc_begin();
     gbc_status bc_finish(double* d_bc);
+    // d_dst: device table of ng device pointers (or null): dst[g][v] += partial of group g.
+    gbc_status bc_scatter(double* const* d_dst);
+    // Per-lane distance sums of the last CC batch (lanes entries) to the host.
+    gbc_status cc_read(unsigned long long* h_cc, int32_t count);
     int32_t lanes() const { return lanes_; }
     bool has_bc() const { return need_bc_; }
     const DevGraph* graph() const { return g_; }
@@ -88,7 +94,8 @@ public:
 private:
     friend struct LaneAccess;
     gbc_status get_graph(int key, cudaGraphExec_t* out);
-    gbc_status alloc_queue(unsigned long long cap);
+    gbc_status alloc_queue(unsigned long long cap, unsigned long long hcap);
+    gbc_status ensure_events(size_t count);
     void release();
 
     const DevGraph* g_ = nullptr;
@@ -97,6 +104,7 @@ private:
     int sparse_ = 2;
     int lpg_ = 16;
     int grid_ = 0;
+    int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
     cudaStream_t stream_ = nullptr;
     size_t bytes_ = 0;
     uint16_t* lvl_ = nullptr;
@@ -106,6 +114,10 @@ private:
     uint32_t* fq_ = nullptr;
     unsigned long long fcap_ = 0;
     unsigned long long* foff_ = nullptr;
+    uint32_t* hq_ = nullptr;              // hub frontier entries
+    unsigned long long hcap_ = 0;
+    unsigned long long* hoff_ = nullptr;
+    int64_t n_hubs_ = 0;
     void* ctl_ = nullptr;
     void* ctl_host_ = nullptr;
     uint32_t* ovf_ = nullptr;
@@ -114,6 +126,7 @@ private:
     struct Captured { int key = -1; cudaGraphExec_t exec = nullptr; };
     std::vector<Captured> graphs_;
     int sm_count_ = 0;
+    std::vector<cudaEvent_t> ev_;       // timing events, two per graph launch
 };
 
 // Plain engine: one source at a time, int32 distances, uint64 sigma, the

@@ -31,19 +31,29 @@ namespace gbc {
 
 namespace {
 
-constexpr uint16_t INF16 = 0xFFFFu;
-constexpr int MAX_LEVEL = 65000;   // lvl is uint16; deeper BFS is reported as GBC_ERR_LIMIT
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int BLOCK = 256;
+constexpr int U = 16;   // neighbours whose lane state is loaded before any of it is used
+
+// Level storage: uint8_t while every BFS stays under 254 levels, uint16_t
+// after a batch went deeper.  All-ones is "unreached".
+template <typename LT>
+struct Lv {
+    static constexpr int INF = (int)(LT)~(LT)0;
+    static constexpr int MAXD = INF - 2;   // deepest level that can still be expanded
+};
 
 struct Ctl {
     int level;
     int maxlevel;
     int done;
-    int err;            // bit0: frontier queue overflow, bit1: level cap
+    int err;            // bit0: a frontier queue overflowed, bit1: level cap of the level type
     unsigned blocks;    // finished-CTA counter of the running launch
     int pad;
-    unsigned long long tail;
+    unsigned long long tail;    // append position, regular queue
+    unsigned long long htail;   // append position, hub queue
+    unsigned long long next;    // fetch position of the running level, regular queue
+    unsigned long long hnext;   // fetch position of the running level, hub queue
 };
 
 struct KArgs {
@@ -53,13 +63,16 @@ struct KArgs {
     int ng;
     const int32_t* w;      // nullable vertex weights
     const int64_t* ff;     // nullable folded distance sums
-    uint16_t* lvl;
+    void* lvl;
     uint64_t* sig;
     void* rho;
     int32_t* vmark;
-    uint32_t* fq;
+    uint32_t* fq;          // regular frontier entries, all levels
     unsigned long long fcap;
     unsigned long long* foff;
+    uint32_t* hq;          // hub frontier entries (vertex degree > HUB_DEG), all levels
+    unsigned long long hcap;
+    unsigned long long* hoff;
     Ctl* ctl;
     uint32_t* ovf;
     unsigned long long* cc;
@@ -68,31 +81,43 @@ struct KArgs {
     int semantics;
 };
 
+constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expanded by a whole CTA
+constexpr int FETCH = 8;        // regular entries a warp takes per fetch
+constexpr int WARPS = BLOCK / 32;
+
 __device__ __forceinline__ size_t sidx(int g, int n, int v, int t) {
     return ((((size_t)g * (size_t)n) + (size_t)v) << 5) + (size_t)t;
 }
 
-// Enqueue (x, g) for level lev unless already enqueued at lev.
-__device__ __forceinline__ void enqueue_once(const KArgs& A, int x, int g, int lev) {
-    if (atomicExch(&A.vmark[(size_t)g * A.n + x], lev) != lev) {
-        unsigned long long pos = atomicAdd(&A.ctl->tail, 1ULL);
-        if (pos < A.fcap) A.fq[pos] = ((uint32_t)x << 5) | (uint32_t)g;
+__device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > HUB_DEG; }
+
+// Warp-aggregated append of the entries of threads with has == true, hub
+// entries to the hub queue, the rest to the regular queue.
+__device__ __forceinline__ void warp_append(const KArgs& A, bool has, bool hub, uint32_t ent) {
+    const int t = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const bool mine = has && (hub == (k == 1));
+        const unsigned m = __ballot_sync(FULL, mine);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long* tail = k ? &A.ctl->htail : &A.ctl->tail;
+        unsigned long long base = 0;
+        if (t == leader) base = atomicAdd(tail, (unsigned long long)__popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (mine) {
+            const unsigned long long pos = base + __popc(m & ((1u << t) - 1u));
+            if (k) { if (pos < A.hcap) A.hq[pos] = ent; }
+            else { if (pos < A.fcap) A.fq[pos] = ent; }
+        }
     }
 }
 
-// Warp-aggregated append of the entries of threads with has == true.
-__device__ __forceinline__ void warp_append(const KArgs& A, bool has, uint32_t ent) {
-    const unsigned m = __ballot_sync(FULL, has);
-    if (!m) return;
-    const int t = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    unsigned long long base = 0;
-    if (t == leader) base = atomicAdd(&A.ctl->tail, (unsigned long long)__popc(m));
-    base = __shfl_sync(FULL, base, leader);
-    if (has) {
-        unsigned long long pos = base + __popc(m & ((1u << t) - 1u));
-        if (pos < A.fcap) A.fq[pos] = ent;
-    }
+// First claim of (x, g) for level lev: a plain read filters repeats before the atomic.
+__device__ __forceinline__ bool claim(const KArgs& A, size_t gbase, int x, int lev) {
+    int32_t* p = &A.vmark[gbase + x];
+    if (*(volatile int32_t*)p == lev) return false;
+    return atomicExch(p, lev) != lev;
 }
 
 __device__ __forceinline__ void lse_add(double& m, double& s, double y) {
@@ -107,7 +132,7 @@ __device__ __forceinline__ void lse_merge(double& m, double& s, double m2, doubl
 }
 
 // Last CTA of a forward launch publishes the next level's frontier bounds.
-__device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done) {
+__device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, int maxd) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -116,15 +141,19 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done) 
             __threadfence();
             A.ctl->blocks = 0;
             if (!done) {
-                unsigned long long tail = atomicAdd(&A.ctl->tail, 0ULL);
-                if (tail > A.fcap) {
+                const unsigned long long tail = atomicAdd(&A.ctl->tail, 0ULL);
+                const unsigned long long htail = atomicAdd(&A.ctl->htail, 0ULL);
+                if (tail > A.fcap || htail > A.hcap) {
                     A.ctl->err |= 1;
                     A.ctl->done = 1;
                     A.ctl->maxlevel = d;
                 } else {
                     A.foff[d + 2] = tail;
-                    if (tail == A.foff[d + 1]) { A.ctl->done = 1; A.ctl->maxlevel = d; }
-                    else if (d + 1 >= MAX_LEVEL) { A.ctl->err |= 2; A.ctl->done = 1; A.ctl->maxlevel = d; }
+                    A.hoff[d + 2] = htail;
+                    A.ctl->next = A.foff[d + 1];
+                    A.ctl->hnext = A.hoff[d + 1];
+                    if (tail == A.foff[d + 1] && htail == A.hoff[d + 1]) { A.ctl->done = 1; A.ctl->maxlevel = d; }
+                    else if (d + 1 >= maxd) { A.ctl->err |= 2; A.ctl->done = 1; A.ctl->maxlevel = d; }
                     else A.ctl->level = d + 1;
                 }
             }
@@ -132,136 +161,224 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done) 
     }
 }
 
-// MODE 0: distances only (closeness sums per lane); 1: exact uint64 sigma;
-// 2: log2-domain sigma (FP64).
+// ---- forward --------------------------------------------------------------
+// Neighbour chunks r0 + 32*sub, stepping 32*nsub (nsub warps share a hub).
+// Pulls sigma from level d-1 neighbours into (acc, of) or (lm, ls) and
+// discovers level d+1.
+template <int MODE, typename LT>
+__device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gbase, LT* lv, bool act, unsigned am,
+                                         long long r0, long long r1, int sub, int nsub, uint64_t& acc, bool& of,
+                                         double& lm, double& ls) {
+    constexpr LT INF = (LT)Lv<LT>::INF;
+    const int t = threadIdx.x & 31;
+    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const double* sigd = reinterpret_cast<const double*>(A.sig);
+    if (__popc(am) > A.sparse) {
+        // lane-parallel: thread t owns lane t; per batch of U neighbours every
+        // level is loaded first, then path counts, then the stores.
+        for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+            const int cnt = (int)min(32LL, r1 - jb);
+            const int xm = (t < cnt) ? A.col[jb + t] : 0;
+            for (int q0 = 0; q0 < cnt; q0 += U) {
+                LT Lx[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                    Lx[u] = (q0 + u < cnt) ? lv[((size_t)x << 5) + t] : dl;
+                }
+                if (MODE != 0 && d > 0) {
+                    if (MODE == 1) {
+                        uint64_t sv[U];
+#pragma unroll
+                        for (int u = 0; u < U; u++) {
+                            const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                            sv[u] = (act && Lx[u] == dprev) ? A.sig[((gbase + (size_t)x) << 5) + t] : 0ULL;
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; u++) {
+                            const uint64_t na = acc + sv[u];
+                            of |= (na < acc);
+                            acc = na;
+                        }
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < U; u++) {
+                            const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                            if (act && Lx[u] == dprev) lse_add(lm, ls, sigd[((gbase + (size_t)x) << 5) + t]);
+                        }
+                    }
+                }
+                unsigned dbits = 0;
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                    const bool disc = act && (q0 + u < cnt) && Lx[u] > dl;
+                    if (disc && Lx[u] == INF) lv[((size_t)x << 5) + t] = dnext;
+                    if (__ballot_sync(FULL, disc)) dbits |= 1u << u;
+                }
+                // thread u claims neighbour u of the batch
+                const int mx = __shfl_sync(FULL, xm, (q0 + t) & 31);
+                const bool has = (t < U) && ((dbits >> t) & 1u) && claim(A, gbase, mx, d + 1);
+                warp_append(A, has, has && is_hub(A, mx), ((uint32_t)mx << 5) | (uint32_t)g);
+            }
+        }
+    } else {
+        // edge-parallel: threads over neighbours, active lanes in turn
+        unsigned rem = am;
+        while (rem) {
+            const int a = __ffs(rem) - 1;
+            rem &= rem - 1u;
+            uint64_t pacc = 0;
+            bool pof = false;
+            double pm = -INFINITY, ps = 0.0;
+            for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+                const long long j = jb + t;
+                bool has = false;
+                int x = 0;
+                if (j < r1) {
+                    x = A.col[j];
+                    LT* px = lv + ((size_t)x << 5) + a;
+                    const LT Lx = *px;
+                    if (MODE != 0 && d > 0 && Lx == dprev) {
+                        const size_t xi = ((gbase + (size_t)x) << 5) + a;
+                        if (MODE == 1) {
+                            const uint64_t sv = A.sig[xi];
+                            const uint64_t na = pacc + sv;
+                            pof |= (na < pacc);
+                            pacc = na;
+                        } else {
+                            lse_add(pm, ps, sigd[xi]);
+                        }
+                    }
+                    if (Lx > dl) {
+                        if (Lx == INF) *px = dnext;
+                        has = claim(A, gbase, x, d + 1);
+                    }
+                }
+                warp_append(A, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
+            }
+            if (MODE == 1) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const uint64_t p2 = __shfl_xor_sync(FULL, pacc, o);
+                    const int f2 = __shfl_xor_sync(FULL, (int)pof, o);
+                    const uint64_t na = pacc + p2;
+                    pof = pof || f2 || (na < pacc);
+                    pacc = na;
+                }
+                if (t == a) { acc = pacc; of = pof; }
+            } else if (MODE == 2) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double m2 = __shfl_xor_sync(FULL, pm, o);
+                    const double s2 = __shfl_xor_sync(FULL, ps, o);
+                    lse_merge(pm, ps, m2, s2);
+                }
+                if (t == a) { lm = pm; ls = ps; }
+            }
+        }
+    }
+}
+
 template <int MODE>
+__device__ __forceinline__ void fwd_store(const KArgs& A, int g, size_t gbase, int v, uint64_t acc, bool of, double lm,
+                                          double ls) {
+    const int t = threadIdx.x & 31;
+    const size_t vi = ((gbase + (size_t)v) << 5) + t;
+    if (MODE == 1) {
+        A.sig[vi] = acc;
+        if (of) atomicOr(&A.ovf[g], 1u << t);
+    } else {
+        reinterpret_cast<double*>(A.sig)[vi] = lm + log2(ls);
+    }
+}
+
+// Forward level kernel.  MODE 0: distances only (closeness sums per lane);
+// 1: exact uint64 sigma; 2: log2-domain sigma (FP64).
+template <int MODE, typename LT>
 __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
     __shared__ unsigned long long cc_sh[MODE == 0 ? 32 * 32 : 1];
+    __shared__ uint64_t h_acc[WARPS][32];
+    __shared__ double h_ls[WARPS][32];
+    __shared__ unsigned char h_of[WARPS][32];
+    __shared__ unsigned long long s_i;
     if (MODE == 0) {
         for (int i = threadIdx.x; i < A.ng * 32; i += blockDim.x) cc_sh[i] = 0ULL;
         __syncthreads();
     }
     const int done = *(volatile int*)&A.ctl->done;
     const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (!done) {
-        const unsigned long long b = A.foff[d], e = A.foff[d + 1];
-        const int t = threadIdx.x & 31;
-        const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
-        double* sigd = reinterpret_cast<double*>(A.sig);
-        for (unsigned long long i = b + wid; i < e; i += nw) {
-            const uint32_t ent = A.fq[i];
+        const LT dl = (LT)d;
+        // hub entries: one CTA per entry, warps split the neighbours
+        const unsigned long long he = A.hoff[d + 1];
+        for (;;) {
+            if (threadIdx.x == 0) s_i = atomicAdd(&A.ctl->hnext, 1ULL);
+            __syncthreads();
+            const unsigned long long i = s_i;
+            __syncthreads();
+            if (i >= he) break;
+            const uint32_t ent = A.hq[i];
             const int v = (int)(ent >> 5), g = (int)(ent & 31u);
             const size_t gbase = (size_t)g * (size_t)A.n;
-            uint16_t* lv = A.lvl + (gbase << 5);
-            const uint16_t L = lv[((size_t)v << 5) + t];
-            const bool act = (L == (uint16_t)d);
+            LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 5);
+            const bool act = (lv[((size_t)v << 5) + t] == dl);
             const unsigned am = __ballot_sync(FULL, act);
-            if (am == 0u) continue;
-            if (MODE == 0 && act) {
+            if (am == 0u) continue;   // uniform across the CTA
+            if (MODE == 0 && act && wib == 0) {
                 const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
                 atomicAdd(&cc_sh[g * 32 + t], (unsigned long long)c);
             }
-            const long long r0 = A.row[v], r1 = A.row[v + 1];
             uint64_t acc = 0;
             bool of = false;
             double lm = -INFINITY, ls = 0.0;
-            if (__popc(am) > A.sparse) {
-                // lane-parallel: thread t owns lane t, neighbours in turn
-                for (long long jb = r0; jb < r1; jb += 32) {
-                    const int cnt = (int)min(32LL, r1 - jb);
-                    const int xm = (t < cnt) ? A.col[jb + t] : 0;
-#pragma unroll 4
-                    for (int q = 0; q < cnt; q++) {
-                        const int x = __shfl_sync(FULL, xm, q);
-                        uint16_t* px = lv + ((size_t)x << 5) + t;
-                        const uint16_t Lx = *px;
-                        bool disc = false;
-                        if (act) {
-                            if (MODE != 0 && d > 0 && Lx == (uint16_t)(d - 1)) {
-                                const size_t xi = ((gbase + (size_t)x) << 5) + t;
-                                if (MODE == 1) {
-                                    const uint64_t s = A.sig[xi];
-                                    const uint64_t na = acc + s;
-                                    of |= (na < acc);
-                                    acc = na;
-                                } else {
-                                    lse_add(lm, ls, sigd[xi]);
-                                }
-                            }
-                            if (Lx > (uint16_t)d) {
-                                disc = true;
-                                if (Lx == INF16) *px = (uint16_t)(d + 1);
-                            }
+            fwd_scan<MODE, LT>(A, d, g, gbase, lv, act, am, A.row[v], A.row[v + 1], wib, WARPS, acc, of, lm, ls);
+            if (MODE != 0) {
+                if (MODE == 1) h_acc[wib][t] = acc;
+                else { h_acc[wib][t] = __double_as_longlong(lm); h_ls[wib][t] = ls; }
+                h_of[wib][t] = of;
+                __syncthreads();
+                if (wib == 0 && act && d > 0) {
+                    for (int w = 1; w < WARPS; w++) {
+                        if (MODE == 1) {
+                            const uint64_t na = acc + h_acc[w][t];
+                            of = of || h_of[w][t] || (na < acc);
+                            acc = na;
+                        } else {
+                            lse_merge(lm, ls, __longlong_as_double(h_acc[w][t]), h_ls[w][t]);
                         }
-                        const unsigned dm = __ballot_sync(FULL, disc);
-                        if (dm && t == 0) enqueue_once(A, x, g, d + 1);
                     }
+                    fwd_store<MODE>(A, g, gbase, v, acc, of, lm, ls);
                 }
-            } else {
-                // edge-parallel: threads over neighbours, active lanes in turn
-                unsigned rem = am;
-                while (rem) {
-                    const int a = __ffs(rem) - 1;
-                    rem &= rem - 1u;
-                    uint64_t pacc = 0;
-                    bool pof = false;
-                    double pm = -INFINITY, ps = 0.0;
-                    for (long long jb = r0; jb < r1; jb += 32) {
-                        const long long j = jb + t;
-                        bool has = false;
-                        int x = 0;
-                        if (j < r1) {
-                            x = A.col[j];
-                            uint16_t* px = lv + ((size_t)x << 5) + a;
-                            const uint16_t Lx = *px;
-                            if (MODE != 0 && d > 0 && Lx == (uint16_t)(d - 1)) {
-                                const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                                if (MODE == 1) {
-                                    const uint64_t s = A.sig[xi];
-                                    const uint64_t na = pacc + s;
-                                    pof |= (na < pacc);
-                                    pacc = na;
-                                } else {
-                                    lse_add(pm, ps, sigd[xi]);
-                                }
-                            }
-                            if (Lx > (uint16_t)d) {
-                                if (Lx == INF16) *px = (uint16_t)(d + 1);
-                                has = (atomicExch(&A.vmark[gbase + x], d + 1) != d + 1);
-                            }
-                        }
-                        warp_append(A, has, ((uint32_t)x << 5) | (uint32_t)g);
-                    }
-                    if (MODE == 1) {
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            const uint64_t p2 = __shfl_xor_sync(FULL, pacc, o);
-                            const int f2 = __shfl_xor_sync(FULL, (int)pof, o);
-                            const uint64_t na = pacc + p2;
-                            pof = pof || f2 || (na < pacc);
-                            pacc = na;
-                        }
-                        if (t == a) { acc = pacc; of = pof; }
-                    } else if (MODE == 2) {
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) {
-                            const double m2 = __shfl_xor_sync(FULL, pm, o);
-                            const double s2 = __shfl_xor_sync(FULL, ps, o);
-                            lse_merge(pm, ps, m2, s2);
-                        }
-                        if (t == a) { lm = pm; ls = ps; }
-                    }
-                }
+                __syncthreads();
             }
-            if (MODE != 0 && act && d > 0) {
-                const size_t vi = ((gbase + (size_t)v) << 5) + t;
-                if (MODE == 1) {
-                    A.sig[vi] = acc;
-                    if (of) atomicOr(&A.ovf[g], 1u << t);
-                } else {
-                    sigd[vi] = lm + log2(ls);
+        }
+        // regular entries: each warp fetches FETCH at a time
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const unsigned long long lim = min(base + FETCH, e);
+            for (unsigned long long i = base; i < lim; i++) {
+                const uint32_t ent = A.fq[i];
+                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+                const size_t gbase = (size_t)g * (size_t)A.n;
+                LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 5);
+                const bool act = (lv[((size_t)v << 5) + t] == dl);
+                const unsigned am = __ballot_sync(FULL, act);
+                if (am == 0u) continue;
+                if (MODE == 0 && act) {
+                    const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
+                    atomicAdd(&cc_sh[g * 32 + t], (unsigned long long)c);
                 }
+                uint64_t acc = 0;
+                bool of = false;
+                double lm = -INFINITY, ls = 0.0;
+                fwd_scan<MODE, LT>(A, d, g, gbase, lv, act, am, A.row[v], A.row[v + 1], 0, 1, acc, of, lm, ls);
+                if (MODE != 0 && act && d > 0) fwd_store<MODE>(A, g, gbase, v, acc, of, lm, ls);
             }
         }
     }
@@ -270,103 +387,171 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
         for (int i = threadIdx.x; i < A.ng * 32; i += blockDim.x)
             if (cc_sh[i]) atomicAdd(&A.cc[i], cc_sh[i]);
     }
-    fwd_last_block(A, d, done);
+    fwd_last_block(A, d, done, Lv<LT>::MAXD);
 }
 
-// Dependency sweep for one level d >= 1 (descending).  LOG: sigma held as
-// log2 and rho as a(w) = log2(1 + delta(w)) - log2 sigma(w), so that
-// sigma(v)/sigma(w) * (1 + delta(w)) = exp2(log2 sigma(v) + a(w)).
+// ---- dependency sweep -------------------------------------------------------
+// LOG: sigma held as log2 and rho as a(w) = log2(1 + delta(w)) - log2 sigma(w),
+// so that sigma(v)/sigma(w) * (1 + delta(w)) = exp2(log2 sigma(v) + a(w)).
+template <bool LOG, typename T, typename LT>
+__device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, bool act, unsigned am,
+                                         double lsv, long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
+    const int t = threadIdx.x & 31;
+    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const T* rho = reinterpret_cast<const T*>(A.rho);
+    const double* rhod = reinterpret_cast<const double*>(A.rho);
+    if (__popc(am) > A.sparse) {
+        for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+            const int cnt = (int)min(32LL, r1 - jb);
+            const int xm = (t < cnt) ? A.col[jb + t] : 0;
+            for (int q0 = 0; q0 < cnt; q0 += U) {
+                LT Lx[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                    Lx[u] = (q0 + u < cnt) ? lv[((size_t)x << 5) + t] : dl;
+                }
+                if (LOG) {
+                    double rv[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                        rv[u] = (act && Lx[u] == dnext) ? rhod[((gbase + (size_t)x) << 5) + t] : -INFINITY;
+                        pc += (Lx[u] == dprev);
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; u++) acc += (T)exp2(lsv + rv[u]);
+                } else {
+                    T rv[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
+                        rv[u] = (act && Lx[u] == dnext) ? rho[((gbase + (size_t)x) << 5) + t] : T(0);
+                        pc += (Lx[u] == dprev);
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; u++) acc += rv[u];
+                }
+            }
+        }
+    } else {
+        unsigned rem = am;
+        while (rem) {
+            const int a = __ffs(rem) - 1;
+            rem &= rem - 1u;
+            const double lsa = LOG ? __shfl_sync(FULL, lsv, a) : 0.0;
+            T pacc = T(0);
+            int ppc = 0;
+            for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+                const long long j = jb + t;
+                if (j < r1) {
+                    const int x = A.col[j];
+                    const LT Lx = lv[((size_t)x << 5) + a];
+                    if (Lx == dnext) {
+                        const size_t xi = ((gbase + (size_t)x) << 5) + a;
+                        if (LOG) pacc += (T)exp2(lsa + rhod[xi]);
+                        else pacc += rho[xi];
+                    } else if (Lx == dprev) {
+                        ppc++;
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                pacc += __shfl_xor_sync(FULL, pacc, o);
+                ppc += __shfl_xor_sync(FULL, ppc, o);
+            }
+            if (t == a) { acc = pacc; pc = ppc; }
+        }
+    }
+}
+
+// delta, rho and the BC contribution of (v, lane t); warp-summed into bcg.
 template <bool LOG, typename T>
+__device__ __forceinline__ void bwd_finish(const KArgs& A, size_t gbase, int v, bool act, double lsv, T acc, int pc,
+                                           bool refsem) {
+    const int t = threadIdx.x & 31;
+    const size_t vi = ((gbase + (size_t)v) << 5) + t;
+    double contrib = 0.0;
+    if (act) {
+        T delta;
+        if (LOG) {
+            delta = acc;
+            reinterpret_cast<double*>(A.rho)[vi] = log2(1.0 + (double)delta) - lsv;
+        } else {
+            const T sv = (T)A.sig[vi];
+            delta = sv * acc;
+            reinterpret_cast<T*>(A.rho)[vi] = (T(1) + delta) / sv;
+        }
+        contrib = (double)delta * (refsem ? (double)pc : 1.0);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(FULL, contrib, o);
+    if (t == 0) A.bcg[gbase + v] += contrib;
+}
+
+template <bool LOG, typename T, typename LT>
 __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
+    __shared__ double h_acc[WARPS][32];
+    __shared__ int h_pc[WARPS][32];
+    __shared__ unsigned long long s_i;
     const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const bool refsem = (A.semantics == GBC_BC_REFERENCE);
     if (d >= 1) {
-        const unsigned long long b = A.foff[d], e = A.foff[d + 1];
-        const int t = threadIdx.x & 31;
-        const unsigned long long wid = ((unsigned long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        const unsigned long long nw = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+        const LT dl = (LT)d;
         const double* sigd = reinterpret_cast<const double*>(A.sig);
-        T* rho = reinterpret_cast<T*>(A.rho);
-        double* rhod = reinterpret_cast<double*>(A.rho);
-        const bool refsem = (A.semantics == GBC_BC_REFERENCE);
-        for (unsigned long long i = b + wid; i < e; i += nw) {
-            const uint32_t ent = A.fq[i];
+        const unsigned long long he = A.hoff[d + 1];
+        for (;;) {
+            if (threadIdx.x == 0) s_i = atomicAdd(&A.ctl->hnext, 1ULL);
+            __syncthreads();
+            const unsigned long long i = s_i;
+            __syncthreads();
+            if (i >= he) break;
+            const uint32_t ent = A.hq[i];
             const int v = (int)(ent >> 5), g = (int)(ent & 31u);
             const size_t gbase = (size_t)g * (size_t)A.n;
-            const uint16_t* lv = A.lvl + (gbase << 5);
-            const size_t vi = ((gbase + (size_t)v) << 5) + t;
-            const bool act = (lv[((size_t)v << 5) + t] == (uint16_t)d);
+            const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 5);
+            const bool act = (lv[((size_t)v << 5) + t] == dl);
             const unsigned am = __ballot_sync(FULL, act);
             if (am == 0u) continue;
-            double lsv = 0.0;
-            if (LOG) lsv = act ? sigd[vi] : 0.0;
+            const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
             T acc = T(0);
             int pc = 0;
-            const long long r0 = A.row[v], r1 = A.row[v + 1];
-            if (__popc(am) > A.sparse) {
-                for (long long jb = r0; jb < r1; jb += 32) {
-                    const int cnt = (int)min(32LL, r1 - jb);
-                    const int xm = (t < cnt) ? A.col[jb + t] : 0;
-#pragma unroll 4
-                    for (int q = 0; q < cnt; q++) {
-                        const int x = __shfl_sync(FULL, xm, q);
-                        const uint16_t Lx = lv[((size_t)x << 5) + t];
-                        if (act) {
-                            if (Lx == (uint16_t)(d + 1)) {
-                                const size_t xi = ((gbase + (size_t)x) << 5) + t;
-                                if (LOG) acc += (T)exp2(lsv + rhod[xi]);
-                                else acc += rho[xi];
-                            } else if (Lx == (uint16_t)(d - 1)) {
-                                pc++;
-                            }
-                        }
-                    }
+            bwd_scan<LOG, T, LT>(A, d, gbase, lv, act, am, lsv, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+            h_acc[wib][t] = (double)acc;
+            h_pc[wib][t] = pc;
+            __syncthreads();
+            if (wib == 0) {
+                for (int w = 1; w < WARPS; w++) {
+                    acc += (T)h_acc[w][t];
+                    pc += h_pc[w][t];
                 }
-            } else {
-                unsigned rem = am;
-                while (rem) {
-                    const int a = __ffs(rem) - 1;
-                    rem &= rem - 1u;
-                    const double lsa = LOG ? __shfl_sync(FULL, lsv, a) : 0.0;
-                    T pacc = T(0);
-                    int ppc = 0;
-                    for (long long jb = r0; jb < r1; jb += 32) {
-                        const long long j = jb + t;
-                        if (j < r1) {
-                            const int x = A.col[j];
-                            const uint16_t Lx = lv[((size_t)x << 5) + a];
-                            if (Lx == (uint16_t)(d + 1)) {
-                                const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                                if (LOG) pacc += (T)exp2(lsa + rhod[xi]);
-                                else pacc += rho[xi];
-                            } else if (Lx == (uint16_t)(d - 1)) {
-                                ppc++;
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        pacc += __shfl_xor_sync(FULL, pacc, o);
-                        ppc += __shfl_xor_sync(FULL, ppc, o);
-                    }
-                    if (t == a) { acc = pacc; pc = ppc; }
-                }
+                bwd_finish<LOG, T>(A, gbase, v, act, lsv, acc, pc, refsem);
             }
-            double contrib = 0.0;
-            if (act) {
-                T delta;
-                if (LOG) {
-                    delta = acc;
-                    rhod[vi] = log2(1.0 + (double)delta) - lsv;
-                } else {
-                    const T sv = (T)A.sig[vi];
-                    delta = sv * acc;
-                    rho[vi] = (T(1) + delta) / sv;
-                }
-                contrib = (double)delta * (refsem ? (double)pc : 1.0);
+            __syncthreads();
+        }
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const unsigned long long lim = min(base + FETCH, e);
+            for (unsigned long long i = base; i < lim; i++) {
+                const uint32_t ent = A.fq[i];
+                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+                const size_t gbase = (size_t)g * (size_t)A.n;
+                const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 5);
+                const bool act = (lv[((size_t)v << 5) + t] == dl);
+                const unsigned am = __ballot_sync(FULL, act);
+                if (am == 0u) continue;
+                const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
+                T acc = T(0);
+                int pc = 0;
+                bwd_scan<LOG, T, LT>(A, d, gbase, lv, act, am, lsv, A.row[v], A.row[v + 1], 0, 1, acc, pc);
+                bwd_finish<LOG, T>(A, gbase, v, act, lsv, acc, pc, refsem);
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(FULL, contrib, o);
-            if (t == 0) A.bcg[gbase + v] += contrib;
         }
     }
     __syncthreads();
@@ -376,66 +561,88 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
         if (prev == gridDim.x - 1) {
             __threadfence();
             A.ctl->blocks = 0;
-            if (d >= 1) A.ctl->level = d - 1;
+            if (d >= 1) {
+                A.ctl->level = d - 1;
+                A.ctl->next = A.foff[d - 1];
+                A.ctl->hnext = A.hoff[d - 1];
+            }
         }
     }
 }
 
 // One CTA: place each lane's source at level 0 and build F_0.
-__global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, int mode) {
+__global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, int mode, int lvl_bytes) {
     const int l = threadIdx.x;
     if (l < kb) {
         const int g = l >> 5, t = l & 31;
         const int s = src[l];
         if (s >= 0 && s < A.n) {
             const size_t i = sidx(g, A.n, s, t);
-            A.lvl[i] = 0;
+            if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[i] = 0;
+            else reinterpret_cast<uint16_t*>(A.lvl)[i] = 0;
             if (mode == 1) A.sig[i] = 1ULL;
             else if (mode == 2) reinterpret_cast<double*>(A.sig)[i] = 0.0;
             if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
-                const unsigned long long pos = atomicAdd(&A.ctl->tail, 1ULL);
-                A.fq[pos] = ((uint32_t)s << 5) | (uint32_t)g;
+                const uint32_t ent = ((uint32_t)s << 5) | (uint32_t)g;
+                if (is_hub(A, s)) A.hq[atomicAdd(&A.ctl->htail, 1ULL)] = ent;
+                else A.fq[atomicAdd(&A.ctl->tail, 1ULL)] = ent;
             }
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned long long tail = atomicAdd(&A.ctl->tail, 0ULL);
+        const unsigned long long htail = atomicAdd(&A.ctl->htail, 0ULL);
         A.foff[0] = 0;
         A.foff[1] = tail;
+        A.hoff[0] = 0;
+        A.hoff[1] = htail;
+        A.ctl->next = 0;
+        A.ctl->hnext = 0;
         A.ctl->level = 0;
         A.ctl->maxlevel = 0;
-        A.ctl->done = (tail == 0);
+        A.ctl->done = (tail == 0 && htail == 0);
         A.ctl->err = 0;
         A.ctl->blocks = 0;
     }
 }
 
-__global__ void bw_begin_kernel(KArgs A) { A.ctl->level = A.ctl->maxlevel; A.ctl->blocks = 0; }
+__global__ void bw_begin_kernel(KArgs A) {
+    const int L = A.ctl->maxlevel;
+    A.ctl->level = L;
+    A.ctl->blocks = 0;
+    A.ctl->next = A.foff[L];
+    A.ctl->hnext = A.hoff[L];
+}
 
 // Reset the lane state touched by the batch (every (v,g) of every level).
-__global__ void cleanup_kernel(KArgs A, unsigned long long count) {
+__global__ void cleanup_kernel(KArgs A, unsigned long long count, unsigned long long hcount, int lvl_bytes) {
     const unsigned long long tid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    for (unsigned long long k = tid; k < count * 32ULL; k += stride) {
+    const unsigned long long total = (count + hcount) * 32ULL;
+    for (unsigned long long k = tid; k < total; k += stride) {
         const unsigned long long i = k >> 5;
         const int t = (int)(k & 31ULL);
-        const uint32_t ent = A.fq[i];
+        const uint32_t ent = (i < count) ? A.fq[i] : A.hq[i - count];
         const int v = (int)(ent >> 5), g = (int)(ent & 31u);
-        A.lvl[sidx(g, A.n, v, t)] = INF16;
+        if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[sidx(g, A.n, v, t)] = 0xFFu;
+        else reinterpret_cast<uint16_t*>(A.lvl)[sidx(g, A.n, v, t)] = 0xFFFFu;
         if (t == 0) A.vmark[(size_t)g * A.n + v] = -1;
     }
 }
 
 // Distances and exact counts of lanes [0,kb) into dense [kb][n] arrays.
-__global__ void sssp_out_kernel(KArgs A, int kb, int32_t* dist, uint64_t* sigma) {
+__global__ void sssp_out_kernel(KArgs A, int kb, int32_t* dist, uint64_t* sigma, int lvl_bytes) {
     const size_t total = (size_t)kb * A.n;
     for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
         const int l = (int)(k / A.n), v = (int)(k % A.n);
         const size_t i = sidx(l >> 5, A.n, v, l & 31);
-        const uint16_t L = A.lvl[i];
-        if (dist) dist[k] = (L == INF16) ? -1 : (int32_t)L;
-        if (sigma) sigma[k] = (L == INF16) ? 0ULL : A.sig[i];
+        int L;
+        bool unreached;
+        if (lvl_bytes == 1) { L = reinterpret_cast<const uint8_t*>(A.lvl)[i]; unreached = (L == 0xFF); }
+        else { L = reinterpret_cast<const uint16_t*>(A.lvl)[i]; unreached = (L == 0xFFFF); }
+        if (dist) dist[k] = unreached ? -1 : L;
+        if (sigma) sigma[k] = unreached ? 0ULL : A.sig[i];
     }
 }
 
@@ -445,6 +652,17 @@ __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, 
         double s = 0.0;
         for (int g = 0; g < ng; g++) s += bcg[(size_t)g * n + v];
         bc[v] = s;
+    }
+}
+
+constexpr int MAX_LEVEL = Lv<uint16_t>::MAXD;
+
+// dst[g][v] += bcg[g][v] for every lane group whose destination is set.
+__global__ void bc_scatter_kernel(const double* __restrict__ bcg, int ng, int n, double* const* __restrict__ dst) {
+    const size_t total = (size_t)ng * n;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+        double* p = dst[k / n];
+        if (p) p[k % n] += bcg[k];
     }
 }
 
@@ -458,6 +676,7 @@ struct LaneAccess {
         A.w = e.g_->w; A.ff = e.g_->ff;
         A.lvl = e.lvl_; A.sig = e.sig_; A.rho = e.rho_; A.vmark = e.vmark_;
         A.fq = e.fq_; A.fcap = e.fcap_; A.foff = e.foff_; A.ctl = (Ctl*)e.ctl_; A.ovf = e.ovf_;
+        A.hq = e.hq_; A.hcap = e.hcap_; A.hoff = e.hoff_;
         A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.semantics = semantics;
         return A;
     }
@@ -474,6 +693,8 @@ void LaneEngine::release() {
     for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
     graphs_.clear();
     cudaFree(lvl_); cudaFree(sig_); cudaFree(rho_); cudaFree(vmark_); cudaFree(fq_); cudaFree(foff_);
+    cudaFree(hq_); cudaFree(hoff_);
+    hq_ = nullptr; hoff_ = nullptr;
     cudaFree(ctl_); cudaFree(ovf_);
     if (ctl_host_) cudaFreeHost(ctl_host_);
     cudaFree(bcg_);
@@ -482,17 +703,32 @@ void LaneEngine::release() {
     ctl_ = nullptr; ovf_ = nullptr; ctl_host_ = nullptr; bcg_ = nullptr; ccbuf_ = nullptr;
 }
 
-LaneEngine::~LaneEngine() { release(); }
+LaneEngine::~LaneEngine() {
+    release();
+    for (auto e : ev_) cudaEventDestroy(e);
+}
 
-gbc_status LaneEngine::alloc_queue(unsigned long long cap) {
-    if (fq_) cudaFree(fq_);
+gbc_status LaneEngine::ensure_events(size_t count) {
+    while (ev_.size() < count) {
+        cudaEvent_t e;
+        GBC_CUDA(cudaEventCreate(&e));
+        ev_.push_back(e);
+    }
+    return GBC_OK;
+}
+
+gbc_status LaneEngine::alloc_queue(unsigned long long cap, unsigned long long hcap) {
+    cudaFree(fq_);
+    cudaFree(hq_);
     fq_ = nullptr;
-    if (cudaMalloc(&fq_, cap * sizeof(uint32_t)) != cudaSuccess) {
+    hq_ = nullptr;
+    if (cudaMalloc(&fq_, cap * sizeof(uint32_t)) != cudaSuccess || cudaMalloc(&hq_, hcap * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
-        set_error("frontier queue allocation of %llu entries failed", cap);
+        set_error("frontier queue allocation of %llu + %llu entries failed", cap, hcap);
         return GBC_ERR_NOMEM;
     }
     fcap_ = cap;
+    hcap_ = hcap;
     for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
     graphs_.clear();
     return GBC_OK;
@@ -507,6 +743,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     lanes_ = lanes;
     ng_ = lanes / 32;
     need_bc_ = need_bc;
+    lvl_bytes_ = 1;
     sparse_ = sparse_lanes < 0 ? 2 : sparse_lanes;
     lpg_ = levels_per_graph > 0 ? levels_per_graph : 16;
     stream_ = stream;
@@ -519,6 +756,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     ok &= cudaMalloc(&lvl_, cells * sizeof(uint16_t)) == cudaSuccess;
     ok &= cudaMalloc(&vmark_, (size_t)ng_ * n * sizeof(int32_t)) == cudaSuccess;
     ok &= cudaMalloc(&foff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
+    ok &= cudaMalloc(&hoff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
     ok &= cudaMalloc(&ctl_, sizeof(Ctl)) == cudaSuccess;
     ok &= cudaMalloc(&ovf_, 32 * sizeof(uint32_t)) == cudaSuccess;
     ok &= cudaMalloc(&ccbuf_, 1024 * sizeof(unsigned long long)) == cudaSuccess;
@@ -534,15 +772,23 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
         set_error("lane state allocation failed (n=%zu lanes=%d)", n, lanes);
         return GBC_ERR_NOMEM;
     }
-    GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16)));
+    // hub entries: at most 32 levels' worth per (hub vertex, group) to start with
+    {
+        std::vector<int64_t> hrow(n + 1);
+        GBC_CUDA(cudaMemcpy(hrow.data(), g->row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+        n_hubs_ = 0;
+        for (size_t v = 0; v < n; v++) n_hubs_ += (hrow[v + 1] - hrow[v]) > HUB_DEG;
+    }
+    GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
+                        (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));
     GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, cells * sizeof(uint16_t), stream_));
     GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * n * sizeof(int32_t), stream_));
     GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
     GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
-    bytes_ = cells * 2 + (size_t)ng_ * n * 4 + fcap_ * 4 + (need_bc ? cells * 16 + (size_t)ng_ * n * 8 : 0);
+    bytes_ = cells * 2 + (size_t)ng_ * n * 4 + (fcap_ + hcap_) * 4 + (need_bc ? cells * 16 + (size_t)ng_ * n * 8 : 0);
     // grid: enough resident CTAs to fill every SM
     int occ = 0;
-    GBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, expand_kernel<1>, BLOCK, 0));
+    GBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, expand_kernel<1, uint8_t>, BLOCK, 0));
     grid_ = sm_count_ * std::max(1, std::min(occ, 8));
     return GBC_OK;
 }
@@ -551,22 +797,32 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
 // Graph keys: 0..2 expand MODE; 3 + (log*2 + f64)*2 + refsem: backward.
 gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     for (auto& c : graphs_) if (c.key == key) { *out = c.exec; return GBC_OK; }
-    KArgs A = LaneAccess::args(*this, key >= 3 ? (((key - 3) & 1) ? GBC_BC_REFERENCE : GBC_BC_BRANDES) : GBC_BC_BRANDES);
+    KArgs A = LaneAccess::args(*this, (key % 100) >= 3 ? ((((key % 100) - 3) & 1) ? GBC_BC_REFERENCE : GBC_BC_BRANDES)
+                                                       : GBC_BC_BRANDES);
     cudaStream_t cs;
     GBC_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     for (int i = 0; i < lpg_ && e == cudaSuccess; i++) {
-        switch (key) {
-            case 0: expand_kernel<0><<<grid_, BLOCK, 0, cs>>>(A); break;
-            case 1: expand_kernel<1><<<grid_, BLOCK, 0, cs>>>(A); break;
-            case 2: expand_kernel<2><<<grid_, BLOCK, 0, cs>>>(A); break;
+        const bool wide = key >= 100;
+        const int k = key % 100;
+        switch (k) {
+            case 0: if (wide) expand_kernel<0, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<0, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
+            case 1: if (wide) expand_kernel<1, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<1, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
+            case 2: if (wide) expand_kernel<2, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<2, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
             default: {
-                const int v = (key - 3) >> 1;  // log*2 + f64
-                if (v == 0) backward_kernel<false, float><<<grid_, BLOCK, 0, cs>>>(A);
-                else if (v == 1) backward_kernel<false, double><<<grid_, BLOCK, 0, cs>>>(A);
-                else if (v == 2) backward_kernel<true, float><<<grid_, BLOCK, 0, cs>>>(A);
-                else backward_kernel<true, double><<<grid_, BLOCK, 0, cs>>>(A);
+                const int v = (k - 3) >> 1;  // log*2 + f64
+                if (wide) {
+                    if (v == 0) backward_kernel<false, float, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else if (v == 1) backward_kernel<false, double, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else if (v == 2) backward_kernel<true, float, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else backward_kernel<true, double, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
+                } else {
+                    if (v == 0) backward_kernel<false, float, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else if (v == 1) backward_kernel<false, double, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else if (v == 2) backward_kernel<true, float, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
+                    else backward_kernel<true, double, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
+                }
             }
         }
         e = cudaGetLastError();
@@ -595,6 +851,18 @@ gbc_status LaneEngine::bc_finish(double* d_bc) {
     return GBC_OK;
 }
 
+gbc_status LaneEngine::bc_scatter(double* const* d_dst) {
+    bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, ng_, g_->n, d_dst);
+    GBC_CUDA(cudaGetLastError());
+    return GBC_OK;
+}
+
+gbc_status LaneEngine::cc_read(unsigned long long* h_cc, int32_t count) {
+    GBC_CUDA(cudaMemcpyAsync(h_cc, ccbuf_, sizeof(unsigned long long) * count, cudaMemcpyDeviceToHost, stream_));
+    GBC_CUDA(cudaStreamSynchronize(stream_));
+    return GBC_OK;
+}
+
 gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
     if (rq.kb < 1 || rq.kb > lanes_) { set_error("batch of %d sources for %d lanes", rq.kb, lanes_); return GBC_ERR_ARG; }
     const bool bc = rq.job != LaneJob::CC;
@@ -605,45 +873,64 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
         if (mode == 0) GBC_CUDA(cudaMemsetAsync(ccbuf_, 0, lanes_ * sizeof(unsigned long long), stream_));
         if (mode == 1) GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
-        seed_kernel<<<1, 1024, 0, stream_>>>(A, rq.d_src, rq.kb, mode);
+        seed_kernel<<<1, 1024, 0, stream_>>>(A, rq.d_src, rq.kb, mode, lvl_bytes_);
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches += 1;
         cudaGraphExec_t fwd;
-        GBC_TRY(get_graph(mode, &fwd));
+        const int wide = (lvl_bytes_ == 2) ? 100 : 0;
+        GBC_TRY(get_graph(wide + mode, &fwd));
         Ctl* h = (Ctl*)ctl_host_;
         int64_t launched = 0;
+        GBC_TRY(ensure_events(2));
         for (;;) {
+            GBC_CUDA(cudaEventRecord(ev_[0], stream_));
             GBC_CUDA(cudaGraphLaunch(fwd, stream_));
+            GBC_CUDA(cudaEventRecord(ev_[1], stream_));
             res.graph_launches++;
             res.kernel_launches += lpg_;
+            res.fwd_kernels += lpg_;
             launched += lpg_;
             GBC_CUDA(cudaMemcpyAsync(h, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
+            res.fwd_ms += ms;
             if (h->done) break;
             if (launched > (int64_t)MAX_LEVEL + 2 * lpg_) { set_error("forward level loop did not terminate"); return GBC_ERR_LIMIT; }
         }
         const int maxlevel = h->maxlevel;
         const unsigned long long entries = std::min<unsigned long long>(h->tail, fcap_);
+        const unsigned long long hentries = std::min<unsigned long long>(h->htail, hcap_);
         if (h->err & 1) {
             // queue overflow: reset the whole lane state, grow the queue, redo the batch
             GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
             GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
             const unsigned long long maxcap = (unsigned long long)ng_ * g_->n * 32ULL + (1ULL << 16);
-            unsigned long long want = std::min(maxcap, std::max(fcap_ * 2, (unsigned long long)h->tail + (1ULL << 20)));
-            if (want <= fcap_) { set_error("frontier queue cannot grow"); return GBC_ERR_LIMIT; }
-            GBC_TRY(alloc_queue(want));
+            const unsigned long long hmax = (unsigned long long)ng_ * n_hubs_ * 32ULL + (1ULL << 12);
+            const unsigned long long want = std::min(maxcap, std::max(fcap_ * 2, (unsigned long long)h->tail + (1ULL << 20)));
+            const unsigned long long hwant = std::min(hmax, std::max(hcap_ * 2, (unsigned long long)h->htail + (1ULL << 12)));
+            if (want <= fcap_ && hwant <= hcap_) { set_error("frontier queue cannot grow"); return GBC_ERR_LIMIT; }
+            GBC_TRY(alloc_queue(std::max(want, fcap_), std::max(hwant, hcap_)));
             continue;
         }
         if (h->err & 2) {
-            cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries);
+            if (lvl_bytes_ == 1) {
+                // deeper than 8-bit levels allow: switch this engine to 16-bit levels, redo
+                lvl_bytes_ = 2;
+                GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
+                GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
+                GBC_CUDA(cudaStreamSynchronize(stream_));
+                continue;
+            }
+            cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
             set_error("BFS deeper than %d levels", MAX_LEVEL);
             return GBC_ERR_LIMIT;
         }
         res.levels += maxlevel + 1;
-        res.frontier_entries += (int64_t)entries;
+        res.frontier_entries += (int64_t)(entries + hentries);
         if (rq.job == LaneJob::SSSP) {
-            sssp_out_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, rq.kb, rq.d_dist, rq.d_sigma);
+            sssp_out_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, rq.kb, rq.d_dist, rq.d_sigma, lvl_bytes_);
             GBC_CUDA(cudaGetLastError());
             res.kernel_launches++;
         }
@@ -655,28 +942,40 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             for (int i = 0; i < ng_; i++) cnt += __builtin_popcount(res.ovf_bits[i]);
             res.overflow_count += cnt;
             if (cnt && rq.abort_on_overflow) {
-                cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries);
+                cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
                 GBC_CUDA(cudaGetLastError());
                 set_error("exact path counts overflowed uint64 in %d lanes", cnt);
                 return GBC_ERR_OVERFLOW;
             }
         }
         if (rq.job == LaneJob::BC && maxlevel >= 1) {
-            const int key = 3 + ((rq.sigma_log ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 + (rq.semantics == GBC_BC_REFERENCE ? 1 : 0);
+            const int key = wide + 3 + ((rq.sigma_log ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
+                            (rq.semantics == GBC_BC_REFERENCE ? 1 : 0);
             cudaGraphExec_t bwd;
             GBC_TRY(get_graph(key, &bwd));
             bw_begin_kernel<<<1, 1, 0, stream_>>>(A);
             res.kernel_launches++;
-            for (int done = 0; done < maxlevel; done += lpg_) {
+            const int nl = (maxlevel + lpg_ - 1) / lpg_;
+            GBC_TRY(ensure_events(2 * nl));
+            for (int i = 0; i < nl; i++) {
+                GBC_CUDA(cudaEventRecord(ev_[2 * i], stream_));
                 GBC_CUDA(cudaGraphLaunch(bwd, stream_));
+                GBC_CUDA(cudaEventRecord(ev_[2 * i + 1], stream_));
                 res.graph_launches++;
                 res.kernel_launches += lpg_;
+                res.bwd_kernels += lpg_;
+            }
+            GBC_CUDA(cudaStreamSynchronize(stream_));
+            for (int i = 0; i < nl; i++) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ev_[2 * i], ev_[2 * i + 1]);
+                res.bwd_ms += ms;
             }
         }
         if (mode == 0 && rq.d_cc) {
             GBC_CUDA(cudaMemcpyAsync(rq.d_cc, ccbuf_, rq.kb * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream_));
         }
-        cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries);
+        cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches++;
         return GBC_OK;

@@ -1,0 +1,503 @@
+// Serving: continuous batching of centrality queries over device-resident
+// graphs (the query loop the reference does not have; its drivers run one
+// computation per process, Seq_CC/CC.cpp:2687, parallel_CC/para_CC.cu:383).
+//
+// One worker thread owns the device work.  Each registered graph keeps its
+// CSR in HBM and, while it has work, one lane engine.  A lane batch is filled
+// from every admitted request on one graph that wants the same kind of sweep
+// (closeness or betweenness), oldest first; a request takes whole 32-lane
+// groups, so its betweenness partials stay separate and are added into its
+// own FP64 result vector after each batch.  Requests that arrive while a
+// batch runs join the next batch.  Engines are created under an HBM budget
+// and idle ones are released when a new graph needs room.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+#include "engine.h"
+
+using namespace gbc;
+
+namespace {
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct SGraph {
+    DevGraph g;
+    std::unique_ptr<LaneEngine> eng;
+    int32_t lanes = 0;
+    int32_t* d_src = nullptr;
+    double** d_dst = nullptr;    // device table: lane group -> destination result vector
+    ~SGraph() {
+        eng.reset();
+        cudaFree(g.row);
+        cudaFree(g.col);
+        cudaFree(d_src);
+        cudaFree(d_dst);
+    }
+};
+
+struct Req {
+    int64_t id = 0;
+    int32_t gid = 0;
+    int32_t kind = GBC_Q_CC;
+    gbc_options opt{};
+    std::vector<int32_t> src;
+    size_t next = 0;             // next source to hand out
+    size_t done = 0;             // sources whose lanes finished
+    int32_t state = GBC_REQ_QUEUED;
+    gbc_status err = GBC_OK;
+    std::string msg;
+    double t_submit = 0, t_done = 0, deadline = 0;
+    double* d_bc = nullptr;      // device FP64 result (BC kinds)
+    std::vector<int64_t> cc;     // host result (CC), indexed by vertex
+    bool admitted = false;
+    int32_t inflight = 0;        // lane batches holding this request's sources or result buffer
+    ~Req() { cudaFree(d_bc); }
+    bool bc() const { return kind != GBC_Q_CC; }
+};
+
+}  // namespace
+
+struct gbc_server_s {
+    gbc_server_config cfg{};
+    size_t budget = 0;
+    int32_t max_lanes = 1024;
+    int32_t max_inflight = 64;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::vector<std::unique_ptr<SGraph>> graphs;
+    std::map<int64_t, std::unique_ptr<Req>> reqs;
+    std::deque<int64_t> fifo;    // admitted or queued requests in arrival order
+    int64_t next_id = 1;
+    bool stop = false;
+    std::thread worker;
+    int32_t rr = 0;              // round-robin position over graphs
+    // counters
+    int64_t completed = 0, batches = 0, shared_batches = 0, edges = 0;
+    double busy_ms = 0;
+
+    void run();
+    size_t engines_bytes() const {
+        size_t b = 0;
+        for (auto& g : graphs) if (g->eng) b += g->eng->device_bytes();
+        return b;
+    }
+    void fail(Req& r, gbc_status st, const char* why) {
+        r.state = GBC_REQ_FAILED;
+        r.err = st;
+        r.msg = why;
+        r.t_done = now_ms();
+    }
+};
+
+namespace {
+
+// Engine for graph gi, making room under the budget by releasing idle engines.
+gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy) {
+    SGraph& G = *S->graphs[gi];
+    if (G.eng) return GBC_OK;
+    int32_t lanes = S->max_lanes;
+    for (;;) {
+        const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true);
+        size_t used = S->engines_bytes();
+        if (used + need > S->budget) {
+            for (size_t j = 0; j < S->graphs.size() && used + need > S->budget; j++) {
+                if ((int32_t)j == gi || !S->graphs[j]->eng || graph_busy[j]) continue;
+                used -= S->graphs[j]->eng->device_bytes();
+                S->graphs[j]->eng.reset();
+            }
+        }
+        if (used + need <= S->budget) break;
+        if (lanes <= 32) { set_error("graph does not fit the HBM budget"); return GBC_ERR_BUSY; }
+        lanes = std::max(32, lanes / 2);
+    }
+    auto e = std::make_unique<LaneEngine>();
+    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, S->stream));
+    if (G.lanes != lanes) {
+        cudaFree(G.d_src);
+        cudaFree(G.d_dst);
+        G.d_src = nullptr;
+        G.d_dst = nullptr;
+        if (cudaMalloc(&G.d_src, sizeof(int32_t) * lanes) != cudaSuccess ||
+            cudaMalloc(&G.d_dst, sizeof(double*) * (lanes / 32)) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("server batch buffers");
+            return GBC_ERR_NOMEM;
+        }
+        G.lanes = lanes;
+    }
+    G.eng = std::move(e);
+    return GBC_OK;
+}
+
+}  // namespace
+
+void gbc_server_s::run() {
+    std::vector<int32_t> hsrc;
+    std::vector<double*> hdst;
+    std::vector<unsigned long long> hcc;
+    struct Slot { Req* r; size_t first; int32_t count; int32_t lane0; };
+    for (;;) {
+        std::vector<Slot> slots;
+        int32_t gi = -1, kind = 0, lanes = 0;
+        SGraph* Gp = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            for (;;) {
+                if (stop) return;
+                // expire deadlines, drop finished ids from the fifo
+                const double t = now_ms();
+                for (auto it = fifo.begin(); it != fifo.end();) {
+                    Req* r = reqs.count(*it) ? reqs[*it].get() : nullptr;
+                    if (!r || r->state == GBC_REQ_DONE || r->state == GBC_REQ_FAILED || r->state == GBC_REQ_CANCELLED) {
+                        it = fifo.erase(it);
+                        continue;
+                    }
+                    if (r->deadline > 0 && t > r->deadline && r->done < r->src.size()) {
+                        fail(*r, GBC_ERR_TIMEOUT, "deadline passed");
+                        cv_done.notify_all();
+                        it = fifo.erase(it);
+                        continue;
+                    }
+                    ++it;
+                }
+                // admission: up to max_inflight requests hold sources in flight
+                int32_t inflight = 0;
+                for (int64_t id : fifo) inflight += reqs[id]->admitted;
+                for (int64_t id : fifo) {
+                    Req* r = reqs[id].get();
+                    if (!r->admitted && inflight < max_inflight) { r->admitted = true; r->state = GBC_REQ_RUNNING; inflight++; }
+                }
+                // pick a graph with pending sources, round robin
+                std::vector<bool> busy(graphs.size(), false);
+                for (int64_t id : fifo) {
+                    Req* r = reqs[id].get();
+                    if (r->admitted && r->next < r->src.size()) busy[r->gid] = true;
+                }
+                for (size_t k = 0; k < graphs.size(); k++) {
+                    const int32_t cand = (int32_t)((rr + k) % graphs.size());
+                    if (busy[cand]) { gi = cand; break; }
+                }
+                if (gi < 0) { cv_work.wait_for(lk, std::chrono::milliseconds(50)); continue; }
+                rr = gi + 1;
+                gbc_status st = ensure_engine(this, gi, busy);
+                if (st != GBC_OK) {
+                    for (int64_t id : fifo) {
+                        Req* r = reqs[id].get();
+                        if (r->gid == gi && r->admitted) fail(*r, st, last_error());
+                    }
+                    cv_done.notify_all();
+                    gi = -1;
+                    continue;
+                }
+                lanes = graphs[gi]->lanes;
+                // fill the batch: oldest request's kind, whole lane groups per request
+                kind = -1;
+                int32_t used = 0;
+                for (int64_t id : fifo) {
+                    Req* r = reqs[id].get();
+                    if (r->gid != gi || !r->admitted || r->next >= r->src.size()) continue;
+                    const int32_t rk = r->bc() ? 1 : 0;
+                    if (kind < 0) kind = rk;
+                    if (rk != kind) continue;
+                    const int32_t room = lanes - used;
+                    if (room < 32) break;
+                    const int32_t take = (int32_t)std::min<size_t>(room, r->src.size() - r->next);
+                    slots.push_back({r, r->next, take, used});
+                    r->next += take;
+                    r->inflight++;
+                    used += ((take + 31) / 32) * 32;
+                }
+                Gp = graphs[gi].get();
+                break;
+            }
+        }
+        // device work outside the lock
+        SGraph& G = *Gp;
+        const int32_t ng = lanes / 32;
+        hsrc.assign(lanes, -1);
+        hdst.assign(ng, nullptr);
+        int32_t kb = 0;
+        for (auto& sl : slots) {
+            for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = sl.r->src[sl.first + i];
+            for (int32_t gg = sl.lane0 / 32; gg < (sl.lane0 + sl.count + 31) / 32; gg++) hdst[gg] = sl.r->d_bc;
+            kb = std::max(kb, ((sl.lane0 + sl.count + 31) / 32) * 32);
+        }
+        const double t0 = now_ms();
+        gbc_status st = GBC_OK;
+        if (cudaMemcpyAsync(G.d_src, hsrc.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+            cudaGetLastError();
+            st = GBC_ERR_CUDA;
+            set_error("source upload failed");
+        }
+        LaneResult res;
+        if (st == GBC_OK && kind == 1) {
+            if (cudaMemcpyAsync(G.d_dst, hdst.data(), sizeof(double*) * ng, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+                cudaGetLastError();
+                st = GBC_ERR_CUDA;
+            }
+            if (st == GBC_OK) st = G.eng->bc_begin();
+            LaneRequest rq;
+            rq.job = LaneJob::BC;
+            rq.d_src = G.d_src;
+            rq.kb = kb;
+            rq.delta_f64 = slots[0].r->opt.delta_precision == GBC_DELTA_F64;
+            rq.semantics = slots[0].r->opt.semantics;
+            rq.abort_on_overflow = true;
+            if (st == GBC_OK) st = G.eng->run(rq, res);
+            if (st == GBC_ERR_OVERFLOW) {
+                rq.sigma_log = 1;
+                rq.abort_on_overflow = false;
+                st = G.eng->run(rq, res);
+            }
+            if (st == GBC_OK) st = G.eng->bc_scatter(G.d_dst);
+            if (st == GBC_OK && cudaStreamSynchronize(stream) != cudaSuccess) { cudaGetLastError(); st = GBC_ERR_CUDA; }
+        } else if (st == GBC_OK) {
+            LaneRequest rq;
+            rq.job = LaneJob::CC;
+            rq.d_src = G.d_src;
+            rq.kb = kb;
+            st = G.eng->run(rq, res);
+            hcc.assign(kb, 0);
+            if (st == GBC_OK) st = G.eng->cc_read(hcc.data(), kb);
+        }
+        const double t1 = now_ms();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            busy_ms += t1 - t0;
+            batches++;
+            if (slots.size() > 1) shared_batches++;
+            for (auto& sl : slots) {
+                Req* r = sl.r;
+                r->inflight--;
+                if (r->state != GBC_REQ_RUNNING) continue;   // cancelled or expired meanwhile
+                if (st != GBC_OK) { fail(*r, st, last_error()); continue; }
+                for (int32_t i = 0; i < sl.count; i++) {
+                    const int32_t v = r->src[sl.first + i];
+                    edges += G.g.comp_edges.empty() ? 0 : G.g.comp_edges[G.g.comp[v]];
+                    if (kind == 0) r->cc[v] = (int64_t)hcc[sl.lane0 + i];
+                }
+                r->done += sl.count;
+                if (r->done == r->src.size()) {
+                    r->state = GBC_REQ_DONE;
+                    r->t_done = now_ms();
+                    completed++;
+                }
+            }
+        }
+        cv_done.notify_all();
+    }
+}
+
+extern "C" {
+
+gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out) {
+    if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    auto S = std::make_unique<gbc_server_s>();
+    if (cfg) S->cfg = *cfg;
+    if (S->cfg.max_lanes != 0 && (S->cfg.max_lanes < 32 || S->cfg.max_lanes > 1024 || S->cfg.max_lanes % 32)) {
+        set_error("max_lanes must be 0 or a multiple of 32 in [32,1024]");
+        return GBC_ERR_ARG;
+    }
+    S->max_lanes = S->cfg.max_lanes ? S->cfg.max_lanes : 1024;
+    S->max_inflight = S->cfg.max_inflight > 0 ? S->cfg.max_inflight : 64;
+    size_t fr = 0, tot = 0;
+    GBC_CUDA(cudaMemGetInfo(&fr, &tot));
+    S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : fr / 2;
+    GBC_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    gbc_server_s* raw = S.get();
+    S->worker = std::thread([raw] { raw->run(); });
+    *out = S.release();
+    return GBC_OK;
+}
+
+gbc_status gbc_server_destroy(gbc_server s) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    s->reqs.clear();
+    s->graphs.clear();
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return GBC_OK;
+}
+
+gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t* col, int32_t n, int32_t* gid) {
+    if (!s || !gid) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    GBC_TRY(validate_csr(row, col, n));
+    auto G = std::make_unique<SGraph>();
+    G->g.n = n;
+    G->g.m = row[n];
+    if (cudaMalloc(&G->g.row, sizeof(int64_t) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&G->g.col, sizeof(int32_t) * std::max<int64_t>(row[n], 1)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("graph allocation");
+        return GBC_ERR_NOMEM;
+    }
+    GBC_CUDA(cudaMemcpy(G->g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+    if (row[n]) GBC_CUDA(cudaMemcpy(G->g.col, col, sizeof(int32_t) * row[n], cudaMemcpyHostToDevice));
+    HostCSR h;
+    h.n = n;
+    h.row.assign(row, row + n + 1);
+    h.col.assign(col, col + row[n]);
+    std::vector<int64_t> sizes;
+    const int32_t nc = components(h, G->g.comp, sizes);
+    G->g.comp_edges.assign(nc, 0);
+    for (int32_t v = 0; v < n; v++) G->g.comp_edges[G->g.comp[v]] += row[v + 1] - row[v];
+    for (auto& e : G->g.comp_edges) e /= 2;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *gid = (int32_t)s->graphs.size();
+    s->graphs.push_back(std::move(G));
+    return GBC_OK;
+}
+
+gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k, uint64_t seed, const gbc_options* opt,
+                             double deadline_ms, int64_t* req_id) {
+    if (!s || !req_id) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    if (kind < GBC_Q_CC || kind > GBC_Q_BC_SAMPLED) { set_error("bad query kind"); return GBC_ERR_ARG; }
+    auto r = std::make_unique<Req>();
+    int32_t n = 0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (gid < 0 || gid >= (int32_t)s->graphs.size()) { set_error("unknown graph %d", gid); return GBC_ERR_NOT_FOUND; }
+        n = s->graphs[gid]->g.n;
+    }
+    gbc_options_default(&r->opt);
+    if (opt) r->opt = *opt;
+    if (r->opt.semantics != GBC_BC_BRANDES && r->opt.semantics != GBC_BC_REFERENCE) { set_error("bad semantics"); return GBC_ERR_ARG; }
+    r->gid = gid;
+    r->kind = kind;
+    if (kind == GBC_Q_BC_SAMPLED) {
+        if (k < 1) { set_error("sampled BC needs k >= 1"); return GBC_ERR_ARG; }
+        Rng rng(seed, 17);
+        r->src.resize(k);
+        for (int32_t i = 0; i < k; i++) r->src[i] = (int32_t)rng.below((uint64_t)n);
+    } else {
+        r->src.resize(n);
+        for (int32_t i = 0; i < n; i++) r->src[i] = i;
+    }
+    if (r->bc()) {
+        if (cudaMalloc(&r->d_bc, sizeof(double) * n) != cudaSuccess || cudaMemset(r->d_bc, 0, sizeof(double) * n) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("result allocation");
+            return GBC_ERR_NOMEM;
+        }
+    } else {
+        r->cc.assign(n, 0);
+    }
+    r->t_submit = now_ms();
+    r->deadline = deadline_ms > 0 ? r->t_submit + deadline_ms : 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->id = s->next_id++;
+    *req_id = r->id;
+    s->fifo.push_back(r->id);
+    s->reqs[r->id] = std::move(r);
+    s->cv_work.notify_all();
+    return GBC_OK;
+}
+
+gbc_status gbc_server_poll(gbc_server s, int64_t id, int32_t* state) {
+    if (!s || !state) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return GBC_ERR_NOT_FOUND; }
+    *state = it->second->state;
+    return GBC_OK;
+}
+
+gbc_status gbc_server_wait(gbc_server s, int64_t id, double timeout_ms, int32_t* state) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    std::unique_lock<std::mutex> lk(s->mu);
+    const double t_end = timeout_ms > 0 ? now_ms() + timeout_ms : 0;
+    for (;;) {
+        auto it = s->reqs.find(id);
+        if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return GBC_ERR_NOT_FOUND; }
+        const int32_t st = it->second->state;
+        if (st == GBC_REQ_DONE || st == GBC_REQ_FAILED || st == GBC_REQ_CANCELLED) {
+            if (state) *state = st;
+            return GBC_OK;
+        }
+        if (t_end > 0 && now_ms() >= t_end) {
+            if (state) *state = st;
+            set_error("wait timed out");
+            return GBC_ERR_TIMEOUT;
+        }
+        s->cv_done.wait_for(lk, std::chrono::milliseconds(20));
+    }
+}
+
+gbc_status gbc_server_fetch(gbc_server s, int64_t id, double* bc, int64_t* cc, double* latency_ms) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    std::unique_ptr<Req> r;
+    int32_t n = 0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(id);
+        if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return GBC_ERR_NOT_FOUND; }
+        const int32_t st = it->second->state;
+        if (it->second->inflight > 0 || st == GBC_REQ_QUEUED || st == GBC_REQ_RUNNING) {
+            set_error("request not finished");
+            return GBC_ERR_BUSY;
+        }
+        if (st == GBC_REQ_FAILED || st == GBC_REQ_CANCELLED) {
+            const gbc_status e = st == GBC_REQ_FAILED ? it->second->err : GBC_ERR_ARG;
+            set_error("request %s: %s", st == GBC_REQ_FAILED ? "failed" : "was cancelled", it->second->msg.c_str());
+            s->reqs.erase(it);
+            return e;
+        }
+        r = std::move(it->second);
+        s->reqs.erase(it);
+        n = s->graphs[r->gid]->g.n;
+    }
+    if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+    if (r->bc() && bc) GBC_CUDA(cudaMemcpy(bc, r->d_bc, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (!r->bc() && cc) std::memcpy(cc, r->cc.data(), sizeof(int64_t) * n);
+    return GBC_OK;
+}
+
+gbc_status gbc_server_cancel(gbc_server s, int64_t id) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return GBC_ERR_NOT_FOUND; }
+    Req* r = it->second.get();
+    if (r->state == GBC_REQ_QUEUED || r->state == GBC_REQ_RUNNING) {
+        r->state = GBC_REQ_CANCELLED;
+        r->t_done = now_ms();
+    }
+    s->cv_done.notify_all();
+    return GBC_OK;
+}
+
+gbc_status gbc_server_counters(gbc_server s, int64_t* completed, int64_t* batches, int64_t* shared, int64_t* edges,
+                               double* busy_ms) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (completed) *completed = s->completed;
+    if (batches) *batches = s->batches;
+    if (shared) *shared = s->shared_batches;
+    if (edges) *edges = s->edges;
+    if (busy_ms) *busy_ms = s->busy_ms;
+    return GBC_OK;
+}
+
+}  // extern "C"

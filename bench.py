@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""Throughput of batched Brandes betweenness on one GB300 (GTEPS).
+
+Workload: R-MAT scale 22, edge factor 16 (a=.57, b=.19, c=.19; symmetrised,
+self-loops and duplicates dropped; seeded vertex relabelling), k = 16,384
+sampled sources (seed 4, uniform over vertices with at least one edge).  A
+step is one lane batch: `--lanes` sources (default 1024) run forward BFS with
+exact uint64 path counts and the dependency sweep, accumulating FP64 BC.
+GTEPS = sum over the step's sources of the undirected edges of the source's
+component / time.
+
+  value : device-resident inputs, gbc_bc_device on a resident graph, CUDA
+          events on the launching stream over exactly --steps steps.
+  e2e   : the host-buffer C ABI a drop-in caller uses -- per step the CSR and
+          the sources are copied from pinned host memory (gbc_graph_create +
+          gbc_bc) and the BC vector is read back.
+  plain : the one-source-at-a-time engine on a sample of the same sources.
+  roofline / cpu_baseline / clocks as documented in the design doc.
+
+--impl reference times the CPU restatement of the reference's sequential
+Brandes (oracle/, the reference's own code is not buildable on the GPU host)
+with all host threads, on a bounded sample of the same sources per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BC/CC GTEPS & p50/p99 query latency, batched+served vs plain, 1×GB300"
+WORKLOAD = "rmat22_ef16_sampled_bc_k16384"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=4)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--lanes", type=int, default=1024)
+    p.add_argument("--scale", type=int, default=22)
+    p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--k", type=int, default=16384)
+    p.add_argument("--delta", default="f64", choices=["f32", "f64"])
+    p.add_argument("--plain-sources", type=int, default=16)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_graph(args):
+    import bc_gb300 as G
+    csr = G.gen_rmat(args.scale, args.edge_factor, 0.57, 0.19, 0.19, seed=1, permute=True)
+    deg = np.diff(csr.row)
+    cand = np.nonzero(deg > 0)[0].astype(np.int32)
+    rng = np.random.default_rng(4)
+    sample = cand[rng.integers(0, len(cand), size=args.k)].astype(np.int32)
+    return csr, sample
+
+
+def comp_edges(csr):
+    """Undirected edges of each vertex's component (GTEPS numerator)."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import connected_components
+    n = csr.n
+    A = sp.csr_matrix((np.ones(csr.m, np.int8), csr.col, csr.row), shape=(n, n))
+    nc, lab = connected_components(A, directed=False)
+    e = np.bincount(lab, weights=np.diff(csr.row), minlength=nc) / 2
+    return e[lab].astype(np.int64)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_traffic():
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_summary.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(csr, sample, n_src, threads):
+    """Oracle (CPU restatement of Seq_Brandes/Brandes.c:224) on a bounded sample."""
+    from oracle import oracle as O
+    og = O.Graph(csr.row, csr.col)
+    src = sample[:n_src]
+    t = time.perf_counter()
+    O.bc(og, src, semantics=O.BC_REFERENCE, nthreads=threads)
+    dt = time.perf_counter() - t
+    return dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    csr, sample = make_graph(args)
+    ce = comp_edges(csr)
+    threads = os.cpu_count() or 1
+    n_src = max(threads, 8)
+    # warm-up (page-in) and timed steps: each step a bounded slice of the sample
+    times, edges = [], 0
+    for i in range(args.warmup + args.steps):
+        lo = (i * n_src) % len(sample)
+        src = sample[lo:lo + n_src]
+        dt = cpu_baseline(csr, src, len(src), threads)
+        if i >= args.warmup:
+            times.append(dt)
+            edges += int(ce[src].sum())
+    tot = sum(times)
+    gteps = edges / tot / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": round(gteps, 6), "unit": "GTEPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * tot / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded R-MAT generator)",
+            "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor,
+                       "sources_per_step": n_src},
+            "cpu_baseline": {"value": round(gteps, 6), "unit": "GTEPS", "cores": threads, "kind": "port",
+                             "sample": f"{n_src} sampled sources per step (reference semantics, FP64)"},
+            "e2e": {"value": round(gteps, 6), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import ctypes as C
+
+    import torch
+
+    import bc_gb300 as G
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    csr, sample = make_graph(args)
+    ce = comp_edges(csr)
+    B = args.lanes
+    # weak scaling: every rank runs its own `steps` batches of distinct sources
+    def step_sources(i):
+        lo = ((rank * (args.warmup + args.steps) + i) * B) % len(sample)
+        idx = (np.arange(B) + lo) % len(sample)
+        return sample[idx]
+
+    opt = dict(semantics=G.BC_BRANDES, delta_precision=G.DELTA_F64 if args.delta == "f64" else G.DELTA_F32,
+               sigma_mode=G.SIGMA_AUTO, lanes=B)
+    o = G.options(**opt)
+    graph = G.Graph(csr)
+    stream = torch.cuda.current_stream(dev)
+    d_src = torch.empty(B, dtype=torch.int32, device=dev)
+    d_bc = torch.empty(csr.n, dtype=torch.float64, device=dev)
+    L = G.lib()
+
+    def run_step(i):
+        d_src.copy_(torch.from_numpy(step_sources(i)))
+        G.check(L.gbc_bc_device(graph.h, C.c_void_p(d_src.data_ptr()), B, C.byref(o),
+                                C.c_void_p(d_bc.data_ptr()), C.c_void_p(stream.cuda_stream)))
+        return _stats(graph)
+
+    def _stats(g):
+        st = G.RunStats()
+        G.check(L.gbc_graph_last_stats(g.h, C.byref(st)))
+        return st
+
+    for i in range(args.warmup):
+        run_step(i)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = Clocks(local)
+    clk.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    fwd_ms = bwd_ms = 0.0
+    fwd_k = bwd_k = launches = 0
+    edges = 0
+    for i in range(args.warmup, args.warmup + args.steps):
+        st = run_step(i)
+        fwd_ms += st.fwd_ms
+        bwd_ms += st.bwd_ms
+        fwd_k += st.fwd_kernels
+        bwd_k += st.bwd_kernels
+        launches += st.kernel_launches
+        edges += int(ce[step_sources(i)].sum())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        te = torch.tensor([edges], device=dev, dtype=torch.float64)
+        dist.all_reduce(te, op=dist.ReduceOp.SUM)
+        edges_all = float(te.item())
+        dist.barrier()
+    else:
+        edges_all = float(edges)
+    gteps = edges_all / (ms * 1e-3) / 1e9
+
+    # roofline of the dominant level kernel (algorithmic bytes per batch per sweep)
+    n, M = csr.n, csr.m
+    adj = 4 * M + 4 * (n + 1)
+    fwd_bytes = (adj + 16 * B * n) * args.steps
+    bwd_bytes = (adj + 16 * B * n + 16 * n) * args.steps
+    dom = "expand_kernel" if fwd_ms >= bwd_ms else "backward_kernel"
+    dom_ms, dom_bytes, dom_k = (fwd_ms, fwd_bytes, fwd_k) if dom == "expand_kernel" else (bwd_ms, bwd_bytes, bwd_k)
+    hbm, peak_kind = peaks()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    tr = load_traffic()
+    traffic = None
+    if tr and tr.get("kernel") == dom and tr.get("per_launch_bytes_full_size"):
+        traffic = tr["per_launch_bytes_full_size"]
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 5), "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": int(dom_bytes / max(dom_k, 1)),
+            "avg_launch_ms": round(dom_ms / max(dom_k, 1), 4)}
+
+    out = None
+    if rank == 0:
+        # plain one-source-at-a-time engine on a sample of the same sources
+        plain_gteps = None
+        if not args.no_plain:
+            ps = sample[:args.plain_sources]
+            graph.bc(ps, engine=G.ENGINE_PLAIN, **{k: v for k, v in opt.items() if k != "lanes"})
+            stp = graph.stats()
+            plain_gteps = float(ce[ps].sum()) / (stp["kernel_ms"] * 1e-3) / 1e9
+        # e2e through the host-buffer C ABI, copies from pinned memory
+        e2e = None
+        if not args.no_e2e:
+            row_p = torch.from_numpy(csr.row).pin_memory()
+            col_p = torch.from_numpy(csr.col).pin_memory()
+            bc_p = torch.empty(csr.n, dtype=torch.float64).pin_memory()
+            src_p = torch.empty(B, dtype=torch.int32).pin_memory()
+            row_np, col_np, bc_np, src_np = row_p.numpy(), col_p.numpy(), bc_p.numpy(), src_p.numpy()
+            e2e_steps = max(1, min(args.steps, 2))
+            t0 = time.perf_counter()
+            e_edges = 0
+            for i in range(e2e_steps):
+                src_np[:] = step_sources(args.warmup + i)
+                h = C.c_void_p()
+                G.check(L.gbc_graph_create(row_np, col_np, csr.n, C.byref(h)))
+                G.check(L.gbc_bc(h, src_np.ctypes.data_as(C.c_void_p), B, C.byref(o), bc_np))
+                L.gbc_graph_destroy(h)
+                e_edges += int(ce[src_np].sum())
+            dt = time.perf_counter() - t0
+            e2e = {"value": round(e_edges / dt / 1e9, 4), "unit": "GTEPS",
+                   "h2d_bytes_per_step": int(csr.row.nbytes + csr.col.nbytes + 4 * B),
+                   "d2h_bytes_per_step": int(8 * csr.n), "steps": e2e_steps,
+                   "path": "gbc_graph_create + gbc_bc (host buffers)"}
+        # CPU baseline: oracle on a bounded sample of the same sources
+        cpu = None
+        if not args.no_cpu:
+            threads = os.cpu_count() or 1
+            n_cpu = max(threads, 4)
+            dt = cpu_baseline(csr, sample, n_cpu, threads)
+            cpu = {"value": round(float(ce[sample[:n_cpu]].sum()) / dt / 1e9, 6), "unit": "GTEPS", "cores": threads,
+                   "kind": "port",
+                   "sample": f"first {n_cpu} of the {args.k} sampled sources, reference semantics, FP64"}
+        out = {"metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",
+               "data": "synthetic (seeded R-MAT generator)",
+               "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor,
+                          "n": n, "m_directed": M, "lanes_per_step": B, "sources": args.k,
+                          "parallelism": f"sources sharded over {ws} GPU(s)",
+                          "l2": "inputs larger than L2 (lane state ~16*B*n bytes per sweep)"},
+               "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+               "plain": None if plain_gteps is None else {
+                   "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),
+                   "speedup_batched_vs_plain": round(gteps / plain_gteps, 2)},
+               "clocks": clocks}
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    graph.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

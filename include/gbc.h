@@ -89,7 +89,10 @@ typedef struct {
     double  total_ms;         /* wall time of the call */
     int32_t lanes;            /* lanes per batch actually used */
     int32_t sigma_mode_used;  /* GBC_SIGMA_EXACT or GBC_SIGMA_LOG */
-    int32_t reserved[8];
+    double  fwd_ms;           /* device time of the forward (BFS / path count) level kernels */
+    double  bwd_ms;           /* device time of the dependency-sweep level kernels */
+    int64_t fwd_kernels;      /* forward level kernels launched (incl. no-op tail launches) */
+    int64_t bwd_kernels;      /* dependency-sweep level kernels launched */
 } gbc_run_stats;
 
 typedef struct gbc_graph_s* gbc_graph;

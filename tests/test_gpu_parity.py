@@ -30,10 +30,32 @@ def graphs(gpu, datasets):
     g["er2k"] = gpu.gen_er(2000, 3.0, seed=4)          # disconnected
     g["karate"] = gpu.read_edgelist(datasets["karate.txt"])
     g["ia-fb"] = gpu.read_edgelist(datasets["ia-fb-messages.mtx"])
+    g["rmat14"] = gpu.gen_rmat(14, 16, seed=2)           # 15 vertices above the hub degree
+    # a star of 3000 leaves (a hub) joined to a 24x24 grid, plus isolated vertices
+    grid = gpu.gen_grid(24, 24, 0.0, seed=1)
+    n0 = grid.n
+    rows, cols = [], []
+    adj = [list(grid.col[grid.row[v]:grid.row[v + 1]]) for v in range(n0)]
+    hub = n0
+    adj.append([0] + list(range(n0 + 1, n0 + 3001)))
+    adj[0].append(hub)
+    for leaf in range(n0 + 1, n0 + 3001):
+        adj.append([hub])
+    adj += [[] for _ in range(5)]
+    row = np.zeros(len(adj) + 1, np.int64)
+    for v, a in enumerate(adj):
+        row[v + 1] = row[v] + len(a)
+    g["star+grid"] = gpu.CSR(row, np.array([x for a in adj for x in sorted(a)], np.int32))
     return g
 
 
-@pytest.mark.parametrize("name", ["ba4096", "rmat12", "grid24", "er2k", "karate"])
+def sources_of(csr, cap, seed=5):
+    if csr.n - csr.start <= cap:
+        return np.arange(csr.start, csr.n, dtype=np.int32)
+    return np.random.default_rng(seed).choice(np.arange(csr.start, csr.n), cap, replace=False).astype(np.int32)
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "grid24", "er2k", "karate", "rmat14", "star+grid"])
 @pytest.mark.parametrize("lanes", [32, 128])
 def test_sssp_bit_exact(gpu, orc, graphs, name, lanes):
     csr = graphs[name]
@@ -50,11 +72,11 @@ def test_sssp_bit_exact(gpu, orc, graphs, name, lanes):
             assert np.array_equal(sig[i], s0), f"sigma mismatch for source {s}"
 
 
-@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "ia-fb"])
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "ia-fb", "rmat14", "star+grid"])
 def test_cc_bit_exact(gpu, orc, graphs, name):
     csr = graphs[name]
     og = to_orc(orc, csr)
-    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    src = sources_of(csr, 3000)
     ref = orc.cc(og, src, nthreads=4)
     with gpu.Graph(csr) as G:
         got = G.cc(src)
@@ -63,12 +85,12 @@ def test_cc_bit_exact(gpu, orc, graphs, name):
         assert np.array_equal(got_plain, ref[:50])
 
 
-@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate"])
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "rmat14", "star+grid"])
 @pytest.mark.parametrize("sem", [0, 1])
 def test_bc_fp64(gpu, orc, graphs, name, sem):
     csr = graphs[name]
     og = to_orc(orc, csr)
-    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    src = sources_of(csr, 1500)
     ref, novf = orc.bc(og, src, semantics=sem, nthreads=4)
     assert novf == 0
     with gpu.Graph(csr) as G:
@@ -78,11 +100,11 @@ def test_bc_fp64(gpu, orc, graphs, name, sem):
         assert st["sources"] == len(src) and st["sigma_mode_used"] == gpu.SIGMA_EXACT
 
 
-@pytest.mark.parametrize("name", ["ba4096", "rmat12"])
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "rmat14"])
 def test_bc_fp32_delta(gpu, orc, graphs, name):
     csr = graphs[name]
     og = to_orc(orc, csr)
-    src = np.arange(csr.start, csr.n, dtype=np.int32)
+    src = sources_of(csr, 1500)
     ref, _ = orc.bc(og, src, nthreads=4)
     with gpu.Graph(csr) as G:
         got = G.bc(src, delta_precision=gpu.DELTA_F32)
@@ -136,3 +158,37 @@ def test_sigma_overflow_log_mode(gpu, orc):
         assert relerr(got, ref) < TOL_F64
         dist, sig, ovf = G.sssp(src)
         assert ovf.all()
+
+
+@pytest.mark.parametrize("sparse", [0, 32])
+def test_expansion_modes_agree(gpu, orc, graphs, sparse):
+    """Lane-parallel only (sparse=0) and edge-parallel only (sparse=32) give
+    the same exact results."""
+    csr = graphs["star+grid"]
+    og = to_orc(orc, csr)
+    src = sources_of(csr, 400, seed=9)
+    ref, _ = orc.bc(og, src, semantics=1)
+    refcc = orc.cc(og, src)
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, semantics=1, sparse_lanes=sparse, lanes=96)
+        assert relerr(got, ref) < TOL_F64
+        assert np.array_equal(G.cc(src, sparse_lanes=sparse, lanes=96), refcc)
+
+
+def test_deep_graph_switches_level_width(gpu, orc):
+    """A 700-vertex path is deeper than 8-bit levels allow: the engine
+    switches to 16-bit levels and stays exact."""
+    n = 700
+    row = np.concatenate([[0], np.cumsum([1] + [2] * (n - 2) + [1])]).astype(np.int64)
+    col = []
+    for v in range(n):
+        col += ([v - 1] if v > 0 else []) + ([v + 1] if v < n - 1 else [])
+    csr = gpu.CSR(row, np.array(col, np.int32))
+    og = to_orc(orc, csr)
+    src = np.array([0, 5, 350, 699], np.int32)
+    ref, _ = orc.bc(og, src)
+    with gpu.Graph(csr) as G:
+        assert relerr(G.bc(src), ref) < TOL_F64
+        assert np.array_equal(G.cc(src), orc.cc(og, src))
+        dist, _, _ = G.sssp(src)
+        assert dist[0, 699] == 699
