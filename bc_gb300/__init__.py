@@ -96,6 +96,9 @@ _PROTOS = [
     ("gbc_reduced_destroy", _st, [_vp]),
     ("gbc_reduced_block_graph", _st, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
     ("gbc_reduced_assemble_cc", _st, [_vp, _i64p, _i64p]),
+    ("gbc_reduced_core_graph", _st, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                     C.POINTER(C.c_int32)]),
+    ("gbc_reduced_assemble_bc", _st, [_vp, _f64p, _f64p]),
     ("gbc_gen_ba", _st, [C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_vp), C.POINTER(_vp)]),
     ("gbc_gen_rmat", _st, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int32,
                            C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
@@ -116,6 +119,7 @@ _PROTOS = [
     ("gbc_server_wait", _st, [_vp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
     ("gbc_server_fetch", _st, [_vp, C.c_int64, _vp, _vp, C.POINTER(C.c_double)]),
     ("gbc_server_cancel", _st, [_vp, C.c_int64]),
+    ("gbc_server_sources", _st, [_vp, C.c_int64, _vp, C.c_int32, C.POINTER(C.c_int32)]),
     ("gbc_server_counters", _st, [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
 ]
@@ -312,6 +316,22 @@ class Reduced:
         w = np.ctypeslib.as_array(C.cast(wp, C.POINTER(C.c_int32)), shape=(max(ns.value, 1),))[: ns.value].copy()
         lib().gbc_free(wp)
         return _take_csr(rp, cp, ns.value), w
+
+    def core_graph(self):
+        """(CSR over core ids, reach weights, vertex of each core id)."""
+        rp, cp, wp, vp, nc = _vp(), _vp(), _vp(), _vp(), C.c_int32()
+        check(lib().gbc_reduced_core_graph(self.h, C.byref(rp), C.byref(cp), C.byref(wp), C.byref(vp), C.byref(nc)))
+        n = nc.value
+        w = np.ctypeslib.as_array(C.cast(wp, C.POINTER(C.c_int32)), shape=(max(n, 1),))[:n].copy()
+        v = np.ctypeslib.as_array(C.cast(vp, C.POINTER(C.c_int32)), shape=(max(n, 1),))[:n].copy()
+        lib().gbc_free(wp)
+        lib().gbc_free(vp)
+        return _take_csr(rp, cp, n), w, v
+
+    def assemble_bc(self, core_bc) -> np.ndarray:
+        out = np.zeros(self.csr.n, np.float64)
+        check(lib().gbc_reduced_assemble_bc(self.h, np.ascontiguousarray(core_bc, dtype=np.float64), out))
+        return out
 
     def assemble_cc(self, D) -> np.ndarray:
         out = np.zeros(self.csr.n, np.int64)

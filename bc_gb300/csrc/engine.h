@@ -123,6 +123,7 @@ private:
     uint32_t* ovf_ = nullptr;
     double* bcg_ = nullptr;
     unsigned long long* ccbuf_ = nullptr;
+    int32_t* srcw_ = nullptr;             // per-lane source weights of the running batch
     struct Captured { int key = -1; cudaGraphExec_t exec = nullptr; };
     std::vector<Captured> graphs_;
     int sm_count_ = 0;

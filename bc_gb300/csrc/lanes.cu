@@ -33,7 +33,7 @@ namespace {
 
 constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int BLOCK = 256;
-constexpr int U = 16;   // neighbours whose lane state is loaded before any of it is used
+
 
 // Level storage: uint8_t while every BFS stays under 254 levels, uint16_t
 // after a batch went deeper.  All-ones is "unreached".
@@ -77,6 +77,7 @@ struct KArgs {
     uint32_t* ovf;
     unsigned long long* cc;
     double* bcg;
+    int32_t* srcw;         // per-lane source weight (vertex weight of the lane's source, 1 without weights)
     int sparse;
     int semantics;
 };
@@ -161,67 +162,219 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, 
     }
 }
 
+// Levels of 32 lanes are one 32-byte (uint8) or 64-byte (uint16) row per
+// vertex.  In lane-parallel expansion a thread owns one 32-bit word of a
+// neighbour's row (LPW lanes) and compares all of them at once; a warp covers
+// SLOTS neighbours per load instruction.
+template <typename LT> struct Simd;
+template <> struct Simd<uint8_t> {
+    static constexpr int LPW = 4;
+    __device__ static __forceinline__ unsigned bc(int d) { return ((unsigned)d & 0xFFu) * 0x01010101u; }
+    __device__ static __forceinline__ unsigned eq(unsigned a, unsigned b) { return __vcmpeq4(a, b); }
+    __device__ static __forceinline__ unsigned gt(unsigned a, unsigned b) { return __vcmpgtu4(a, b); }
+    __device__ static __forceinline__ bool has(unsigned m, int j) { return (m >> (8 * j)) & 1u; }
+};
+template <> struct Simd<uint16_t> {
+    static constexpr int LPW = 2;
+    __device__ static __forceinline__ unsigned bc(int d) { return ((unsigned)d & 0xFFFFu) * 0x00010001u; }
+    __device__ static __forceinline__ unsigned eq(unsigned a, unsigned b) { return __vcmpeq2(a, b); }
+    __device__ static __forceinline__ unsigned gt(unsigned a, unsigned b) { return __vcmpgtu2(a, b); }
+    __device__ static __forceinline__ bool has(unsigned m, int j) { return (m >> (16 * j)) & 1u; }
+};
+
+// Lane-parallel forward scan of v's neighbour chunks (r0 + 32*sub, step
+// 32*nsub).  Result for lane t is returned in thread t.
+template <int MODE, typename LT>
+__device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t gbase, LT* lv, int v, long long r0,
+                                          long long r1, int sub, int nsub, uint64_t& acc, bool& of, double& lm,
+                                          double& ls) {
+    using S = Simd<LT>;
+    constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
+    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV;
+    const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
+    const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1);
+    const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
+    const uint64_t* sg = A.sig + (gbase << 5) + w * LPW;
+    const double* sgd = reinterpret_cast<const double*>(sg);
+    uint64_t a[LPW];
+    double m[LPW], sl[LPW];
+    unsigned ofm = 0;
+#pragma unroll
+    for (int j = 0; j < LPW; j++) { a[j] = 0; m[j] = -INFINITY; sl[j] = 0.0; }
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+        const int cnt = (int)min(32LL, r1 - jb);
+        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        unsigned Lw[ITER];
+        int xs[ITER];
+#pragma unroll
+        for (int k = 0; k < ITER; k++) {
+            const int q = k * SLOTS + s;
+            xs[k] = __shfl_sync(FULL, xm, q);
+            Lw[k] = (q < cnt) ? lvw[(size_t)xs[k] * WPV + w] : d4;
+        }
+        if (MODE != 0 && d > 0) {
+#pragma unroll
+            for (int k = 0; k < ITER; k++) {
+                const unsigned pm = S::eq(Lw[k], dp4) & act4;
+                if (pm) {
+                    const size_t xo = (size_t)xs[k] << 5;
+#pragma unroll
+                    for (int j = 0; j < LPW; j++) {
+                        if (!S::has(pm, j)) continue;
+                        if (MODE == 1) {
+                            const uint64_t sv = sg[xo + j];
+                            const uint64_t na = a[j] + sv;
+                            ofm |= (unsigned)(na < a[j]) << j;
+                            a[j] = na;
+                        } else {
+                            lse_add(m[j], sl[j], sgd[xo + j]);
+                        }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < ITER; k++) {
+            const int q = k * SLOTS + s;
+            const unsigned un = S::eq(Lw[k], 0xFFFFFFFFu) & act4;   // unreached, in active lanes
+            const unsigned gm = S::gt(Lw[k], d4) & act4;            // unreached or already at d+1
+            if (un) {
+                LT* px = lv + ((size_t)xs[k] << 5) + w * LPW;
+#pragma unroll
+                for (int j = 0; j < LPW; j++)
+                    if (S::has(un, j)) px[j] = (LT)(d + 1);
+            }
+            const unsigned bal = __ballot_sync(FULL, gm != 0u);
+            const unsigned slotm = (bal >> (s * WPV)) & ((1u << WPV) - 1u);
+            const bool has = (w == 0) && (q < cnt) && slotm && claim(A, gbase, xs[k], d + 1);
+            warp_append(A, has, has && is_hub(A, xs[k]), ((uint32_t)xs[k] << 5) | (uint32_t)g);
+        }
+    }
+    // sum the slots (every slot then holds the totals), hand lane t to thread t
+#pragma unroll
+    for (int o = WPV; o < 32; o <<= 1) {
+        if (MODE == 1) {
+            unsigned of2 = __shfl_xor_sync(FULL, ofm, o);
+#pragma unroll
+            for (int j = 0; j < LPW; j++) {
+                const uint64_t p = __shfl_xor_sync(FULL, a[j], o);
+                const uint64_t na = a[j] + p;
+                ofm |= (unsigned)(na < a[j]) << j;
+                a[j] = na;
+            }
+            ofm |= of2;
+        } else if (MODE == 2) {
+#pragma unroll
+            for (int j = 0; j < LPW; j++) {
+                const double m2 = __shfl_xor_sync(FULL, m[j], o);
+                const double s2 = __shfl_xor_sync(FULL, sl[j], o);
+                lse_merge(m[j], sl[j], m2, s2);
+            }
+        }
+    }
+    const int src = t / LPW, jj = t % LPW;
+    if (MODE == 1) {
+        uint64_t r = 0;
+#pragma unroll
+        for (int j = 0; j < LPW; j++) {
+            const uint64_t vj = __shfl_sync(FULL, a[j], src);
+            if (j == jj) r = vj;
+        }
+        acc = r;
+        of = (__shfl_sync(FULL, ofm, src) >> jj) & 1u;
+    } else if (MODE == 2) {
+#pragma unroll
+        for (int j = 0; j < LPW; j++) {
+            const double mj = __shfl_sync(FULL, m[j], src);
+            const double sj = __shfl_sync(FULL, sl[j], src);
+            if (j == jj) { lm = mj; ls = sj; }
+        }
+    }
+}
+
+// Lane-parallel dependency scan: sum of rho over successors, predecessor
+// count, for lane t in thread t.
+template <bool LOG, typename T, typename LT>
+__device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, const LT* lv, int v, double lsv,
+                                          long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
+    using S = Simd<LT>;
+    constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
+    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV;
+    const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
+    const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1), dn4 = S::bc(d + 1);
+    const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
+    const T* rh = reinterpret_cast<const T*>(A.rho) + (gbase << 5) + w * LPW;
+    const double* rhd = reinterpret_cast<const double*>(A.rho) + (gbase << 5) + w * LPW;
+    T a[LPW];
+    int pcs[LPW];
+    double lsj[LPW];
+#pragma unroll
+    for (int j = 0; j < LPW; j++) {
+        a[j] = T(0);
+        pcs[j] = 0;
+        lsj[j] = LOG ? __shfl_sync(FULL, lsv, w * LPW + j) : 0.0;
+    }
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+        const int cnt = (int)min(32LL, r1 - jb);
+        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        unsigned Lw[ITER];
+        int xs[ITER];
+#pragma unroll
+        for (int k = 0; k < ITER; k++) {
+            const int q = k * SLOTS + s;
+            xs[k] = __shfl_sync(FULL, xm, q);
+            Lw[k] = (q < cnt) ? lvw[(size_t)xs[k] * WPV + w] : d4;
+        }
+#pragma unroll
+        for (int k = 0; k < ITER; k++) {
+            const unsigned sm = S::eq(Lw[k], dn4) & act4;
+            const unsigned pm = S::eq(Lw[k], dp4) & act4;
+            const size_t xo = (size_t)xs[k] << 5;
+#pragma unroll
+            for (int j = 0; j < LPW; j++) {
+                if (S::has(sm, j)) {
+                    if (LOG) a[j] += (T)exp2(lsj[j] + rhd[xo + j]);
+                    else a[j] += rh[xo + j];
+                }
+                pcs[j] += S::has(pm, j);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = WPV; o < 32; o <<= 1) {
+#pragma unroll
+        for (int j = 0; j < LPW; j++) {
+            a[j] += __shfl_xor_sync(FULL, a[j], o);
+            pcs[j] += __shfl_xor_sync(FULL, pcs[j], o);
+        }
+    }
+    const int src = t / LPW, jj = t % LPW;
+    T r = T(0);
+    int p = 0;
+#pragma unroll
+    for (int j = 0; j < LPW; j++) {
+        const T vj = __shfl_sync(FULL, a[j], src);
+        const int pj = __shfl_sync(FULL, pcs[j], src);
+        if (j == jj) { r = vj; p = pj; }
+    }
+    acc = r;
+    pc = p;
+}
+
 // ---- forward --------------------------------------------------------------
 // Neighbour chunks r0 + 32*sub, stepping 32*nsub (nsub warps share a hub).
 // Pulls sigma from level d-1 neighbours into (acc, of) or (lm, ls) and
 // discovers level d+1.
 template <int MODE, typename LT>
-__device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gbase, LT* lv, bool act, unsigned am,
-                                         long long r0, long long r1, int sub, int nsub, uint64_t& acc, bool& of,
-                                         double& lm, double& ls) {
+__device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gbase, LT* lv, int v, bool act,
+                                         unsigned am, long long r0, long long r1, int sub, int nsub, uint64_t& acc,
+                                         bool& of, double& lm, double& ls) {
     constexpr LT INF = (LT)Lv<LT>::INF;
     const int t = threadIdx.x & 31;
     const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const double* sigd = reinterpret_cast<const double*>(A.sig);
     if (__popc(am) > A.sparse) {
-        // lane-parallel: thread t owns lane t; per batch of U neighbours every
-        // level is loaded first, then path counts, then the stores.
-        for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
-            const int cnt = (int)min(32LL, r1 - jb);
-            const int xm = (t < cnt) ? A.col[jb + t] : 0;
-            for (int q0 = 0; q0 < cnt; q0 += U) {
-                LT Lx[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                    Lx[u] = (q0 + u < cnt) ? lv[((size_t)x << 5) + t] : dl;
-                }
-                if (MODE != 0 && d > 0) {
-                    if (MODE == 1) {
-                        uint64_t sv[U];
-#pragma unroll
-                        for (int u = 0; u < U; u++) {
-                            const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                            sv[u] = (act && Lx[u] == dprev) ? A.sig[((gbase + (size_t)x) << 5) + t] : 0ULL;
-                        }
-#pragma unroll
-                        for (int u = 0; u < U; u++) {
-                            const uint64_t na = acc + sv[u];
-                            of |= (na < acc);
-                            acc = na;
-                        }
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < U; u++) {
-                            const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                            if (act && Lx[u] == dprev) lse_add(lm, ls, sigd[((gbase + (size_t)x) << 5) + t]);
-                        }
-                    }
-                }
-                unsigned dbits = 0;
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                    const bool disc = act && (q0 + u < cnt) && Lx[u] > dl;
-                    if (disc && Lx[u] == INF) lv[((size_t)x << 5) + t] = dnext;
-                    if (__ballot_sync(FULL, disc)) dbits |= 1u << u;
-                }
-                // thread u claims neighbour u of the batch
-                const int mx = __shfl_sync(FULL, xm, (q0 + t) & 31);
-                const bool has = (t < U) && ((dbits >> t) & 1u) && claim(A, gbase, mx, d + 1);
-                warp_append(A, has, has && is_hub(A, mx), ((uint32_t)mx << 5) | (uint32_t)g);
-            }
-        }
+        fwd_lanes<MODE, LT>(A, d, g, gbase, lv, v, r0, r1, sub, nsub, acc, of, lm, ls);
     } else {
         // edge-parallel: threads over neighbours, active lanes in turn
         unsigned rem = am;
@@ -333,7 +486,7 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
             uint64_t acc = 0;
             bool of = false;
             double lm = -INFINITY, ls = 0.0;
-            fwd_scan<MODE, LT>(A, d, g, gbase, lv, act, am, A.row[v], A.row[v + 1], wib, WARPS, acc, of, lm, ls);
+            fwd_scan<MODE, LT>(A, d, g, gbase, lv, v, act, am, A.row[v], A.row[v + 1], wib, WARPS, acc, of, lm, ls);
             if (MODE != 0) {
                 if (MODE == 1) h_acc[wib][t] = acc;
                 else { h_acc[wib][t] = __double_as_longlong(lm); h_ls[wib][t] = ls; }
@@ -377,7 +530,7 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
                 uint64_t acc = 0;
                 bool of = false;
                 double lm = -INFINITY, ls = 0.0;
-                fwd_scan<MODE, LT>(A, d, g, gbase, lv, act, am, A.row[v], A.row[v + 1], 0, 1, acc, of, lm, ls);
+                fwd_scan<MODE, LT>(A, d, g, gbase, lv, v, act, am, A.row[v], A.row[v + 1], 0, 1, acc, of, lm, ls);
                 if (MODE != 0 && act && d > 0) fwd_store<MODE>(A, g, gbase, v, acc, of, lm, ls);
             }
         }
@@ -394,46 +547,15 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
 // LOG: sigma held as log2 and rho as a(w) = log2(1 + delta(w)) - log2 sigma(w),
 // so that sigma(v)/sigma(w) * (1 + delta(w)) = exp2(log2 sigma(v) + a(w)).
 template <bool LOG, typename T, typename LT>
-__device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, bool act, unsigned am,
-                                         double lsv, long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
+__device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, int v, bool act,
+                                         unsigned am, double lsv, long long r0, long long r1, int sub, int nsub, T& acc,
+                                         int& pc) {
     const int t = threadIdx.x & 31;
     const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const T* rho = reinterpret_cast<const T*>(A.rho);
     const double* rhod = reinterpret_cast<const double*>(A.rho);
     if (__popc(am) > A.sparse) {
-        for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
-            const int cnt = (int)min(32LL, r1 - jb);
-            const int xm = (t < cnt) ? A.col[jb + t] : 0;
-            for (int q0 = 0; q0 < cnt; q0 += U) {
-                LT Lx[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                    Lx[u] = (q0 + u < cnt) ? lv[((size_t)x << 5) + t] : dl;
-                }
-                if (LOG) {
-                    double rv[U];
-#pragma unroll
-                    for (int u = 0; u < U; u++) {
-                        const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                        rv[u] = (act && Lx[u] == dnext) ? rhod[((gbase + (size_t)x) << 5) + t] : -INFINITY;
-                        pc += (Lx[u] == dprev);
-                    }
-#pragma unroll
-                    for (int u = 0; u < U; u++) acc += (T)exp2(lsv + rv[u]);
-                } else {
-                    T rv[U];
-#pragma unroll
-                    for (int u = 0; u < U; u++) {
-                        const int x = __shfl_sync(FULL, xm, (q0 + u) & 31);
-                        rv[u] = (act && Lx[u] == dnext) ? rho[((gbase + (size_t)x) << 5) + t] : T(0);
-                        pc += (Lx[u] == dprev);
-                    }
-#pragma unroll
-                    for (int u = 0; u < U; u++) acc += rv[u];
-                }
-            }
-        }
+        bwd_lanes<LOG, T, LT>(A, d, gbase, lv, v, lsv, r0, r1, sub, nsub, acc, pc);
     } else {
         unsigned rem = am;
         while (rem) {
@@ -468,22 +590,26 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
 
 // delta, rho and the BC contribution of (v, lane t); warp-summed into bcg.
 template <bool LOG, typename T>
-__device__ __forceinline__ void bwd_finish(const KArgs& A, size_t gbase, int v, bool act, double lsv, T acc, int pc,
-                                           bool refsem) {
+__device__ __forceinline__ void bwd_finish(const KArgs& A, int g, size_t gbase, int v, bool act, double lsv, T acc,
+                                           int pc, bool refsem) {
     const int t = threadIdx.x & 31;
     const size_t vi = ((gbase + (size_t)v) << 5) + t;
     double contrib = 0.0;
     if (act) {
+        // with vertex weights (reach of folded vertices) a target v counts w[v]
+        // times and a source s contributes w[s] times
+        const T tw = A.w ? (T)A.w[v] : T(1);
+        const int lane = (g << 5) + t;
         T delta;
         if (LOG) {
             delta = acc;
-            reinterpret_cast<double*>(A.rho)[vi] = log2(1.0 + (double)delta) - lsv;
+            reinterpret_cast<double*>(A.rho)[vi] = log2((double)tw + (double)delta) - lsv;
         } else {
             const T sv = (T)A.sig[vi];
             delta = sv * acc;
-            reinterpret_cast<T*>(A.rho)[vi] = (T(1) + delta) / sv;
+            reinterpret_cast<T*>(A.rho)[vi] = (tw + delta) / sv;
         }
-        contrib = (double)delta * (refsem ? (double)pc : 1.0);
+        contrib = (double)delta * (double)A.srcw[lane] * (refsem ? (double)pc : 1.0);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(FULL, contrib, o);
@@ -518,7 +644,7 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
             const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
             T acc = T(0);
             int pc = 0;
-            bwd_scan<LOG, T, LT>(A, d, gbase, lv, act, am, lsv, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+            bwd_scan<LOG, T, LT>(A, d, gbase, lv, v, act, am, lsv, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
             h_acc[wib][t] = (double)acc;
             h_pc[wib][t] = pc;
             __syncthreads();
@@ -527,7 +653,7 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
                     acc += (T)h_acc[w][t];
                     pc += h_pc[w][t];
                 }
-                bwd_finish<LOG, T>(A, gbase, v, act, lsv, acc, pc, refsem);
+                bwd_finish<LOG, T>(A, g, gbase, v, act, lsv, acc, pc, refsem);
             }
             __syncthreads();
         }
@@ -549,8 +675,8 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
                 const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
                 T acc = T(0);
                 int pc = 0;
-                bwd_scan<LOG, T, LT>(A, d, gbase, lv, act, am, lsv, A.row[v], A.row[v + 1], 0, 1, acc, pc);
-                bwd_finish<LOG, T>(A, gbase, v, act, lsv, acc, pc, refsem);
+                bwd_scan<LOG, T, LT>(A, d, gbase, lv, v, act, am, lsv, A.row[v], A.row[v + 1], 0, 1, acc, pc);
+                bwd_finish<LOG, T>(A, g, gbase, v, act, lsv, acc, pc, refsem);
             }
         }
     }
@@ -582,6 +708,7 @@ __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, in
             else reinterpret_cast<uint16_t*>(A.lvl)[i] = 0;
             if (mode == 1) A.sig[i] = 1ULL;
             else if (mode == 2) reinterpret_cast<double*>(A.sig)[i] = 0.0;
+            A.srcw[l] = A.w ? A.w[s] : 1;
             if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
                 const uint32_t ent = ((uint32_t)s << 5) | (uint32_t)g;
                 if (is_hub(A, s)) A.hq[atomicAdd(&A.ctl->htail, 1ULL)] = ent;
@@ -657,12 +784,15 @@ __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, 
 
 constexpr int MAX_LEVEL = Lv<uint16_t>::MAXD;
 
-// dst[g][v] += bcg[g][v] for every lane group whose destination is set.
+// dst[g][v] += bcg[g][v] for every lane group whose destination is set.  One
+// thread per vertex walks the groups in order, so groups that share a
+// destination (one request spanning several groups) never race.
 __global__ void bc_scatter_kernel(const double* __restrict__ bcg, int ng, int n, double* const* __restrict__ dst) {
-    const size_t total = (size_t)ng * n;
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
-        double* p = dst[k / n];
-        if (p) p[k % n] += bcg[k];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        for (int g = 0; g < ng; g++) {
+            double* p = dst[g];
+            if (p) p[v] += bcg[(size_t)g * n + v];
+        }
     }
 }
 
@@ -678,6 +808,7 @@ struct LaneAccess {
         A.fq = e.fq_; A.fcap = e.fcap_; A.foff = e.foff_; A.ctl = (Ctl*)e.ctl_; A.ovf = e.ovf_;
         A.hq = e.hq_; A.hcap = e.hcap_; A.hoff = e.hoff_;
         A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.semantics = semantics;
+        A.srcw = e.srcw_;
         return A;
     }
 };
@@ -699,6 +830,8 @@ void LaneEngine::release() {
     if (ctl_host_) cudaFreeHost(ctl_host_);
     cudaFree(bcg_);
     cudaFree(ccbuf_);
+    cudaFree(srcw_);
+    srcw_ = nullptr;
     lvl_ = nullptr; sig_ = nullptr; rho_ = nullptr; vmark_ = nullptr; fq_ = nullptr; foff_ = nullptr;
     ctl_ = nullptr; ovf_ = nullptr; ctl_host_ = nullptr; bcg_ = nullptr; ccbuf_ = nullptr;
 }
@@ -760,6 +893,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     ok &= cudaMalloc(&ctl_, sizeof(Ctl)) == cudaSuccess;
     ok &= cudaMalloc(&ovf_, 32 * sizeof(uint32_t)) == cudaSuccess;
     ok &= cudaMalloc(&ccbuf_, 1024 * sizeof(unsigned long long)) == cudaSuccess;
+    ok &= cudaMalloc(&srcw_, 1024 * sizeof(int32_t)) == cudaSuccess;
     ok &= cudaMallocHost(&ctl_host_, sizeof(Ctl)) == cudaSuccess;
     if (need_bc) {
         ok &= cudaMalloc(&sig_, cells * sizeof(uint64_t)) == cudaSuccess;

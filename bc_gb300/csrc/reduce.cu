@@ -39,7 +39,15 @@ struct Reduction {
     std::vector<int64_t> r, ff;       // reach and folded distance sums
     std::vector<int32_t> parent;      // folded vertex -> vertex it was folded into
     std::vector<int32_t> fold_order;
+    std::vector<int64_t> fold_rp;     // reach of the parent just before it absorbed fold_order[i]
     std::vector<uint8_t> folded, is_ap;
+    // folded graph ("core": unfolded vertices, live edges) for betweenness
+    HostCSR core;
+    std::vector<int32_t> core_v;      // core id -> vertex
+    std::vector<int32_t> core_w;      // reach of each core vertex
+    std::unique_ptr<DevGraph> cdg;
+    int32_t* d_cw = nullptr;
+    std::unique_ptr<LaneEngine> ceng;
     int32_t n_hub = 0;
     // connected components of the folded graph (alive vertices)
     std::vector<int32_t> comp;        // per vertex slot (-1 for the phantom slot)
@@ -67,8 +75,11 @@ struct Reduction {
     std::mutex mu;
     ~Reduction() {
         eng.reset();
+        ceng.reset();
         if (dg) { cudaFree(dg->row); cudaFree(dg->col); }
+        if (cdg) { cudaFree(cdg->row); cudaFree(cdg->col); }
         cudaFree(d_w);
+        cudaFree(d_cw);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -98,6 +109,7 @@ static void fold(const int64_t* row, const int32_t* col, Reduction& R, std::vect
         R.folded[d1] = 1;
         R.parent[d1] = p;
         hub[p] = 1;
+        R.fold_rp.push_back(R.r[p]);
         R.r[p] += R.r[d1];
         R.ff[p] += R.r[d1] + R.ff[d1];
         for (int64_t e = lo[p]; e < row[p + 1]; e++)
@@ -419,6 +431,98 @@ static gbc_status assemble_cc(Reduction& R, const std::vector<int64_t>& D, int64
     return GBC_OK;
 }
 
+// Betweenness through D1 folding.  Folding a degree-1 vertex u (reach r_u)
+// into v (reach r_v before absorbing u) in a component of N vertices puts v
+// on the shortest paths of exactly the 2 r_u (N - r_u - r_v) ordered pairs
+// between u's vertices and the vertices not yet folded into v; summing over
+// folding events covers every pair with an endpoint in a pendant tree once.
+// Pairs of distinct core vertices s, t stand for r_s r_t original pairs, so
+// the core contributes reach-weighted Brandes: delta_s(v) = sum over
+// successors w of sigma_sv/sigma_sw (r_w + delta_s(w)), BC(v) += r_s delta_s(v).
+static void fold_bc(const Reduction& R, std::vector<double>& bc) {
+    bc.assign(R.n, 0.0);
+    for (size_t i = 0; i < R.fold_order.size(); i++) {
+        const int32_t d1 = R.fold_order[i];
+        const int32_t p = R.parent[d1];
+        const int64_t N = R.comp_w[R.comp[d1]];
+        const int64_t ru = R.r[d1];
+        bc[p] += 2.0 * (double)ru * (double)(N - ru - R.fold_rp[i]);
+    }
+}
+
+static gbc_status core_upload(Reduction& R) {
+    if (R.cdg) return GBC_OK;
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+    auto g = std::make_unique<DevGraph>();
+    g->n = R.core.n;
+    g->m = R.core.m();
+    bool ok = cudaMalloc(&g->row, sizeof(int64_t) * (g->n + 1)) == cudaSuccess;
+    ok &= cudaMalloc(&g->col, sizeof(int32_t) * std::max<int64_t>(g->m, 1)) == cudaSuccess;
+    ok &= cudaMalloc(&R.d_cw, sizeof(int32_t) * std::max<int32_t>(g->n, 1)) == cudaSuccess;
+    if (!ok) { cudaGetLastError(); set_error("core graph allocation"); cudaFree(g->row); cudaFree(g->col); return GBC_ERR_NOMEM; }
+    GBC_CUDA(cudaMemcpy(g->row, R.core.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
+    if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.core.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
+    if (g->n) GBC_CUDA(cudaMemcpy(R.d_cw, R.core_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
+    g->w = R.d_cw;
+    g->ff = nullptr;
+    R.cdg = std::move(g);
+    return GBC_OK;
+}
+
+// Reach-weighted Brandes over every core vertex on the device.
+static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double>& out) {
+    GBC_TRY(core_upload(R));
+    const int32_t nc = R.core.n;
+    out.assign(nc, 0.0);
+    if (nc == 0) return GBC_OK;
+    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((nc + 31) / 32) * 32);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(nc, lanes, true) > fr / 2) lanes -= 32;
+    if (!R.ceng || R.ceng->lanes() != lanes) {
+        R.ceng = std::make_unique<LaneEngine>();
+        GBC_TRY(R.ceng->init(R.cdg.get(), lanes, true, o.sparse_lanes, o.levels_per_graph, R.stream));
+    }
+    int32_t* d_src = nullptr;
+    double* d_bc = nullptr;
+    if (cudaMalloc(&d_src, sizeof(int32_t) * nc) != cudaSuccess || cudaMalloc(&d_bc, sizeof(double) * nc) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_src);
+        set_error("core buffers");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_bc, [](void* p) { cudaFree(p); });
+    std::vector<int32_t> src(nc);
+    for (int32_t i = 0; i < nc; i++) src[i] = i;
+    GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, R.stream));
+    GBC_TRY(R.ceng->bc_begin());
+    LaneResult res;
+    for (int32_t b0 = 0; b0 < nc; b0 += lanes) {
+        LaneRequest rq;
+        rq.job = LaneJob::BC;
+        rq.d_src = d_src + b0;
+        rq.kb = std::min(lanes, nc - b0);
+        rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
+        rq.semantics = GBC_BC_BRANDES;
+        rq.sigma_log = o.sigma_mode == GBC_SIGMA_LOG;
+        rq.abort_on_overflow = !rq.sigma_log;
+        gbc_status st = R.ceng->run(rq, res);
+        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO) {
+            rq.sigma_log = 1;
+            rq.abort_on_overflow = false;
+            st = R.ceng->run(rq, res);
+        }
+        if (st != GBC_OK) return st;
+    }
+    GBC_TRY(R.ceng->bc_finish(d_bc));
+    GBC_CUDA(cudaMemcpyAsync(out.data(), d_bc, sizeof(double) * nc, cudaMemcpyDeviceToHost, R.stream));
+    GBC_CUDA(cudaStreamSynchronize(R.stream));
+    return GBC_OK;
+}
+
 }  // namespace gbc
 
 using namespace gbc;
@@ -445,6 +549,27 @@ gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t
     std::vector<int32_t> lc;
     std::vector<int64_t> lo;
     fold(row, col, R, lc, lo);
+    {
+        std::vector<int32_t> cid(n, -1);
+        for (int32_t v = start; v < n; v++)
+            if (!R.folded[v]) { cid[v] = (int32_t)R.core_v.size(); R.core_v.push_back(v); }
+        const int32_t nc = (int32_t)R.core_v.size();
+        R.core.n = nc;
+        R.core.row.assign(nc + 1, 0);
+        R.core_w.resize(nc);
+        for (int32_t i = 0; i < nc; i++) {
+            const int32_t v = R.core_v[i];
+            R.core.row[i + 1] = R.core.row[i] + (row[v + 1] - lo[v]);
+            if (R.r[v] > INT32_MAX) { set_error("reach exceeds int32"); return GBC_ERR_ARG; }
+            R.core_w[i] = (int32_t)R.r[v];
+        }
+        R.core.col.resize(R.core.row[nc]);
+        for (int32_t i = 0; i < nc; i++) {
+            const int32_t v = R.core_v[i];
+            int64_t o = R.core.row[i];
+            for (int64_t e = lo[v]; e < row[v + 1]; e++) R.core.col[o++] = cid[lc[e]];
+        }
+    }
     GBC_TRY(split(row, R, lc, lo));
     // components of folded vertices follow their root
     for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
@@ -487,10 +612,48 @@ gbc_status gbc_cc_reduced(gbc_reduced h, const gbc_options* opt, int64_t* cc) {
 }
 
 gbc_status gbc_bc_reduced(gbc_reduced h, const gbc_options* opt, double* bc) {
-    (void)opt;
     if (!h || !bc) { set_error("NULL argument"); return GBC_ERR_ARG; }
-    set_error("betweenness through the reduction is not available yet");
-    return GBC_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->R.mu);
+    gbc_options o;
+    gbc_options_default(&o);
+    if (opt) o = *opt;
+    if (o.semantics != GBC_BC_BRANDES) {
+        set_error("betweenness through the reduction supports GBC_BC_BRANDES only");
+        return GBC_ERR_ARG;
+    }
+    if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("bad lanes"); return GBC_ERR_ARG; }
+    std::vector<double> cb, fb;
+    GBC_TRY(core_bc(h->R, o, cb));
+    fold_bc(h->R, fb);
+    for (int32_t v = 0; v < h->R.n; v++) bc[v] = fb[v];
+    for (size_t i = 0; i < h->R.core_v.size(); i++) bc[h->R.core_v[i]] += cb[i];
+    return GBC_OK;
+}
+
+gbc_status gbc_reduced_core_graph(gbc_reduced h, int64_t** row, int32_t** col, int32_t** weight, int32_t** vertex,
+                                  int32_t* n_core) {
+    if (!h || !row || !col || !weight || !vertex || !n_core) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    const Reduction& R = h->R;
+    GBC_TRY(export_csr(R.core, row, col));
+    const size_t nc = std::max<size_t>(R.core.n, 1);
+    *weight = (int32_t*)malloc(sizeof(int32_t) * nc);
+    *vertex = (int32_t*)malloc(sizeof(int32_t) * nc);
+    if (!*weight || !*vertex) { free(*row); free(*col); free(*weight); free(*vertex); set_error("host allocation"); return GBC_ERR_NOMEM; }
+    if (R.core.n) {
+        std::memcpy(*weight, R.core_w.data(), sizeof(int32_t) * R.core.n);
+        std::memcpy(*vertex, R.core_v.data(), sizeof(int32_t) * R.core.n);
+    }
+    *n_core = R.core.n;
+    return GBC_OK;
+}
+
+gbc_status gbc_reduced_assemble_bc(gbc_reduced h, const double* core_bc, double* bc) {
+    if (!h || (!core_bc && h->R.core.n) || !bc) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::vector<double> fb;
+    fold_bc(h->R, fb);
+    for (int32_t v = 0; v < h->R.n; v++) bc[v] = fb[v];
+    for (size_t i = 0; i < h->R.core_v.size(); i++) bc[h->R.core_v[i]] += core_bc[i];
+    return GBC_OK;
 }
 
 gbc_status gbc_reduced_block_graph(gbc_reduced h, int64_t** row, int32_t** col, int32_t** weight, int32_t* n_slots) {

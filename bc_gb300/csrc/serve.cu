@@ -209,7 +209,8 @@ void gbc_server_s::run() {
                 for (int64_t id : fifo) {
                     Req* r = reqs[id].get();
                     if (r->gid != gi || !r->admitted || r->next >= r->src.size()) continue;
-                    const int32_t rk = r->bc() ? 1 : 0;
+                    // requests share a batch only when they need the same sweep
+                    const int32_t rk = r->bc() ? 1 + r->opt.semantics * 2 + (r->opt.delta_precision == GBC_DELTA_F64) : 0;
                     if (kind < 0) kind = rk;
                     if (rk != kind) continue;
                     const int32_t room = lanes - used;
@@ -230,6 +231,7 @@ void gbc_server_s::run() {
         hsrc.assign(lanes, -1);
         hdst.assign(ng, nullptr);
         int32_t kb = 0;
+        const bool bc_batch = kind > 0;
         for (auto& sl : slots) {
             for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = sl.r->src[sl.first + i];
             for (int32_t gg = sl.lane0 / 32; gg < (sl.lane0 + sl.count + 31) / 32; gg++) hdst[gg] = sl.r->d_bc;
@@ -243,7 +245,7 @@ void gbc_server_s::run() {
             set_error("source upload failed");
         }
         LaneResult res;
-        if (st == GBC_OK && kind == 1) {
+        if (st == GBC_OK && bc_batch) {
             if (cudaMemcpyAsync(G.d_dst, hdst.data(), sizeof(double*) * ng, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
                 cudaGetLastError();
                 st = GBC_ERR_CUDA;
@@ -287,7 +289,7 @@ void gbc_server_s::run() {
                 for (int32_t i = 0; i < sl.count; i++) {
                     const int32_t v = r->src[sl.first + i];
                     edges += G.g.comp_edges.empty() ? 0 : G.g.comp_edges[G.g.comp[v]];
-                    if (kind == 0) r->cc[v] = (int64_t)hcc[sl.lane0 + i];
+                    if (!bc_batch) r->cc[v] = (int64_t)hcc[sl.lane0 + i];
                 }
                 r->done += sl.count;
                 if (r->done == r->src.size()) {
@@ -471,6 +473,20 @@ gbc_status gbc_server_fetch(gbc_server s, int64_t id, double* bc, int64_t* cc, d
     if (latency_ms) *latency_ms = r->t_done - r->t_submit;
     if (r->bc() && bc) GBC_CUDA(cudaMemcpy(bc, r->d_bc, sizeof(double) * n, cudaMemcpyDeviceToHost));
     if (!r->bc() && cc) std::memcpy(cc, r->cc.data(), sizeof(int64_t) * n);
+    return GBC_OK;
+}
+
+gbc_status gbc_server_sources(gbc_server s, int64_t id, int32_t* out, int32_t cap, int32_t* k) {
+    if (!s || !k) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return GBC_ERR_NOT_FOUND; }
+    const std::vector<int32_t>& src = it->second->src;
+    *k = (int32_t)src.size();
+    if (out) {
+        if (cap < (int32_t)src.size()) { set_error("capacity %d < %zu sources", cap, src.size()); return GBC_ERR_ARG; }
+        std::memcpy(out, src.data(), sizeof(int32_t) * src.size());
+    }
     return GBC_OK;
 }
 

@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--serve-seconds", type=float, default=8.0)
+    p.add_argument("--serve-rate", type=float, default=40.0, help="query arrivals per second")
+    p.add_argument("--no-serve", action="store_true")
     return p.parse_args()
 
 
@@ -170,6 +173,66 @@ def cpu_baseline(csr, sample, n_src, threads):
     O.bc(og, src, semantics=O.BC_REFERENCE, nthreads=threads)
     dt = time.perf_counter() - t
     return dt
+
+
+def serving(G, seconds, rate, seed=11):
+    """Poisson stream of queries over device-resident graphs (a scaled-down
+    version of the 64-graph serving mix): exact CC on the small graphs,
+    k = 64 / 1024 sampled BC everywhere.  Returns p50/p99 latency and the
+    GTEPS the server delivered over the stream."""
+    import ctypes as C
+    import random
+    L = G.lib()
+    specs = [("ba", G.gen_ba(4096, 2, 1)), ("ba", G.gen_ba(65536, 8, 2)), ("er", G.gen_er(32768, 4.0, 3)),
+             ("er", G.gen_er(131072, 32.0, 4)), ("grid", G.gen_grid(128, 128, 0.0, 5)),
+             ("rmat", G.gen_rmat(10, 16, seed=6)), ("rmat", G.gen_rmat(16, 16, seed=7)),
+             ("rmat", G.gen_rmat(18, 16, seed=8))]
+    cfg = G.ServerConfig()
+    cfg.max_lanes = 1024
+    h = C.c_void_p()
+    G.check(L.gbc_server_create(C.byref(cfg), C.byref(h)))
+    gids = []
+    for _, csr in specs:
+        gid = C.c_int32()
+        G.check(L.gbc_server_add_graph(h, csr.row, csr.col, csr.n, C.byref(gid)))
+        gids.append(gid.value)
+    rng = random.Random(seed)
+    o = G.options()
+    reqs = []
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        gi = rng.randrange(len(specs))
+        n = specs[gi][1].n
+        r = rng.random()
+        if r < 0.25 and n <= 32768:
+            kind, k = G.Q_CC, 0
+        elif r < 0.7:
+            kind, k = G.Q_BC_SAMPLED, 64
+        else:
+            kind, k = G.Q_BC_SAMPLED, 1024
+        rid = C.c_int64()
+        G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
+        reqs.append((rid.value, gi))
+        time.sleep(rng.expovariate(rate))
+    lats = []
+    for rid, gi in reqs:
+        st = C.c_int32()
+        G.check(L.gbc_server_wait(h, rid, 600000.0, C.byref(st)))
+        n = specs[gi][1].n
+        bc = np.zeros(n)
+        cc = np.zeros(n, np.int64)
+        lat = C.c_double()
+        G.check(L.gbc_server_fetch(h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                                   C.byref(lat)))
+        lats.append(lat.value)
+    v = [C.c_int64() for _ in range(4)] + [C.c_double()]
+    G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
+    L.gbc_server_destroy(h)
+    lats = np.array(lats)
+    return {"queries": len(lats), "p50_ms": round(float(np.percentile(lats, 50)), 3),
+            "p99_ms": round(float(np.percentile(lats, 99)), 3), "rate_per_s": rate, "graphs": len(specs),
+            "lane_batches": v[1].value, "shared_batches": v[2].value,
+            "gteps_busy": round(v[3].value / (v[4].value * 1e-3) / 1e9, 3) if v[4].value > 0 else None}
 
 
 def run_reference(args):
@@ -348,6 +411,9 @@ def main():
             cpu = {"value": round(float(ce[sample[:n_cpu]].sum()) / dt / 1e9, 6), "unit": "GTEPS", "cores": threads,
                    "kind": "port",
                    "sample": f"first {n_cpu} of the {args.k} sampled sources, reference semantics, FP64"}
+        serve = None
+        if not args.no_serve:
+            serve = serving(G, args.serve_seconds, args.serve_rate)
         out = {"metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",
@@ -360,7 +426,7 @@ def main():
                "plain": None if plain_gteps is None else {
                    "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),
                    "speedup_batched_vs_plain": round(gteps / plain_gteps, 2)},
-               "clocks": clocks}
+               "serving": serve, "clocks": clocks}
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.barrier()

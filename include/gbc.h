@@ -161,8 +161,10 @@ gbc_status gbc_reduced_info_get(gbc_reduced r, gbc_reduced_info* info);
 /* Closeness of every vertex slot through the reduction: cc[n] (host).
  * Equal to gbc_cc over all vertices of the unreduced graph. */
 gbc_status gbc_cc_reduced(gbc_reduced r, const gbc_options* opt, int64_t* cc);
-/* Betweenness of every vertex slot through D1 folding (GBC_BC_BRANDES only):
- * sources are the unfolded vertices weighted by their reach. */
+/* Betweenness (GBC_BC_BRANDES) of every vertex slot through D1 folding:
+ * reach-weighted Brandes over the unfolded vertices on the device plus the
+ * exact pair counts of the folded pendant trees.  Equal to gbc_bc over all
+ * vertices of the unreduced graph. */
 gbc_status gbc_bc_reduced(gbc_reduced r, const gbc_options* opt, double* bc);
 gbc_status gbc_reduced_destroy(gbc_reduced r);
 /* The block graph the reduction hands to the device: slot CSR (malloc'd,
@@ -171,6 +173,14 @@ gbc_status gbc_reduced_block_graph(gbc_reduced r, int64_t** row, int32_t** col, 
 /* Host assembly step: given D[s] = sum_u d(s,u) * w'(u) for every slot s of
  * the block graph, write the closeness of every vertex slot to cc[n]. */
 gbc_status gbc_reduced_assemble_cc(gbc_reduced r, const int64_t* D, int64_t* cc);
+/* The folded ("core") graph betweenness runs on: CSR over the unfolded
+ * vertices (malloc'd, free with gbc_free), their reach weights and the
+ * vertex slot of each core id. */
+gbc_status gbc_reduced_core_graph(gbc_reduced r, int64_t** row, int32_t** col, int32_t** weight, int32_t** vertex,
+                                  int32_t* n_core);
+/* Host assembly step for betweenness: core_bc[i] = reach-weighted Brandes
+ * betweenness of core id i; adds the folding contributions, writes bc[n]. */
+gbc_status gbc_reduced_assemble_bc(gbc_reduced r, const double* core_bc, double* bc);
 
 /* ---- synthetic graphs (host CSR, malloc'd; free with gbc_free) --------
  * All generators are deterministic for a seed on any host. */
@@ -223,6 +233,10 @@ gbc_status gbc_server_wait(gbc_server s, int64_t req_id, double timeout_ms, int3
  * from submit to completion goes to *latency_ms. Frees the request. */
 gbc_status gbc_server_fetch(gbc_server s, int64_t req_id, double* bc, int64_t* cc, double* latency_ms);
 gbc_status gbc_server_cancel(gbc_server s, int64_t req_id);
+/* The source vertices of a request (the drawn sample for GBC_Q_BC_SAMPLED):
+ * *k = count; out (may be NULL) receives them if cap >= count.  Valid until
+ * the request is fetched. */
+gbc_status gbc_server_sources(gbc_server s, int64_t req_id, int32_t* out, int32_t cap, int32_t* k);
 /* Aggregate counters: completed requests, lane batches, shared batches
  * (batches that carried sources of more than one request), edges traversed. */
 gbc_status gbc_server_counters(gbc_server s, int64_t* completed, int64_t* batches, int64_t* shared_batches,

@@ -1,0 +1,131 @@
+"""GPU: the D1 + block reduction end to end, the struct-CSR drop-in entry
+points, and the device-pointer entry points, against the oracle and the
+reference's own outputs (golden fixtures)."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from compat_structs import bind, load
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+STRUCT = json.load(open(os.path.join(GOLDEN, "structure.json")))
+
+
+def fixture(name):
+    return np.load(os.path.join(GOLDEN, name.split(".")[0] + ".npz"))
+
+
+@pytest.mark.parametrize("name", sorted(STRUCT))
+def test_reduced_cc_matches_reference(gpu, datasets, name):
+    csr = gpu.read_edgelist(datasets[name])
+    R = gpu.Reduced(csr)
+    got = R.cc()
+    assert np.array_equal(got[csr.start:], fixture(name)["cc_ref"][csr.start:])
+    info = R.info()
+    st = STRUCT[name]
+    assert (info["d1_folded"], info["articulation_points"]) == (st["d1"], st["ap"])
+
+
+@pytest.mark.parametrize("case", ["rmat14+pendants", "sparse-er+pendants", "grid-holes"])
+def test_reduced_cc_disconnected(gpu, orc, case):
+    if case == "rmat14+pendants":
+        csr = gpu.add_pendants(gpu.gen_rmat(14, 4, seed=5), 3000, 3, 9)
+    elif case == "sparse-er+pendants":
+        csr = gpu.add_pendants(gpu.gen_er(4000, 1.5, seed=5), 600, 3, 9)
+    else:
+        csr = gpu.gen_grid(40, 40, 0.3, seed=2, largest_only=False)
+    og = orc.Graph(csr.row, csr.col)
+    ref = orc.cc(og, np.arange(csr.n), nthreads=8)
+    assert np.array_equal(gpu.Reduced(csr).cc(), ref)
+
+
+def test_dropin_entry_points(gpu, datasets):
+    L = bind(gpu.lib())
+    for name in ["karate.txt", "dolphins.txt", "ia-fb-messages.mtx", "testdata2.txt"]:
+        fx = fixture(name)
+        g, c = load(L, datasets[name])
+        vs = c.contents.csrVSize
+        bcs = (C.c_float * vs)()
+        L.computeBC(c, bcs)
+        bc = np.frombuffer(bcs, np.float32).astype(np.float64)
+        ref = fx["bc_ref_f32"].astype(np.float64)
+        assert np.max(np.abs(bc[:-1] - ref) / np.maximum(np.abs(ref), 1.0)) < 5e-5, name
+        ccs = (C.c_int * vs)()
+        L.computeCC(c, ccs)
+        cc = np.frombuffer(ccs, np.int32)[:-1]
+        assert np.array_equal(cc[c.contents.startNodeID:], fx["cc_ref"][c.contents.startNodeID:].astype(np.int32))
+        L.gpu_vb(c)
+        assert np.array_equal(np.ctypeslib.as_array(c.contents.CCs, shape=(vs - 1,)), cc)
+        L.gpu_fan(g, c)
+        assert np.array_equal(np.ctypeslib.as_array(c.contents.CCs, shape=(vs - 1,)), cc)
+        g2, c2 = load(L, datasets[name])
+        out = (C.c_int * (2 * vs))()
+        L.compute_D1_AP_CC_shareBased_DegreeOrder(c2, out)
+        d1ap = np.frombuffer(out, np.int32)[:vs - 1]
+        s = c2.contents.startNodeID
+        assert np.array_equal(d1ap[s:], fx["d1ap_cc_ref"][s:].astype(np.int32)), name
+        st = STRUCT[name]
+        assert (c2.contents.foldedDegreeOneCount, c2.contents.ap_count) == (st["d1"], st["ap"])
+
+
+def test_karate_golden_through_dropin(gpu, datasets):
+    L = bind(gpu.lib())
+    g, c = load(L, datasets["karate.txt"])
+    vs = c.contents.csrVSize
+    bcs = (C.c_float * vs)()
+    L.computeBC(c, bcs)
+    gold = np.loadtxt(os.path.join(GOLDEN, "karate_BC_Score.txt"), skiprows=1)
+    got = np.frombuffer(bcs, np.float32)[1:vs - 1].astype(np.float64)
+    assert np.max(np.abs(got - gold) / np.maximum(gold, 1.0)) < 2e-6
+
+
+def test_device_pointer_entry_points(gpu, orc):
+    torch = pytest.importorskip("torch")
+    csr = gpu.gen_ba(3000, 3, 4)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.arange(0, 3000, 3, dtype=np.int32)
+    L = gpu.lib()
+    d_row = torch.from_numpy(csr.row).cuda()
+    d_col = torch.from_numpy(csr.col).cuda()
+    h = C.c_void_p()
+    gpu.check(L.gbc_graph_create_device(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), csr.n,
+                                        csr.m, C.byref(h)))
+    d_src = torch.from_numpy(src).cuda()
+    d_bc = torch.empty(csr.n, dtype=torch.float64, device="cuda")
+    d_cc = torch.empty(len(src), dtype=torch.int64, device="cuda")
+    st = torch.cuda.current_stream()
+    o = gpu.options()
+    gpu.check(L.gbc_bc_device(h, C.c_void_p(d_src.data_ptr()), len(src), C.byref(o), C.c_void_p(d_bc.data_ptr()),
+                              C.c_void_p(st.cuda_stream)))
+    gpu.check(L.gbc_cc_device(h, C.c_void_p(d_src.data_ptr()), len(src), C.byref(o), C.c_void_p(d_cc.data_ptr()),
+                              C.c_void_p(st.cuda_stream)))
+    torch.cuda.synchronize()
+    ref, _ = orc.bc(og, src)
+    assert np.max(np.abs(d_bc.cpu().numpy() - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+    assert np.array_equal(d_cc.cpu().numpy(), orc.cc(og, src))
+    L.gbc_graph_destroy(h)
+
+
+@pytest.mark.parametrize("case", ["karate", "ca-HepPh", "rmat13+pendants", "forest+er"])
+def test_reduced_bc_matches_plain_brandes(gpu, orc, datasets, case):
+    """Betweenness through D1 folding (reach-weighted Brandes on the device
+    plus the folded pair counts) equals plain Brandes of the whole graph."""
+    if case == "karate":
+        csr = gpu.read_edgelist(datasets["karate.txt"])
+    elif case == "ca-HepPh":
+        csr = gpu.read_edgelist(datasets["ca-HepPh.mtx"])
+    elif case == "rmat13+pendants":
+        csr = gpu.add_pendants(gpu.gen_rmat(13, 4, seed=5), 2500, 3, 9)
+    else:
+        csr = gpu.add_pendants(gpu.gen_er(3000, 1.2, seed=7), 800, 3, 11)
+    og = orc.Graph(csr.row, csr.col, csr.start)
+    ref, _ = orc.bc(og, np.arange(csr.start, csr.n), semantics=orc.BC_BRANDES, nthreads=8)
+    R = gpu.Reduced(csr)
+    got = R.bc()
+    assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+    with pytest.raises(gpu.GbcError):
+        R.bc(semantics=gpu.BC_REFERENCE)

@@ -1,0 +1,178 @@
+"""GPU serving: continuous batching over device-resident graphs.  Requests
+that arrive while others run share lane batches; every result equals the
+same request run alone (closeness exactly, betweenness within 1e-9
+relative), and deadlines, cancellation and admission behave."""
+import ctypes as C
+import random
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+
+
+class Server:
+    def __init__(self, gbc, budget=0, max_lanes=0, max_inflight=0):
+        self.g = gbc
+        self.L = gbc.lib()
+        cfg = gbc.ServerConfig()
+        cfg.hbm_budget_bytes = budget
+        cfg.max_lanes = max_lanes
+        cfg.max_inflight = max_inflight
+        self.h = C.c_void_p()
+        gbc.check(self.L.gbc_server_create(C.byref(cfg), C.byref(self.h)))
+        self.n = {}
+
+    def add(self, csr):
+        gid = C.c_int32()
+        self.g.check(self.L.gbc_server_add_graph(self.h, csr.row, csr.col, csr.n, C.byref(gid)))
+        self.n[gid.value] = csr.n
+        return gid.value
+
+    def submit(self, gid, kind, k=0, seed=0, deadline_ms=0.0, **opt):
+        rid = C.c_int64()
+        self.g.check(self.L.gbc_server_submit(self.h, gid, kind, k, seed, C.byref(self.g.options(**opt)),
+                                              deadline_ms, C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid, timeout_ms=120000.0):
+        st = C.c_int32()
+        self.g.check(self.L.gbc_server_wait(self.h, rid, timeout_ms, C.byref(st)))
+        return st.value
+
+    def fetch(self, rid, gid):
+        n = self.n[gid]
+        bc = np.zeros(n, np.float64)
+        cc = np.zeros(n, np.int64)
+        lat = C.c_double()
+        st = self.L.gbc_server_fetch(self.h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                                     C.byref(lat))
+        return st, bc, cc, lat.value
+
+    def sources(self, rid):
+        k = C.c_int32()
+        self.g.check(self.L.gbc_server_sources(self.h, rid, None, 0, C.byref(k)))
+        out = np.zeros(k.value, np.int32)
+        self.g.check(self.L.gbc_server_sources(self.h, rid, out.ctypes.data_as(C.c_void_p), k.value, C.byref(k)))
+        return out
+
+    def counters(self):
+        v = [C.c_int64() for _ in range(4)] + [C.c_double()]
+        self.g.check(self.L.gbc_server_counters(self.h, *[C.byref(x) for x in v]))
+        return dict(completed=v[0].value, batches=v[1].value, shared=v[2].value, edges=v[3].value,
+                    busy_ms=v[4].value)
+
+    def close(self):
+        self.L.gbc_server_destroy(self.h)
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1.0)))
+
+
+@pytest.fixture(scope="module")
+def graphs(gpu):
+    return [gpu.gen_ba(2000, 3, 1), gpu.gen_grid(30, 30, 0.05, seed=3), gpu.gen_rmat(11, 8, seed=2),
+            gpu.gen_er(1500, 6.0, seed=4)]
+
+
+def run_alone(gpu, csr, kind, k, seed, sem):
+    S = Server(gpu)
+    gid = S.add(csr)
+    rid = S.submit(gid, kind, k, seed, semantics=sem)
+    assert S.wait(rid) == gpu.REQ_DONE
+    st, bc, cc, _ = S.fetch(rid, gid)
+    assert st == 0
+    S.close()
+    return bc, cc
+
+
+def test_mixed_stream_equals_alone(gpu, orc, graphs):
+    S = Server(gpu, max_lanes=256)
+    gids = [S.add(g) for g in graphs]
+    rng = random.Random(5)
+    plan = []
+    for i in range(24):
+        gi = rng.randrange(len(graphs))
+        kind = rng.choice([gpu.Q_CC, gpu.Q_BC_SAMPLED, gpu.Q_BC_SAMPLED, gpu.Q_BC])
+        k = rng.choice([64, 300]) if kind == gpu.Q_BC_SAMPLED else 0
+        if kind == gpu.Q_BC and graphs[gi].n > 1200:
+            kind, k = gpu.Q_BC_SAMPLED, 1024
+        plan.append((gi, kind, k, 100 + i, rng.choice([0, 1])))
+    rids = [None] * len(plan)
+
+    def client(lo, hi):
+        for j in range(lo, hi):
+            gi, kind, k, seed, sem = plan[j]
+            rids[j] = S.submit(gids[gi], kind, k, seed, semantics=sem)
+            time.sleep(rng.random() * 0.01)
+
+    th = [threading.Thread(target=client, args=(a, a + 6)) for a in range(0, 24, 6)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    results = []
+    for j, rid in enumerate(rids):
+        assert S.wait(rid) == gpu.REQ_DONE
+        results.append(S.fetch(rid, gids[plan[j][0]]))
+    c = S.counters()
+    S.close()
+    assert c["completed"] == len(plan)
+    assert c["shared"] > 0, "no lane batch carried more than one request"
+    lats = [r[3] for r in results]
+    assert all(l > 0 for l in lats)
+    for j, (gi, kind, k, seed, sem) in enumerate(plan):
+        st, bc, cc, _ = results[j]
+        assert st == 0
+        abc, acc = run_alone(gpu, graphs[gi], kind, k, seed, sem)
+        if kind == gpu.Q_CC:
+            assert np.array_equal(cc, acc)
+            og = orc.Graph(graphs[gi].row, graphs[gi].col)
+            assert np.array_equal(cc, orc.cc(og, np.arange(graphs[gi].n)))
+        else:
+            assert relerr(bc, abc) < TOL, (j, plan[j])
+    # exact-BC requests checked against the oracle over all sources
+    for j, (gi, kind, k, seed, sem) in enumerate(plan):
+        if kind != gpu.Q_BC:
+            continue
+        og = orc.Graph(graphs[gi].row, graphs[gi].col)
+        ref, _ = orc.bc(og, np.arange(graphs[gi].n), semantics=sem, nthreads=8)
+        assert relerr(results[j][1], ref) < TOL
+
+
+def test_deadline_cancel_and_unknown(gpu, graphs):
+    S = Server(gpu, max_lanes=32)
+    gid = S.add(graphs[0])
+    slow = S.submit(gid, gpu.Q_BC, deadline_ms=1.0)      # 2000 sources in 32-lane batches: cannot finish in 1 ms
+    assert S.wait(slow) == gpu.REQ_FAILED
+    st, _, _, _ = S.fetch(slow, gid)
+    assert st == 8   # GBC_ERR_TIMEOUT
+    r2 = S.submit(gid, gpu.Q_BC)
+    S.g.check(S.L.gbc_server_cancel(S.h, r2))
+    assert S.wait(r2) == gpu.REQ_CANCELLED
+    st = C.c_int32()
+    assert S.L.gbc_server_poll(S.h, 987654, C.byref(st)) == 6   # GBC_ERR_NOT_FOUND
+    rid = C.c_int64()
+    assert S.L.gbc_server_submit(S.h, 99, gpu.Q_CC, 0, 0, None, 0.0, C.byref(rid)) == 6
+    ok = S.submit(gid, gpu.Q_BC_SAMPLED, 40, 7)
+    assert S.wait(ok) == gpu.REQ_DONE
+    S.close()
+
+
+def test_admission_under_small_budget(gpu, orc, graphs):
+    # a budget that holds only a narrow engine for one graph at a time
+    S = Server(gpu, budget=64 << 20, max_lanes=1024)
+    gids = [S.add(g) for g in graphs[:3]]
+    rids = [(g, S.submit(g, gpu.Q_CC)) for g in gids]
+    for g, r in rids:
+        assert S.wait(r) == gpu.REQ_DONE
+        st, _, cc, _ = S.fetch(r, g)
+        assert st == 0
+        csr = graphs[gids.index(g)]
+        og = orc.Graph(csr.row, csr.col)
+        assert np.array_equal(cc, orc.cc(og, np.arange(csr.n)))
+    S.close()
