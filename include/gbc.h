@@ -138,6 +138,25 @@ gbc_status gbc_cc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const
 gbc_status gbc_sssp(gbc_graph g, const int32_t* sources, int32_t k, const gbc_options* opt,
                     int32_t* dist, uint64_t* sigma, uint8_t* ovf);
 
+/* ---- closeness without allocation ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory at call time -- a process that reserved all of HBM for its own pool
+ * up front (any cudaMalloc would fail or fragment it), or a latency-critical
+ * path that must not risk the device synchronisation cudaMalloc/cudaFree can
+ * bring.  Device CSR (row[n+1] int64, col int32), device sources[k]; writes
+ * cc[i] (device int64) = sum of hop distances from sources[i], like gbc_cc.
+ * The BFS state lives in one fixed file-scope device array (16 MB on every
+ * GPU that loads the library, kept until exit), so n is limited to
+ * GBC_NOALLOC_MAX_VERTICES; larger graphs get GBC_ERR_ARG.  Nothing is
+ * allocated on the host or the device.  Every call shares that array and
+ * re-initialises it; calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  Runs on
+ * `stream` (a cudaStream_t) and returns when the results are written. */
+#define GBC_NOALLOC_MAX_VERTICES (1 << 21)
+gbc_status gbc_cc_noalloc(const int64_t* d_row, const int32_t* d_col, int32_t n, const int32_t* d_sources,
+                          int32_t k, int64_t* d_cc, void* stream);
+
 /* ---- D1 folding + articulation-point (block) reduction ---------------- */
 typedef struct gbc_reduced_s* gbc_reduced;
 typedef struct {
