@@ -183,19 +183,24 @@ template <> struct Simd<uint16_t> {
 };
 
 // Lane-parallel forward scan of v's neighbour chunks (r0 + 32*sub, step
-// 32*nsub).  Result for lane t is returned in thread t.
+// 32*nsub).  Result for lane t is returned in thread t.  Path counts of the
+// LPW lanes a thread owns are read as 16-byte pairs; per-slot partial sums
+// meet in shared memory and are added in slot order.
 template <int MODE, typename LT>
 __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t gbase, LT* lv, int v, long long r0,
                                           long long r1, int sub, int nsub, uint64_t& acc, bool& of, double& lm,
                                           double& ls) {
     using S = Simd<LT>;
     constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
-    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV;
+    constexpr unsigned PAIR = (LPW == 4) ? 0xFFFFu : 0xFFFFFFFFu;   // level bits of one pair of lanes
+    __shared__ uint64_t part_a[WARPS][SLOTS][32];
+    __shared__ double part_s[MODE == 2 ? WARPS : 1][SLOTS][32];
+    __shared__ unsigned char part_o[WARPS][SLOTS][32];
+    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV, wib = threadIdx.x >> 5;
     const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
     const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1);
     const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
     const uint64_t* sg = A.sig + (gbase << 5) + w * LPW;
-    const double* sgd = reinterpret_cast<const double*>(sg);
     uint64_t a[LPW];
     double m[LPW], sl[LPW];
     unsigned ofm = 0;
@@ -203,11 +208,13 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
     for (int j = 0; j < LPW; j++) { a[j] = 0; m[j] = -INFINITY; sl[j] = 0.0; }
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
         const int cnt = (int)min(32LL, r1 - jb);
+        const int kmax = (cnt + SLOTS - 1) / SLOTS;   // uniform across the warp
         const int xm = (t < cnt) ? A.col[jb + t] : 0;
         unsigned Lw[ITER];
         int xs[ITER];
 #pragma unroll
         for (int k = 0; k < ITER; k++) {
+            if (k >= kmax) break;
             const int q = k * SLOTS + s;
             xs[k] = __shfl_sync(FULL, xm, q);
             Lw[k] = (q < cnt) ? lvw[(size_t)xs[k] * WPV + w] : d4;
@@ -215,26 +222,37 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
         if (MODE != 0 && d > 0) {
 #pragma unroll
             for (int k = 0; k < ITER; k++) {
+                if (k >= kmax) break;
                 const unsigned pm = S::eq(Lw[k], dp4) & act4;
-                if (pm) {
-                    const size_t xo = (size_t)xs[k] << 5;
+                if (!pm) continue;
+                const size_t xo = (size_t)xs[k] << 5;
 #pragma unroll
-                    for (int j = 0; j < LPW; j++) {
-                        if (!S::has(pm, j)) continue;
-                        if (MODE == 1) {
-                            const uint64_t sv = sg[xo + j];
-                            const uint64_t na = a[j] + sv;
-                            ofm |= (unsigned)(na < a[j]) << j;
-                            a[j] = na;
-                        } else {
-                            lse_add(m[j], sl[j], sgd[xo + j]);
+                for (int pr = 0; pr < LPW / 2; pr++) {
+                    const unsigned pmp = (pm >> (pr * 2 * (32 / LPW))) & PAIR;
+                    if (!pmp) continue;
+                    if (MODE == 1) {
+                        const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(sg + xo + 2 * pr);
+                        const uint64_t v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            if (!S::has(pm, 2 * pr + h)) continue;
+                            const uint64_t na = a[2 * pr + h] + v2[h];
+                            ofm |= (unsigned)(na < a[2 * pr + h]) << (2 * pr + h);
+                            a[2 * pr + h] = na;
                         }
+                    } else {
+                        const double2 vv = *reinterpret_cast<const double2*>(sg + xo + 2 * pr);
+                        const double v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++)
+                            if (S::has(pm, 2 * pr + h)) lse_add(m[2 * pr + h], sl[2 * pr + h], v2[h]);
                     }
                 }
             }
         }
 #pragma unroll
         for (int k = 0; k < ITER; k++) {
+            if (k >= kmax) break;
             const int q = k * SLOTS + s;
             const unsigned un = S::eq(Lw[k], 0xFFFFFFFFu) & act4;   // unreached, in active lanes
             const unsigned gm = S::gt(Lw[k], d4) & act4;            // unreached or already at d+1
@@ -250,46 +268,35 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
             warp_append(A, has, has && is_hub(A, xs[k]), ((uint32_t)xs[k] << 5) | (uint32_t)g);
         }
     }
-    // sum the slots (every slot then holds the totals), hand lane t to thread t
+    if (MODE == 0) return;
+    // slot partials -> shared memory (indexed by lane), then thread t adds its lane's slots in order
 #pragma unroll
-    for (int o = WPV; o < 32; o <<= 1) {
-        if (MODE == 1) {
-            unsigned of2 = __shfl_xor_sync(FULL, ofm, o);
-#pragma unroll
-            for (int j = 0; j < LPW; j++) {
-                const uint64_t p = __shfl_xor_sync(FULL, a[j], o);
-                const uint64_t na = a[j] + p;
-                ofm |= (unsigned)(na < a[j]) << j;
-                a[j] = na;
-            }
-            ofm |= of2;
-        } else if (MODE == 2) {
-#pragma unroll
-            for (int j = 0; j < LPW; j++) {
-                const double m2 = __shfl_xor_sync(FULL, m[j], o);
-                const double s2 = __shfl_xor_sync(FULL, sl[j], o);
-                lse_merge(m[j], sl[j], m2, s2);
-            }
-        }
+    for (int j = 0; j < LPW; j++) {
+        const int lane = w * LPW + j;
+        if (MODE == 1) { part_a[wib][s][lane] = a[j]; part_o[wib][s][lane] = (ofm >> j) & 1u; }
+        else { part_a[wib][s][lane] = __double_as_longlong(m[j]); part_s[wib][s][lane] = sl[j]; }
     }
-    const int src = t / LPW, jj = t % LPW;
+    __syncwarp();
     if (MODE == 1) {
-        uint64_t r = 0;
+        uint64_t r = part_a[wib][0][t];
+        bool o = part_o[wib][0][t];
 #pragma unroll
-        for (int j = 0; j < LPW; j++) {
-            const uint64_t vj = __shfl_sync(FULL, a[j], src);
-            if (j == jj) r = vj;
+        for (int k = 1; k < SLOTS; k++) {
+            const uint64_t p = part_a[wib][k][t];
+            const uint64_t na = r + p;
+            o = o || part_o[wib][k][t] || (na < r);
+            r = na;
         }
         acc = r;
-        of = (__shfl_sync(FULL, ofm, src) >> jj) & 1u;
-    } else if (MODE == 2) {
+        of = o;
+    } else {
+        double mm = __longlong_as_double(part_a[wib][0][t]), ss = part_s[wib][0][t];
 #pragma unroll
-        for (int j = 0; j < LPW; j++) {
-            const double mj = __shfl_sync(FULL, m[j], src);
-            const double sj = __shfl_sync(FULL, sl[j], src);
-            if (j == jj) { lm = mj; ls = sj; }
-        }
+        for (int k = 1; k < SLOTS; k++) lse_merge(mm, ss, __longlong_as_double(part_a[wib][k][t]), part_s[wib][k][t]);
+        lm = mm;
+        ls = ss;
     }
+    __syncwarp();
 }
 
 // Lane-parallel dependency scan: sum of rho over successors, predecessor
@@ -299,7 +306,10 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
                                           long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
     using S = Simd<LT>;
     constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
-    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV;
+    constexpr unsigned PAIR = (LPW == 4) ? 0xFFFFu : 0xFFFFFFFFu;
+    __shared__ double part_a[WARPS][SLOTS][32];
+    __shared__ int part_p[WARPS][SLOTS][32];
+    const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV, wib = threadIdx.x >> 5;
     const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
     const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1), dn4 = S::bc(d + 1);
     const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
@@ -316,49 +326,73 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
     }
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
         const int cnt = (int)min(32LL, r1 - jb);
+        const int kmax = (cnt + SLOTS - 1) / SLOTS;
         const int xm = (t < cnt) ? A.col[jb + t] : 0;
         unsigned Lw[ITER];
         int xs[ITER];
 #pragma unroll
         for (int k = 0; k < ITER; k++) {
+            if (k >= kmax) break;
             const int q = k * SLOTS + s;
             xs[k] = __shfl_sync(FULL, xm, q);
             Lw[k] = (q < cnt) ? lvw[(size_t)xs[k] * WPV + w] : d4;
         }
 #pragma unroll
         for (int k = 0; k < ITER; k++) {
+            if (k >= kmax) break;
             const unsigned sm = S::eq(Lw[k], dn4) & act4;
             const unsigned pm = S::eq(Lw[k], dp4) & act4;
-            const size_t xo = (size_t)xs[k] << 5;
 #pragma unroll
-            for (int j = 0; j < LPW; j++) {
-                if (S::has(sm, j)) {
-                    if (LOG) a[j] += (T)exp2(lsj[j] + rhd[xo + j]);
-                    else a[j] += rh[xo + j];
+            for (int j = 0; j < LPW; j++) pcs[j] += S::has(pm, j);
+            if (!sm) continue;
+            const size_t xo = (size_t)xs[k] << 5;
+            if (!LOG && sizeof(T) == 4 && LPW == 4) {
+                const float4 vv = *reinterpret_cast<const float4*>(rh + xo);
+                const float v4[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+                for (int j = 0; j < LPW; j++)
+                    if (S::has(sm, j)) a[j] += (T)v4[j];
+            } else {
+#pragma unroll
+                for (int pr = 0; pr < LPW / 2; pr++) {
+                    const unsigned smp = (sm >> (pr * 2 * (32 / LPW))) & PAIR;
+                    if (!smp) continue;
+                    if (LOG || sizeof(T) == 8) {
+                        const double2 vv = *reinterpret_cast<const double2*>((LOG ? rhd : reinterpret_cast<const double*>(rh)) + xo + 2 * pr);
+                        const double v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            if (!S::has(sm, 2 * pr + h)) continue;
+                            if (LOG) a[2 * pr + h] += (T)exp2(lsj[2 * pr + h] + v2[h]);
+                            else a[2 * pr + h] += (T)v2[h];
+                        }
+                    } else {
+                        const float2 vv = *reinterpret_cast<const float2*>(rh + xo + 2 * pr);
+                        const float v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++)
+                            if (S::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
+                    }
                 }
-                pcs[j] += S::has(pm, j);
             }
         }
     }
 #pragma unroll
-    for (int o = WPV; o < 32; o <<= 1) {
-#pragma unroll
-        for (int j = 0; j < LPW; j++) {
-            a[j] += __shfl_xor_sync(FULL, a[j], o);
-            pcs[j] += __shfl_xor_sync(FULL, pcs[j], o);
-        }
-    }
-    const int src = t / LPW, jj = t % LPW;
-    T r = T(0);
-    int p = 0;
-#pragma unroll
     for (int j = 0; j < LPW; j++) {
-        const T vj = __shfl_sync(FULL, a[j], src);
-        const int pj = __shfl_sync(FULL, pcs[j], src);
-        if (j == jj) { r = vj; p = pj; }
+        part_a[wib][s][w * LPW + j] = (double)a[j];
+        part_p[wib][s][w * LPW + j] = pcs[j];
+    }
+    __syncwarp();
+    T r = (T)part_a[wib][0][t];
+    int p = part_p[wib][0][t];
+#pragma unroll
+    for (int k = 1; k < SLOTS; k++) {
+        r += (T)part_a[wib][k][t];
+        p += part_p[wib][k][t];
     }
     acc = r;
     pc = p;
+    __syncwarp();
 }
 
 // ---- forward --------------------------------------------------------------
