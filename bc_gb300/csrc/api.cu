@@ -25,6 +25,11 @@ struct gbc_graph_s {
     double* d_bc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<int32_t> last_src;
+    // lane assignment: per-vertex level-profile key and degree (computed once)
+    std::vector<uint32_t> key;
+    std::vector<int32_t> deg;
+    int32_t* d_pos = nullptr;
+    int64_t pos_cap = 0;
     ~gbc_graph_s() {
         eng.reset();
         cudaFree(g.row);
@@ -32,6 +37,7 @@ struct gbc_graph_s {
         cudaFree(d_src);
         cudaFree(d_ccb);
         cudaFree(d_bc);
+        cudaFree(d_pos);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -113,14 +119,17 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     return GBC_OK;
 }
 
-// Autotune lanes: as wide as the sources and the memory budget allow.
-static int32_t pick_lanes(const DevGraph& g, int64_t k, bool bc, int32_t requested) {
+// Autotune lanes: as wide as the sources and the memory budget allow; an
+// existing engine that is wide enough is kept.
+static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested) {
     if (requested) return requested;
+    const DevGraph& g = G->g;
     int32_t lanes = (int32_t)std::min<int64_t>(1024, ((k + 31) / 32) * 32);
     lanes = std::max(lanes, 32);
+    if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes) return G->eng->lanes();
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
-    const size_t budget = fr / 2;
+    const size_t budget = (fr + (G->eng ? G->eng->device_bytes() : 0)) / 2;
     while (lanes > 32 && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= 32;
     return lanes;
 }
@@ -135,7 +144,86 @@ static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_o
     return GBC_OK;
 }
 
-static gbc_status stage_sources(gbc_graph_s* G, const int32_t* sources, int32_t k, std::vector<int32_t>& hsrc) {
+// Level-profile key of every vertex: one forward batch from the 32 highest-
+// degree vertices; key = (level from the top vertex, nearest of the others).
+static gbc_status ensure_order_key(gbc_graph_s* G, LaneEngine* E) {
+    if (!G->key.empty()) return GBC_OK;
+    const DevGraph& g = G->g;
+    std::vector<int64_t> row(g.n + 1);
+    GBC_CUDA(cudaMemcpy(row.data(), g.row, sizeof(int64_t) * (g.n + 1), cudaMemcpyDeviceToHost));
+    G->deg.resize(g.n);
+    for (int32_t v = 0; v < g.n; v++) G->deg[v] = (int32_t)(row[v + 1] - row[v]);
+    std::vector<int32_t> idx(g.n);
+    for (int32_t v = 0; v < g.n; v++) idx[v] = v;
+    const int32_t kb = std::min<int32_t>(32, g.n);
+    std::partial_sort(idx.begin(), idx.begin() + kb, idx.end(),
+                      [&](int32_t a, int32_t b) { return G->deg[a] != G->deg[b] ? G->deg[a] > G->deg[b] : a < b; });
+    int32_t* d_hub = nullptr;
+    uint32_t* d_key = nullptr;
+    if (cudaMalloc(&d_hub, sizeof(int32_t) * 32) != cudaSuccess || cudaMalloc(&d_key, sizeof(uint32_t) * g.n) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_hub);
+        set_error("order key buffers");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<void, void (*)(void*)> f1(d_hub, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_key, [](void* p) { cudaFree(p); });
+    GBC_CUDA(cudaMemcpyAsync(d_hub, idx.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, G->stream));
+    LaneRequest rq;
+    rq.job = LaneJob::CC;
+    rq.d_src = d_hub;
+    rq.kb = kb;
+    rq.d_profile_key = d_key;
+    LaneResult res;
+    GBC_TRY(E->run(rq, res));
+    G->key.resize(g.n);
+    GBC_CUDA(cudaMemcpyAsync(G->key.data(), d_key, sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    return GBC_OK;
+}
+
+// Reorder sources so that each 32-lane group holds sources with similar BFS
+// level profiles (denser lane masks, fewer frontier entries).  pos[i] = index
+// in the caller's list of the i-th ordered source.
+static gbc_status order_sources(gbc_graph_s* G, const gbc_options& o, bool bc, std::vector<int32_t>& hsrc,
+                                std::vector<int32_t>& pos) {
+    const int64_t k = (int64_t)hsrc.size();
+    pos.resize(k);
+    for (int64_t i = 0; i < k; i++) pos[i] = (int32_t)i;
+    if (o.engine == GBC_ENGINE_PLAIN || o.source_order != 0 || k <= 32) return GBC_OK;
+    LaneEngine* E = nullptr;
+    GBC_TRY(get_engine(G, pick_lanes(G, k, bc, o.lanes), bc, o, &E));
+    GBC_TRY(ensure_order_key(G, E));
+    const std::vector<uint32_t>& key = G->key;
+    const std::vector<int32_t>& deg = G->deg;
+    std::stable_sort(pos.begin(), pos.end(), [&](int32_t a, int32_t b) {
+        const int32_t x = hsrc[a], y = hsrc[b];
+        if (key[x] != key[y]) return key[x] < key[y];
+        return deg[x] > deg[y];
+    });
+    std::vector<int32_t> ordered(k);
+    for (int64_t i = 0; i < k; i++) ordered[i] = hsrc[pos[i]];
+    hsrc.swap(ordered);
+    return GBC_OK;
+}
+
+static gbc_status upload_sources(gbc_graph_s* G, const std::vector<int32_t>& hsrc) {
+    if ((int64_t)hsrc.size() > G->src_cap) {
+        cudaFree(G->d_src);
+        G->d_src = nullptr;
+        if (cudaMalloc(&G->d_src, sizeof(int32_t) * hsrc.size()) != cudaSuccess) { cudaGetLastError(); set_error("source buffer"); return GBC_ERR_NOMEM; }
+        G->src_cap = (int64_t)hsrc.size();
+    }
+    GBC_CUDA(cudaMemcpyAsync(G->d_src, hsrc.data(), sizeof(int32_t) * hsrc.size(), cudaMemcpyHostToDevice, G->stream));
+    return GBC_OK;
+}
+
+__global__ void scatter_cc_kernel(const unsigned long long* __restrict__ in, const int32_t* __restrict__ pos, int32_t k,
+                                  int64_t* __restrict__ out) {
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) out[pos[i]] = (int64_t)in[i];
+}
+
+static gbc_status resolve_sources(gbc_graph_s* G, const int32_t* sources, int32_t k, std::vector<int32_t>& hsrc) {
     const DevGraph& g = G->g;
     if (k < 0) { set_error("k < 0"); return GBC_ERR_ARG; }
     if (k == 0) {
@@ -148,13 +236,6 @@ static gbc_status stage_sources(gbc_graph_s* G, const int32_t* sources, int32_t 
         for (int32_t i = 0; i < k; i++)
             if (hsrc[i] < 0 || hsrc[i] >= g.n) { set_error("source %d out of range [0,%d)", hsrc[i], g.n); return GBC_ERR_ARG; }
     }
-    if ((int64_t)hsrc.size() > G->src_cap) {
-        cudaFree(G->d_src);
-        G->d_src = nullptr;
-        if (cudaMalloc(&G->d_src, sizeof(int32_t) * hsrc.size()) != cudaSuccess) { cudaGetLastError(); set_error("source buffer"); return GBC_ERR_NOMEM; }
-        G->src_cap = (int64_t)hsrc.size();
-    }
-    GBC_CUDA(cudaMemcpyAsync(G->d_src, hsrc.data(), sizeof(int32_t) * hsrc.size(), cudaMemcpyHostToDevice, G->stream));
     return GBC_OK;
 }
 
@@ -200,7 +281,7 @@ static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const
         }
         return GBC_OK;
     }
-    const int32_t lanes = pick_lanes(g, k, true, o.lanes);
+    const int32_t lanes = pick_lanes(G, k, true, o.lanes);
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, true, o, &E));
     lanes_used = lanes;
@@ -239,7 +320,7 @@ static gbc_status cc_core(gbc_graph_s* G, const int32_t* d_src, const int32_t* h
         batches = k;
         return GBC_OK;
     }
-    const int32_t lanes = pick_lanes(g, k, false, o.lanes);
+    const int32_t lanes = pick_lanes(G, k, false, o.lanes);
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, false, o, &E));
     lanes_used = lanes;
@@ -344,8 +425,10 @@ gbc_status gbc_bc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
-    std::vector<int32_t> hsrc;
-    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    std::vector<int32_t> hsrc, pos;
+    GBC_TRY(resolve_sources(G, sources, k, hsrc));
+    GBC_TRY(order_sources(G, o, true, hsrc, pos));
+    GBC_TRY(upload_sources(G, hsrc));
     const int32_t kk = (int32_t)hsrc.size();
     if (!G->d_bc) {
         if (cudaMalloc(&G->d_bc, sizeof(double) * G->g.n) != cudaSuccess) { cudaGetLastError(); set_error("bc buffer"); return GBC_ERR_NOMEM; }
@@ -375,18 +458,25 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     cudaStream_t us = (cudaStream_t)stream;
     GBC_CUDA(cudaEventRecord(G->ev0, us));
     GBC_CUDA(cudaStreamWaitEvent(G->stream, G->ev0, 0));
+    // the source list comes to the host (k ints) to be validated and grouped
+    std::vector<int32_t> hsrc(k), pos;
+    GBC_CUDA(cudaMemcpyAsync(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    for (int32_t i = 0; i < k; i++)
+        if (hsrc[i] < 0 || hsrc[i] >= G->g.n) { set_error("source %d out of range [0,%d)", hsrc[i], G->g.n); return GBC_ERR_ARG; }
+    GBC_TRY(order_sources(G, o, true, hsrc, pos));
+    GBC_TRY(upload_sources(G, hsrc));
     LaneResult res;
     int32_t lanes = 0;
     int sig = 0;
     int64_t batches = 0;
-    GBC_TRY(bc_core(G, d_sources, k, o, d_bc, res, lanes, sig, batches));
+    GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
+    GBC_TRY(bc_core(G, G->d_src, k, o, d_bc, res, lanes, sig, batches));
     GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
     GBC_CUDA(cudaStreamWaitEvent(us, G->ev1, 0));
     GBC_CUDA(cudaEventSynchronize(G->ev1));
     float ms = 0;
     cudaEventElapsedTime(&ms, G->ev0, G->ev1);
-    std::vector<int32_t> hsrc(k);
-    GBC_CUDA(cudaMemcpy(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
     finish_stats(G, res, k, batches, lanes, sig, hsrc, ms, now_ms() - t0);
     return GBC_OK;
 }
@@ -397,8 +487,10 @@ gbc_status gbc_cc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
-    std::vector<int32_t> hsrc;
-    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    std::vector<int32_t> hsrc, pos;
+    GBC_TRY(resolve_sources(G, sources, k, hsrc));
+    GBC_TRY(order_sources(G, o, false, hsrc, pos));
+    GBC_TRY(upload_sources(G, hsrc));
     const int32_t kk = (int32_t)hsrc.size();
     if (kk > G->ccb_cap) {
         cudaFree(G->d_ccb);
@@ -410,11 +502,13 @@ gbc_status gbc_cc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     int32_t lanes = 0;
     int64_t batches = 0;
     GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
-    GBC_TRY(cc_core(G, G->d_src, hsrc.data(), kk, o, G->d_ccb, cc, res, lanes, batches));
+    std::vector<int64_t> ordered(kk);
+    GBC_TRY(cc_core(G, G->d_src, hsrc.data(), kk, o, G->d_ccb, ordered.data(), res, lanes, batches));
     GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
     if (o.engine != GBC_ENGINE_PLAIN)
-        GBC_CUDA(cudaMemcpyAsync(cc, G->d_ccb, sizeof(int64_t) * kk, cudaMemcpyDeviceToHost, G->stream));
+        GBC_CUDA(cudaMemcpyAsync(ordered.data(), G->d_ccb, sizeof(int64_t) * kk, cudaMemcpyDeviceToHost, G->stream));
     GBC_CUDA(cudaStreamSynchronize(G->stream));
+    for (int32_t i = 0; i < kk; i++) cc[pos[i]] = ordered[i];
     float ms = 0;
     cudaEventElapsedTime(&ms, G->ev0, G->ev1);
     finish_stats(G, res, kk, batches, lanes, GBC_SIGMA_EXACT, hsrc, ms, now_ms() - t0);
@@ -432,17 +526,38 @@ gbc_status gbc_cc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     cudaStream_t us = (cudaStream_t)stream;
     GBC_CUDA(cudaEventRecord(G->ev0, us));
     GBC_CUDA(cudaStreamWaitEvent(G->stream, G->ev0, 0));
+    std::vector<int32_t> hsrc(k), pos;
+    GBC_CUDA(cudaMemcpyAsync(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    for (int32_t i = 0; i < k; i++)
+        if (hsrc[i] < 0 || hsrc[i] >= G->g.n) { set_error("source %d out of range [0,%d)", hsrc[i], G->g.n); return GBC_ERR_ARG; }
+    GBC_TRY(order_sources(G, o, false, hsrc, pos));
+    GBC_TRY(upload_sources(G, hsrc));
+    if (k > G->ccb_cap) {
+        cudaFree(G->d_ccb);
+        G->d_ccb = nullptr;
+        if (cudaMalloc(&G->d_ccb, sizeof(unsigned long long) * k) != cudaSuccess) { cudaGetLastError(); set_error("cc buffer"); return GBC_ERR_NOMEM; }
+        G->ccb_cap = k;
+    }
+    if (k > G->pos_cap) {
+        cudaFree(G->d_pos);
+        G->d_pos = nullptr;
+        if (cudaMalloc(&G->d_pos, sizeof(int32_t) * k) != cudaSuccess) { cudaGetLastError(); set_error("position buffer"); return GBC_ERR_NOMEM; }
+        G->pos_cap = k;
+    }
+    GBC_CUDA(cudaMemcpyAsync(G->d_pos, pos.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, G->stream));
     LaneResult res;
     int32_t lanes = 0;
     int64_t batches = 0;
-    GBC_TRY(cc_core(G, d_sources, nullptr, k, o, (unsigned long long*)d_cc, nullptr, res, lanes, batches));
+    GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
+    GBC_TRY(cc_core(G, G->d_src, nullptr, k, o, G->d_ccb, nullptr, res, lanes, batches));
+    scatter_cc_kernel<<<std::max(1, std::min(1024, (k + 255) / 256)), 256, 0, G->stream>>>(G->d_ccb, G->d_pos, k, d_cc);
+    GBC_CUDA(cudaGetLastError());
     GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
     GBC_CUDA(cudaStreamWaitEvent(us, G->ev1, 0));
     GBC_CUDA(cudaEventSynchronize(G->ev1));
     float ms = 0;
     cudaEventElapsedTime(&ms, G->ev0, G->ev1);
-    std::vector<int32_t> hsrc(k);
-    GBC_CUDA(cudaMemcpy(hsrc.data(), d_sources, sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
     finish_stats(G, res, k, batches, lanes, GBC_SIGMA_EXACT, hsrc, ms, now_ms() - t0);
     return GBC_OK;
 }
@@ -454,7 +569,8 @@ gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_op
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
     std::vector<int32_t> hsrc;
-    GBC_TRY(stage_sources(G, sources, k, hsrc));
+    GBC_TRY(resolve_sources(G, sources, k, hsrc));
+    GBC_TRY(upload_sources(G, hsrc));
     const int32_t n = G->g.n;
     const int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((k + 31) / 32) * 32);
     LaneEngine* E = nullptr;

@@ -53,6 +53,7 @@ struct LaneRequest {
     int32_t* d_dist = nullptr;           // [kb][n] (SSSP) nullable
     uint64_t* d_sigma = nullptr;         // [kb][n] (SSSP) nullable
     bool abort_on_overflow = false;      // exact sigma: stop before the backward sweep if a lane overflowed
+    uint32_t* d_profile_key = nullptr;   // [n] (CC job): level of lane 0 << 16 | min level of lanes 1..31
 };
 
 struct LaneResult {

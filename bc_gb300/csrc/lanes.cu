@@ -49,7 +49,7 @@ struct Ctl {
     int done;
     int err;            // bit0: a frontier queue overflowed, bit1: level cap of the level type
     unsigned blocks;    // finished-CTA counter of the running launch
-    int pad;
+    int any_ovf;        // some lane's exact path count overflowed uint64
     unsigned long long tail;    // append position, regular queue
     unsigned long long htail;   // append position, hub queue
     unsigned long long next;    // fetch position of the running level, regular queue
@@ -474,7 +474,10 @@ __device__ __forceinline__ void fwd_store(const KArgs& A, int g, size_t gbase, i
     const size_t vi = ((gbase + (size_t)v) << 5) + t;
     if (MODE == 1) {
         A.sig[vi] = acc;
-        if (of) atomicOr(&A.ovf[g], 1u << t);
+        if (of) {
+            atomicOr(&A.ovf[g], 1u << t);
+            A.ctl->any_ovf = 1;
+        }
     } else {
         reinterpret_cast<double*>(A.sig)[vi] = lm + log2(ls);
     }
@@ -807,6 +810,23 @@ __global__ void sssp_out_kernel(KArgs A, int kb, int32_t* dist, uint64_t* sigma,
     }
 }
 
+// Level profile of every vertex from the first lane group: (level in lane 0)
+// << 16 | (smallest level over lanes 1..31); unreached = all ones.  Used to
+// group sources whose BFS levels move together into the same lane group.
+__global__ void profile_key_kernel(KArgs A, int lvl_bytes, uint32_t* __restrict__ key) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.n; v += gridDim.x * blockDim.x) {
+        unsigned l0 = 0xFFFFu, lm = 0xFFFFu;
+        for (int t = 0; t < 32; t++) {
+            const size_t i = sidx(0, A.n, v, t);
+            unsigned L = lvl_bytes == 1 ? reinterpret_cast<const uint8_t*>(A.lvl)[i] : reinterpret_cast<const uint16_t*>(A.lvl)[i];
+            if (lvl_bytes == 1 && L == 0xFFu) L = 0xFFFFu;
+            if (t == 0) l0 = L;
+            else lm = min(lm, L);
+        }
+        key[v] = (l0 << 16) | lm;
+    }
+}
+
 // bc[v] = sum over lane groups of the per-group partials (fixed order).
 __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, double* __restrict__ bc) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -1064,6 +1084,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
             res.fwd_ms += ms;
             if (h->done) break;
+            if (h->any_ovf && rq.abort_on_overflow) break;   // the batch is redone in log form anyway
             if (launched > (int64_t)MAX_LEVEL + 2 * lpg_) { set_error("forward level loop did not terminate"); return GBC_ERR_LIMIT; }
         }
         const int maxlevel = h->maxlevel;
@@ -1097,6 +1118,11 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         }
         res.levels += maxlevel + 1;
         res.frontier_entries += (int64_t)(entries + hentries);
+        if (rq.d_profile_key) {
+            profile_key_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, lvl_bytes_, rq.d_profile_key);
+            GBC_CUDA(cudaGetLastError());
+            res.kernel_launches++;
+        }
         if (rq.job == LaneJob::SSSP) {
             sssp_out_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, rq.kb, rq.d_dist, rq.d_sigma, lvl_bytes_);
             GBC_CUDA(cudaGetLastError());

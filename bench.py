@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--scale", type=int, default=22)
     p.add_argument("--edge-factor", type=int, default=16)
     p.add_argument("--k", type=int, default=16384)
-    p.add_argument("--delta", default="f64", choices=["f32", "f64"])
+    p.add_argument("--delta", default="f32", choices=["f32", "f64"],
+                   help="dependency-sweep precision (FP32 delta with FP64 BC sums is the default design)")
     p.add_argument("--plain-sources", type=int, default=16)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
@@ -373,6 +374,25 @@ def main():
     out = None
     if rank == 0:
         # plain one-source-at-a-time engine on a sample of the same sources
+        # precision: the step's sources with FP32 and FP64 dependency sweeps
+        s0 = step_sources(args.warmup)
+        bc32 = graph.bc(s0, **{**opt, "delta_precision": G.DELTA_F32})
+        bc64 = graph.bc(s0, **{**opt, "delta_precision": G.DELTA_F64})
+        nz = bc64 > 0
+        prec = {"delta_f32_rel_err_vs_f64": float(np.max(np.abs(bc32 - bc64) / np.maximum(np.abs(bc64), 1.0))),
+                "delta_f32_rel_err_vs_f64_nonzero": float(np.max(np.abs(bc32[nz] - bc64[nz]) / bc64[nz])) if nz.any() else 0.0,
+                "sources": int(B),
+                "note": "rel err = max|a-b|/max(|b|,1) as in the tests; the FP64-delta path is checked against the "
+                        "FP64 oracle to 1e-9 in tests"}
+        # closeness on the same graph: batched lanes vs the plain engine
+        graph.cc(s0, lanes=B)
+        stc = graph.stats()
+        cc_gteps = float(ce[s0].sum()) / (stc["kernel_ms"] * 1e-3) / 1e9
+        graph.cc(s0[:args.plain_sources], engine=G.ENGINE_PLAIN)
+        stp = graph.stats()
+        cc_plain = float(ce[s0[:args.plain_sources]].sum()) / (stp["kernel_ms"] * 1e-3) / 1e9
+        closeness = {"value": round(cc_gteps, 3), "unit": "GTEPS", "sources": int(B),
+                     "plain": round(cc_plain, 3), "speedup_batched_vs_plain": round(cc_gteps / cc_plain, 2)}
         plain_gteps = None
         if not args.no_plain:
             ps = sample[:args.plain_sources]
@@ -426,7 +446,7 @@ def main():
                "plain": None if plain_gteps is None else {
                    "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),
                    "speedup_batched_vs_plain": round(gteps / plain_gteps, 2)},
-               "serving": serve, "clocks": clocks}
+               "closeness": closeness, "precision": prec, "serving": serve, "clocks": clocks}
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.barrier()

@@ -73,7 +73,9 @@ typedef struct {
     int32_t sparse_lanes;     /* a frontier task with <= this many active lanes expands
                                  edge-parallel, otherwise lane-parallel; -1 = autotune */
     int32_t levels_per_graph; /* level kernels per captured CUDA graph; 0 = default */
-    int32_t reserved[9];
+    int32_t source_order;     /* 0: group sources with similar BFS level profiles into the same
+                                 lane group (results do not depend on it); 1: lanes in the order given */
+    int32_t reserved[8];
 } gbc_options;
 
 typedef struct {
