@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "libgbc.so")
 
 BC_BRANDES, BC_REFERENCE = 0, 1
 DELTA_F32, DELTA_F64 = 0, 1
-SIGMA_AUTO, SIGMA_EXACT, SIGMA_LOG = 0, 1, 2
+SIGMA_AUTO, SIGMA_EXACT, SIGMA_WIDE = 0, 1, 2
 ENGINE_AUTO, ENGINE_PLAIN, ENGINE_LANES = 0, 1, 2
 Q_CC, Q_BC, Q_BC_SAMPLED = 0, 1, 2
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)

@@ -113,7 +113,7 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (opt) o = *opt;
     if (o.semantics != GBC_BC_BRANDES && o.semantics != GBC_BC_REFERENCE) { set_error("bad semantics"); return GBC_ERR_ARG; }
     if (o.delta_precision != GBC_DELTA_F32 && o.delta_precision != GBC_DELTA_F64) { set_error("bad delta precision"); return GBC_ERR_ARG; }
-    if (o.sigma_mode < GBC_SIGMA_AUTO || o.sigma_mode > GBC_SIGMA_LOG) { set_error("bad sigma mode"); return GBC_ERR_ARG; }
+    if (o.sigma_mode < GBC_SIGMA_AUTO || o.sigma_mode > GBC_SIGMA_WIDE) { set_error("bad sigma mode"); return GBC_ERR_ARG; }
     if (o.engine < GBC_ENGINE_AUTO || o.engine > GBC_ENGINE_LANES) { set_error("bad engine"); return GBC_ERR_ARG; }
     if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("lanes must be 0 or a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
     return GBC_OK;
@@ -275,8 +275,8 @@ static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const
         lanes_used = 1;
         sigma_used = GBC_SIGMA_EXACT;
         batches = k;
-        if (res.overflow_count && o.sigma_mode != GBC_SIGMA_LOG) {
-            set_error("exact path counts overflowed uint64 for %d sources (plain engine has no log form)", res.overflow_count);
+        if (res.overflow_count && o.sigma_mode != GBC_SIGMA_WIDE) {
+            set_error("exact path counts overflowed uint64 for %d sources (plain engine has no wide form)", res.overflow_count);
             return GBC_ERR_OVERFLOW;
         }
         return GBC_OK;
@@ -286,8 +286,10 @@ static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const
     GBC_TRY(get_engine(G, lanes, true, o, &E));
     lanes_used = lanes;
     GBC_TRY(E->bc_begin());
-    sigma_used = o.sigma_mode == GBC_SIGMA_LOG ? GBC_SIGMA_LOG : GBC_SIGMA_EXACT;
+    sigma_used = o.sigma_mode == GBC_SIGMA_WIDE ? GBC_SIGMA_WIDE : GBC_SIGMA_EXACT;
     batches = 0;
+    // AUTO: once a batch of this call has overflowed, the later ones start in wide form
+    bool wide = (o.sigma_mode == GBC_SIGMA_WIDE);
     for (int32_t b0 = 0; b0 < k; b0 += lanes) {
         LaneRequest rq;
         rq.job = LaneJob::BC;
@@ -295,15 +297,16 @@ static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const
         rq.kb = std::min(lanes, k - b0);
         rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
         rq.semantics = o.semantics;
-        rq.sigma_log = (o.sigma_mode == GBC_SIGMA_LOG);
-        rq.abort_on_overflow = !rq.sigma_log;
+        rq.sigma_wide = wide;
+        rq.abort_on_overflow = !rq.sigma_wide;
         gbc_status st = E->run(rq, res);
-        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO) {
-            rq.sigma_log = 1;
+        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO && !wide) {
+            wide = true;
+            rq.sigma_wide = 1;
             rq.abort_on_overflow = false;
-            sigma_used = GBC_SIGMA_LOG;
             st = E->run(rq, res);
         }
+        if (wide) sigma_used = GBC_SIGMA_WIDE;
         if (st != GBC_OK) return st;
         batches++;
     }

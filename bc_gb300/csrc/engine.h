@@ -45,7 +45,7 @@ struct LaneRequest {
     LaneJob job = LaneJob::CC;
     const int32_t* d_src = nullptr;  // device sources of this batch
     int32_t kb = 0;                  // sources in this batch (<= lanes)
-    int sigma_log = 0;               // 1: log2-domain path counts
+    int sigma_wide = 0;              // 1: wide-exponent path counts
     int delta_f64 = 1;
     int semantics = GBC_BC_BRANDES;
     unsigned long long* d_cc = nullptr;  // [kb] per-lane distance sums (CC)
@@ -104,7 +104,6 @@ private:
     bool need_bc_ = false;
     int sparse_ = 2;
     int lpg_ = 16;
-    int grid_ = 0;
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
     cudaStream_t stream_ = nullptr;
     size_t bytes_ = 0;

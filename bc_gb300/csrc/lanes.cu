@@ -83,8 +83,18 @@ struct KArgs {
 };
 
 constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expanded by a whole CTA
-constexpr int FETCH = 8;        // regular entries a warp takes per fetch
+constexpr int FETCH = 32;       // regular entries a warp takes per fetch, one per thread
+constexpr int LIGHT = 16;       // an entry with (active lanes x degree) <= LIGHT is expanded by one thread
+constexpr int STG = 128;        // regular-queue entries a warp stages in shared memory per append
 constexpr int WARPS = BLOCK / 32;
+// Minimum resident CTAs per SM the level kernels are compiled for.  Deep
+// graphs (16-bit levels) have small, latency-bound levels and need 4 (64
+// registers); so do the wide-sigma variants, which would otherwise take over
+// 100 registers.  For exact sigma on 8-bit levels 0 leaves the choice to the
+// compiler, which also lands on 64 registers and measured 4-6% faster on
+// R-MAT scale 22 than forcing 4 or 5 (48 registers); unbounded (113+
+// registers, 2 CTAs) is 35% slower.
+template <typename LT, bool WIDE> constexpr int MINB = (sizeof(LT) == 2 || WIDE) ? 4 : 0;
 
 __device__ __forceinline__ size_t sidx(int g, int n, int v, int t) {
     return ((((size_t)g * (size_t)n) + (size_t)v) << 5) + (size_t)t;
@@ -92,26 +102,132 @@ __device__ __forceinline__ size_t sidx(int g, int n, int v, int t) {
 
 __device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > HUB_DEG; }
 
-// Warp-aggregated append of the entries of threads with has == true, hub
-// entries to the hub queue, the rest to the regular queue.
-__device__ __forceinline__ void warp_append(const KArgs& A, bool has, bool hub, uint32_t ent) {
+// ---- wide-exponent path counts ---------------------------------------------
+// Path counts past uint64 are held as (1 + f/2^44) * 2^(e - WBIAS) in one
+// 64-bit word e << 44 | f (the word 0 is zero): 44 fraction bits (relative
+// step 5.7e-14) and a 20-bit exponent, so |log2| < 2^19.  A sum aligns the
+// exponents with integer arithmetic and adds once in FP64; the dependency
+// sweep multiplies mantissas and adds exponents.  No exp2/log2 is evaluated,
+// which matters on a part whose FP64 rate is a small fraction of FP32.
+constexpr int WFRAC = 44;
+constexpr int WBIAS = 1 << 19;
+constexpr int WEMAX = (1 << (64 - WFRAC)) - 1;
+constexpr unsigned long long WFMASK = (1ULL << WFRAC) - 1ULL;
+constexpr unsigned long long WONE = (unsigned long long)WBIAS << WFRAC;
+constexpr int WEMPTY = -0x7FFFFFFF;   // exponent of an empty accumulator
+
+// x * 2^k for positive normal x; 0 below the normal range.
+__device__ __forceinline__ double pow2s(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7FF) + k;
+    if (be < 1) return 0.0;
+    if (be > 2046) return INFINITY;
+    return __longlong_as_double(b + (long long)k * (1LL << 52));
+}
+__device__ __forceinline__ float pow2s(float x, int k) {
+    const int b = __float_as_int(x);
+    const int be = ((b >> 23) & 0xFF) + k;
+    if (be < 1) return 0.0f;
+    if (be > 254) return INFINITY;
+    return __int_as_float(b + k * (1 << 23));
+}
+
+__device__ __forceinline__ int wexp(uint64_t u) { return (int)(u >> WFRAC) - WBIAS; }
+template <typename T> __device__ __forceinline__ T wmant(uint64_t u);
+template <> __device__ __forceinline__ double wmant<double>(uint64_t u) {
+    return __longlong_as_double((long long)((1023ULL << 52) | ((u & WFMASK) << (52 - WFRAC))));
+}
+template <> __device__ __forceinline__ float wmant<float>(uint64_t u) {   // rounded to 24 bits
+    return __uint_as_float(0x3F800000u + (unsigned)(((u & WFMASK) + (1ULL << (WFRAC - 24))) >> (WFRAC - 23)));
+}
+
+// Word of s * 2^E for positive normal s, rounded to 44 fraction bits.  Below
+// the range gives 0; above it sets of.
+__device__ __forceinline__ uint64_t wpack(double s, int E, bool& of) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+    int e = E + (int)((b >> 52) & 0x7FF) - 1023;
+    unsigned long long f = ((b & ((1ULL << 52) - 1ULL)) + (1ULL << (51 - WFRAC))) >> (52 - WFRAC);
+    if (f >> WFRAC) { f = 0; e++; }
+    const int eb = e + WBIAS;
+    if (eb < 1) return 0ULL;
+    if (eb > WEMAX) { of = true; return ~0ULL; }
+    return ((unsigned long long)eb << WFRAC) | f;
+}
+__device__ __forceinline__ uint64_t wpack(float s, int E, bool& of) {
+    const unsigned b = __float_as_uint(s);
+    const int eb = E + (int)((b >> 23) & 0xFF) - 127 + WBIAS;
+    if (eb < 1) return 0ULL;
+    if (eb > WEMAX) { of = true; return ~0ULL; }
+    return ((unsigned long long)eb << WFRAC) | ((unsigned long long)(b & 0x7FFFFFu) << (WFRAC - 23));
+}
+
+// Accumulators s * 2^E (E == WEMPTY: empty).
+__device__ __forceinline__ void wadd(double& s, int& E, uint64_t u) {
+    const int e = wexp(u);
+    const double m = wmant<double>(u);
+    if (E == WEMPTY) { s = m; E = e; }
+    else if (e > E) { s = pow2s(s, E - e) + m; E = e; }
+    else s += pow2s(m, e - E);
+}
+__device__ __forceinline__ void wmerge(double& s, int& E, double s2, int E2) {
+    if (E2 == WEMPTY) return;
+    if (E == WEMPTY) { s = s2; E = E2; }
+    else if (E2 > E) { s = pow2s(s, E - E2) + s2; E = E2; }
+    else s += pow2s(s2, E2 - E);
+}
+
+// sigma(v) * rho(w) as a plain T, sigma(v) given as mantissa mv and exponent ev.
+template <typename T>
+__device__ __forceinline__ T wterm(T mv, int ev, uint64_t r) {
+    return pow2s(mv * wmant<T>(r), ev + wexp(r));
+}
+
+// ---- frontier appends ------------------------------------------------------
+// A warp stages the regular entries it discovers in shared memory and appends
+// them to the queue with one atomic per STG entries (or at the end of the
+// launch), so the queue tail sees few atomics even when every entry of a level
+// discovers one or two vertices.
+struct Stage {
+    uint32_t* buf;
+    int cnt;   // uniform across the warp
+};
+
+__device__ __forceinline__ void stage_flush(const KArgs& A, Stage& S) {
     const int t = threadIdx.x & 31;
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        const bool mine = has && (hub == (k == 1));
-        const unsigned m = __ballot_sync(FULL, mine);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        unsigned long long* tail = k ? &A.ctl->htail : &A.ctl->tail;
+    __syncwarp();
+    if (S.cnt == 0) return;
+    unsigned long long base = 0;
+    if (t == 0) base = atomicAdd(&A.ctl->tail, (unsigned long long)S.cnt);
+    base = __shfl_sync(FULL, base, 0);
+    for (int k = t; k < S.cnt; k += 32) {
+        const unsigned long long pos = base + (unsigned long long)k;
+        if (pos < A.fcap) A.fq[pos] = S.buf[k];
+    }
+    __syncwarp();
+    S.cnt = 0;
+}
+
+// Entries of threads with has == true: hub entries straight to the hub queue,
+// the rest to the warp's stage.
+__device__ __forceinline__ void warp_append(const KArgs& A, Stage& S, bool has, bool hub, uint32_t ent) {
+    const int t = threadIdx.x & 31;
+    const unsigned lt = (1u << t) - 1u;
+    const unsigned hm = __ballot_sync(FULL, has && hub);
+    if (hm) {
+        const int leader = __ffs(hm) - 1;
         unsigned long long base = 0;
-        if (t == leader) base = atomicAdd(tail, (unsigned long long)__popc(m));
+        if (t == leader) base = atomicAdd(&A.ctl->htail, (unsigned long long)__popc(hm));
         base = __shfl_sync(FULL, base, leader);
-        if (mine) {
-            const unsigned long long pos = base + __popc(m & ((1u << t) - 1u));
-            if (k) { if (pos < A.hcap) A.hq[pos] = ent; }
-            else { if (pos < A.fcap) A.fq[pos] = ent; }
+        if (has && hub) {
+            const unsigned long long pos = base + __popc(hm & lt);
+            if (pos < A.hcap) A.hq[pos] = ent;
         }
     }
+    const unsigned m = __ballot_sync(FULL, has && !hub);
+    if (!m) return;
+    if (S.cnt + __popc(m) > STG) stage_flush(A, S);
+    if (has && !hub) S.buf[S.cnt + __popc(m & lt)] = ent;
+    S.cnt += __popc(m);
 }
 
 // First claim of (x, g) for level lev: a plain read filters repeats before the atomic.
@@ -119,17 +235,6 @@ __device__ __forceinline__ bool claim(const KArgs& A, size_t gbase, int x, int l
     int32_t* p = &A.vmark[gbase + x];
     if (*(volatile int32_t*)p == lev) return false;
     return atomicExch(p, lev) != lev;
-}
-
-__device__ __forceinline__ void lse_add(double& m, double& s, double y) {
-    if (y > m) { s = s * exp2(m - y) + 1.0; m = y; }
-    else s += exp2(y - m);
-}
-__device__ __forceinline__ void lse_merge(double& m, double& s, double m2, double s2) {
-    const double M = fmax(m, m2);
-    if (M == -INFINITY) { m = M; s = 0.0; return; }
-    s = s * exp2(m - M) + s2 * exp2(m2 - M);
-    m = M;
 }
 
 // Last CTA of a forward launch publishes the next level's frontier bounds.
@@ -182,30 +287,74 @@ template <> struct Simd<uint16_t> {
     __device__ static __forceinline__ bool has(unsigned m, int j) { return (m >> (16 * j)) & 1u; }
 };
 
+// Lanes of one level row whose level equals d, as a 32-bit mask (bit t = lane
+// t), read with 16-byte loads by a single thread.  The byte (half-word) compare
+// leaves the top bit of each matching lane set; one multiply gathers those
+// bits, whose shifted copies land on distinct positions, into the top nibble.
+__device__ __forceinline__ unsigned row_mask(const uint8_t* r, int d) {
+    const uint4* p = reinterpret_cast<const uint4*>(r);
+    const uint4 a = p[0], b = p[1];
+    const unsigned w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const unsigned d4 = Simd<uint8_t>::bc(d);
+    unsigned m = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) m |= (((__vcmpeq4(w[k], d4) & 0x80808080u) * 0x00204081u) >> 28) << (4 * k);
+    return m;
+}
+__device__ __forceinline__ unsigned row_mask(const uint16_t* r, int d) {
+    const uint4* p = reinterpret_cast<const uint4*>(r);
+    const unsigned d2 = Simd<uint16_t>::bc(d);
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const uint4 a = p[q];
+        const unsigned w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) m |= (((__vcmpeq2(w[k], d2) & 0x80008000u) * 0x8001u) >> 30) << (8 * q + 2 * k);
+    }
+    return m;
+}
+
+// One regular entry per thread of a fetch: its active-lane mask and CSR row.
+template <typename LT>
+__device__ __forceinline__ void fetch_entry(const KArgs& A, int d, unsigned long long i, unsigned long long e,
+                                            uint32_t& ent, unsigned& am, long long& r0, long long& r1) {
+    ent = 0;
+    am = 0;
+    r0 = r1 = 0;
+    if (i >= e) return;
+    ent = A.fq[i];
+    const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+    am = row_mask(reinterpret_cast<const LT*>(A.lvl) + ((((size_t)g * (size_t)A.n) + (size_t)v) << 5), d);
+    r0 = A.row[v];
+    r1 = A.row[v + 1];
+}
+
 // Lane-parallel forward scan of v's neighbour chunks (r0 + 32*sub, step
 // 32*nsub).  Result for lane t is returned in thread t.  Path counts of the
 // LPW lanes a thread owns are read as 16-byte pairs; per-slot partial sums
 // meet in shared memory and are added in slot order.
 template <int MODE, typename LT>
-__device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t gbase, LT* lv, int v, long long r0,
-                                          long long r1, int sub, int nsub, uint64_t& acc, bool& of, double& lm,
-                                          double& ls) {
-    using S = Simd<LT>;
-    constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
+__device__ __forceinline__ void fwd_lanes(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, int v,
+                                          long long r0, long long r1, int sub, int nsub, uint64_t& acc, bool& of,
+                                          int& we_out, double& ws_out) {
+    using Sd = Simd<LT>;
+    constexpr int LPW = Sd::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
     constexpr unsigned PAIR = (LPW == 4) ? 0xFFFFu : 0xFFFFFFFFu;   // level bits of one pair of lanes
     __shared__ uint64_t part_a[WARPS][SLOTS][32];
     __shared__ double part_s[MODE == 2 ? WARPS : 1][SLOTS][32];
     __shared__ unsigned char part_o[WARPS][SLOTS][32];
     const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV, wib = threadIdx.x >> 5;
     const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
-    const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1);
-    const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
+    const unsigned d4 = Sd::bc(d), dp4 = Sd::bc(d - 1);
+    const unsigned act4 = Sd::eq(lvw[(size_t)v * WPV + w], d4);
     const uint64_t* sg = A.sig + (gbase << 5) + w * LPW;
     uint64_t a[LPW];
-    double m[LPW], sl[LPW];
+    int we[LPW];
+    double ws[LPW];
     unsigned ofm = 0;
 #pragma unroll
-    for (int j = 0; j < LPW; j++) { a[j] = 0; m[j] = -INFINITY; sl[j] = 0.0; }
+    for (int j = 0; j < LPW; j++) { a[j] = 0; we[j] = WEMPTY; ws[j] = 0.0; }
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
         const int cnt = (int)min(32LL, r1 - jb);
         const int kmax = (cnt + SLOTS - 1) / SLOTS;   // uniform across the warp
@@ -223,29 +372,25 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
 #pragma unroll
             for (int k = 0; k < ITER; k++) {
                 if (k >= kmax) break;
-                const unsigned pm = S::eq(Lw[k], dp4) & act4;
+                const unsigned pm = Sd::eq(Lw[k], dp4) & act4;
                 if (!pm) continue;
                 const size_t xo = (size_t)xs[k] << 5;
 #pragma unroll
                 for (int pr = 0; pr < LPW / 2; pr++) {
                     const unsigned pmp = (pm >> (pr * 2 * (32 / LPW))) & PAIR;
                     if (!pmp) continue;
-                    if (MODE == 1) {
-                        const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(sg + xo + 2 * pr);
-                        const uint64_t v2[2] = {vv.x, vv.y};
+                    const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(sg + xo + 2 * pr);
+                    const uint64_t v2[2] = {vv.x, vv.y};
 #pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            if (!S::has(pm, 2 * pr + h)) continue;
+                    for (int h = 0; h < 2; h++) {
+                        if (!Sd::has(pm, 2 * pr + h)) continue;
+                        if (MODE == 1) {
                             const uint64_t na = a[2 * pr + h] + v2[h];
                             ofm |= (unsigned)(na < a[2 * pr + h]) << (2 * pr + h);
                             a[2 * pr + h] = na;
+                        } else {
+                            wadd(ws[2 * pr + h], we[2 * pr + h], v2[h]);
                         }
-                    } else {
-                        const double2 vv = *reinterpret_cast<const double2*>(sg + xo + 2 * pr);
-                        const double v2[2] = {vv.x, vv.y};
-#pragma unroll
-                        for (int h = 0; h < 2; h++)
-                            if (S::has(pm, 2 * pr + h)) lse_add(m[2 * pr + h], sl[2 * pr + h], v2[h]);
                     }
                 }
             }
@@ -254,18 +399,18 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
         for (int k = 0; k < ITER; k++) {
             if (k >= kmax) break;
             const int q = k * SLOTS + s;
-            const unsigned un = S::eq(Lw[k], 0xFFFFFFFFu) & act4;   // unreached, in active lanes
-            const unsigned gm = S::gt(Lw[k], d4) & act4;            // unreached or already at d+1
+            const unsigned un = Sd::eq(Lw[k], 0xFFFFFFFFu) & act4;   // unreached, in active lanes
+            const unsigned gm = Sd::gt(Lw[k], d4) & act4;            // unreached or already at d+1
             if (un) {
                 LT* px = lv + ((size_t)xs[k] << 5) + w * LPW;
 #pragma unroll
                 for (int j = 0; j < LPW; j++)
-                    if (S::has(un, j)) px[j] = (LT)(d + 1);
+                    if (Sd::has(un, j)) px[j] = (LT)(d + 1);
             }
             const unsigned bal = __ballot_sync(FULL, gm != 0u);
             const unsigned slotm = (bal >> (s * WPV)) & ((1u << WPV) - 1u);
             const bool has = (w == 0) && (q < cnt) && slotm && claim(A, gbase, xs[k], d + 1);
-            warp_append(A, has, has && is_hub(A, xs[k]), ((uint32_t)xs[k] << 5) | (uint32_t)g);
+            warp_append(A, S, has, has && is_hub(A, xs[k]), ((uint32_t)xs[k] << 5) | (uint32_t)g);
         }
     }
     if (MODE == 0) return;
@@ -274,7 +419,7 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
     for (int j = 0; j < LPW; j++) {
         const int lane = w * LPW + j;
         if (MODE == 1) { part_a[wib][s][lane] = a[j]; part_o[wib][s][lane] = (ofm >> j) & 1u; }
-        else { part_a[wib][s][lane] = __double_as_longlong(m[j]); part_s[wib][s][lane] = sl[j]; }
+        else { part_a[wib][s][lane] = (uint64_t)(long long)we[j]; part_s[wib][s][lane] = ws[j]; }
     }
     __syncwarp();
     if (MODE == 1) {
@@ -290,39 +435,43 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, int d, int g, size_t g
         acc = r;
         of = o;
     } else {
-        double mm = __longlong_as_double(part_a[wib][0][t]), ss = part_s[wib][0][t];
+        int ee = (int)(long long)part_a[wib][0][t];
+        double ss = part_s[wib][0][t];
 #pragma unroll
-        for (int k = 1; k < SLOTS; k++) lse_merge(mm, ss, __longlong_as_double(part_a[wib][k][t]), part_s[wib][k][t]);
-        lm = mm;
-        ls = ss;
+        for (int k = 1; k < SLOTS; k++) wmerge(ss, ee, part_s[wib][k][t], (int)(long long)part_a[wib][k][t]);
+        we_out = ee;
+        ws_out = ss;
     }
     __syncwarp();
 }
 
-// Lane-parallel dependency scan: sum of rho over successors, predecessor
-// count, for lane t in thread t.
-template <bool LOG, typename T, typename LT>
-__device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, const LT* lv, int v, double lsv,
+// Lane-parallel dependency scan: sum of sigma(v)*rho(w) (WIDE) or rho(w) over
+// successors, predecessor count, for lane t in thread t.  mvt/evt: sigma(v) of
+// lane t in wide form.
+template <bool WIDE, typename T, typename LT>
+__device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, const LT* lv, int v, T mvt, int evt,
                                           long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
-    using S = Simd<LT>;
-    constexpr int LPW = S::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
+    using Sd = Simd<LT>;
+    constexpr int LPW = Sd::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
     constexpr unsigned PAIR = (LPW == 4) ? 0xFFFFu : 0xFFFFFFFFu;
     __shared__ double part_a[WARPS][SLOTS][32];
     __shared__ int part_p[WARPS][SLOTS][32];
     const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV, wib = threadIdx.x >> 5;
     const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
-    const unsigned d4 = S::bc(d), dp4 = S::bc(d - 1), dn4 = S::bc(d + 1);
-    const unsigned act4 = S::eq(lvw[(size_t)v * WPV + w], d4);
+    const unsigned d4 = Sd::bc(d), dp4 = Sd::bc(d - 1), dn4 = Sd::bc(d + 1);
+    const unsigned act4 = Sd::eq(lvw[(size_t)v * WPV + w], d4);
     const T* rh = reinterpret_cast<const T*>(A.rho) + (gbase << 5) + w * LPW;
-    const double* rhd = reinterpret_cast<const double*>(A.rho) + (gbase << 5) + w * LPW;
+    const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho) + (gbase << 5) + w * LPW;
     T a[LPW];
     int pcs[LPW];
-    double lsj[LPW];
+    T mj[LPW];
+    int ej[LPW];
 #pragma unroll
     for (int j = 0; j < LPW; j++) {
         a[j] = T(0);
         pcs[j] = 0;
-        lsj[j] = LOG ? __shfl_sync(FULL, lsv, w * LPW + j) : 0.0;
+        mj[j] = WIDE ? __shfl_sync(FULL, mvt, w * LPW + j) : T(0);
+        ej[j] = WIDE ? __shfl_sync(FULL, evt, w * LPW + j) : 0;
     }
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
         const int cnt = (int)min(32LL, r1 - jb);
@@ -340,38 +489,41 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
 #pragma unroll
         for (int k = 0; k < ITER; k++) {
             if (k >= kmax) break;
-            const unsigned sm = S::eq(Lw[k], dn4) & act4;
-            const unsigned pm = S::eq(Lw[k], dp4) & act4;
+            const unsigned sm = Sd::eq(Lw[k], dn4) & act4;
+            const unsigned pm = Sd::eq(Lw[k], dp4) & act4;
 #pragma unroll
-            for (int j = 0; j < LPW; j++) pcs[j] += S::has(pm, j);
+            for (int j = 0; j < LPW; j++) pcs[j] += Sd::has(pm, j);
             if (!sm) continue;
             const size_t xo = (size_t)xs[k] << 5;
-            if (!LOG && sizeof(T) == 4 && LPW == 4) {
+            if (!WIDE && sizeof(T) == 4 && LPW == 4) {
                 const float4 vv = *reinterpret_cast<const float4*>(rh + xo);
                 const float v4[4] = {vv.x, vv.y, vv.z, vv.w};
 #pragma unroll
                 for (int j = 0; j < LPW; j++)
-                    if (S::has(sm, j)) a[j] += (T)v4[j];
+                    if (Sd::has(sm, j)) a[j] += (T)v4[j];
             } else {
 #pragma unroll
                 for (int pr = 0; pr < LPW / 2; pr++) {
                     const unsigned smp = (sm >> (pr * 2 * (32 / LPW))) & PAIR;
                     if (!smp) continue;
-                    if (LOG || sizeof(T) == 8) {
-                        const double2 vv = *reinterpret_cast<const double2*>((LOG ? rhd : reinterpret_cast<const double*>(rh)) + xo + 2 * pr);
+                    if (WIDE) {
+                        const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(rw + xo + 2 * pr);
+                        const uint64_t v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++)
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += wterm<T>(mj[2 * pr + h], ej[2 * pr + h], v2[h]);
+                    } else if (sizeof(T) == 8) {
+                        const double2 vv = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(rh) + xo + 2 * pr);
                         const double v2[2] = {vv.x, vv.y};
 #pragma unroll
-                        for (int h = 0; h < 2; h++) {
-                            if (!S::has(sm, 2 * pr + h)) continue;
-                            if (LOG) a[2 * pr + h] += (T)exp2(lsj[2 * pr + h] + v2[h]);
-                            else a[2 * pr + h] += (T)v2[h];
-                        }
+                        for (int h = 0; h < 2; h++)
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
                     } else {
                         const float2 vv = *reinterpret_cast<const float2*>(rh + xo + 2 * pr);
                         const float v2[2] = {vv.x, vv.y};
 #pragma unroll
                         for (int h = 0; h < 2; h++)
-                            if (S::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
                     }
                 }
             }
@@ -397,18 +549,17 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
 
 // ---- forward --------------------------------------------------------------
 // Neighbour chunks r0 + 32*sub, stepping 32*nsub (nsub warps share a hub).
-// Pulls sigma from level d-1 neighbours into (acc, of) or (lm, ls) and
+// Pulls sigma from level d-1 neighbours into (acc, of) or (we, ws) and
 // discovers level d+1.
 template <int MODE, typename LT>
-__device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gbase, LT* lv, int v, bool act,
+__device__ __forceinline__ void fwd_scan(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, int v,
                                          unsigned am, long long r0, long long r1, int sub, int nsub, uint64_t& acc,
-                                         bool& of, double& lm, double& ls) {
+                                         bool& of, int& we, double& ws) {
     constexpr LT INF = (LT)Lv<LT>::INF;
     const int t = threadIdx.x & 31;
     const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
-    const double* sigd = reinterpret_cast<const double*>(A.sig);
     if (__popc(am) > A.sparse) {
-        fwd_lanes<MODE, LT>(A, d, g, gbase, lv, v, r0, r1, sub, nsub, acc, of, lm, ls);
+        fwd_lanes<MODE, LT>(A, S, d, g, gbase, lv, v, r0, r1, sub, nsub, acc, of, we, ws);
     } else {
         // edge-parallel: threads over neighbours, active lanes in turn
         unsigned rem = am;
@@ -417,7 +568,8 @@ __device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gb
             rem &= rem - 1u;
             uint64_t pacc = 0;
             bool pof = false;
-            double pm = -INFINITY, ps = 0.0;
+            int pe = WEMPTY;
+            double ps = 0.0;
             for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
                 const long long j = jb + t;
                 bool has = false;
@@ -427,14 +579,13 @@ __device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gb
                     LT* px = lv + ((size_t)x << 5) + a;
                     const LT Lx = *px;
                     if (MODE != 0 && d > 0 && Lx == dprev) {
-                        const size_t xi = ((gbase + (size_t)x) << 5) + a;
+                        const uint64_t sv = A.sig[((gbase + (size_t)x) << 5) + a];
                         if (MODE == 1) {
-                            const uint64_t sv = A.sig[xi];
                             const uint64_t na = pacc + sv;
                             pof |= (na < pacc);
                             pacc = na;
                         } else {
-                            lse_add(pm, ps, sigd[xi]);
+                            wadd(ps, pe, sv);
                         }
                     }
                     if (Lx > dl) {
@@ -442,7 +593,7 @@ __device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gb
                         has = claim(A, gbase, x, d + 1);
                     }
                 }
-                warp_append(A, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
+                warp_append(A, S, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
             }
             if (MODE == 1) {
 #pragma unroll
@@ -457,40 +608,99 @@ __device__ __forceinline__ void fwd_scan(const KArgs& A, int d, int g, size_t gb
             } else if (MODE == 2) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
-                    const double m2 = __shfl_xor_sync(FULL, pm, o);
+                    const int e2 = __shfl_xor_sync(FULL, pe, o);
                     const double s2 = __shfl_xor_sync(FULL, ps, o);
-                    lse_merge(pm, ps, m2, s2);
+                    wmerge(ps, pe, s2, e2);
                 }
-                if (t == a) { lm = pm; ls = ps; }
+                if (t == a) { we = pe; ws = ps; }
             }
         }
     }
 }
 
+// Store sigma of (v, lane a) of group g; flag lanes whose count left the range.
 template <int MODE>
-__device__ __forceinline__ void fwd_store(const KArgs& A, int g, size_t gbase, int v, uint64_t acc, bool of, double lm,
-                                          double ls) {
-    const int t = threadIdx.x & 31;
-    const size_t vi = ((gbase + (size_t)v) << 5) + t;
-    if (MODE == 1) {
-        A.sig[vi] = acc;
-        if (of) {
-            atomicOr(&A.ovf[g], 1u << t);
-            A.ctl->any_ovf = 1;
+__device__ __forceinline__ void fwd_store(const KArgs& A, int g, size_t gbase, int v, int a, uint64_t acc, bool of,
+                                          int we, double ws) {
+    const size_t vi = ((gbase + (size_t)v) << 5) + a;
+    if (MODE == 2) acc = wpack(ws, we, of);
+    A.sig[vi] = acc;
+    if (of) {
+        atomicOr(&A.ovf[g], 1u << a);
+        A.ctl->any_ovf = 1;
+    }
+}
+
+// Light entries, one per thread: the thread walks its entry's active lanes in
+// order and, for each, the neighbours in CSR order.  Threads step together so
+// that discoveries can be appended warp-wide after every step.
+template <int MODE, typename LT>
+__device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint32_t ent, unsigned am, long long r0,
+                                          long long r1, unsigned long long* cc_sh) {
+    constexpr LT INF = (LT)Lv<LT>::INF;
+    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+    const size_t gbase = (size_t)g * (size_t)A.n;
+    LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 5);
+    if (MODE == 0 && am) {
+        const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
+        for (unsigned r = am; r; r &= r - 1u) atomicAdd(&cc_sh[g * 32 + __ffs(r) - 1], (unsigned long long)c);
+    }
+    const int steps = __popc(am) * (int)(r1 - r0);
+    const int maxs = __reduce_max_sync(FULL, steps);
+    unsigned rem = am;
+    int a = 0;
+    long long j = r1;
+    uint64_t acc = 0;
+    bool of = false;
+    int we = WEMPTY;
+    double ws = 0.0;
+    for (int it = 0; it < maxs; it++) {
+        bool has = false, hub = false;
+        int x = 0;
+        if (it < steps) {
+            if (j == r1) {
+                a = __ffs(rem) - 1;
+                rem &= rem - 1u;
+                j = r0;
+                acc = 0;
+                of = false;
+                we = WEMPTY;
+                ws = 0.0;
+            }
+            x = A.col[j];
+            LT* px = lv + ((size_t)x << 5) + a;
+            const LT Lx = *px;
+            if (MODE != 0 && d > 0 && Lx == dprev) {
+                const uint64_t sv = A.sig[((gbase + (size_t)x) << 5) + a];
+                if (MODE == 1) {
+                    const uint64_t na = acc + sv;
+                    of |= (na < acc);
+                    acc = na;
+                } else {
+                    wadd(ws, we, sv);
+                }
+            }
+            if (Lx > dl) {
+                if (Lx == INF) *px = dnext;
+                has = claim(A, gbase, x, d + 1);
+                hub = has && is_hub(A, x);
+            }
+            if (++j == r1 && MODE != 0 && d > 0) fwd_store<MODE>(A, g, gbase, v, a, acc, of, we, ws);
         }
-    } else {
-        reinterpret_cast<double*>(A.sig)[vi] = lm + log2(ls);
+        warp_append(A, S, has, hub, ((uint32_t)x << 5) | (uint32_t)g);
     }
 }
 
 // Forward level kernel.  MODE 0: distances only (closeness sums per lane);
-// 1: exact uint64 sigma; 2: log2-domain sigma (FP64).
+// 1: exact uint64 sigma; 2: wide-exponent sigma.
 template <int MODE, typename LT>
-__global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
+__global__ void __launch_bounds__(BLOCK, (MINB<LT, MODE == 2>)) expand_kernel(KArgs A) {
     __shared__ unsigned long long cc_sh[MODE == 0 ? 32 * 32 : 1];
     __shared__ uint64_t h_acc[WARPS][32];
-    __shared__ double h_ls[WARPS][32];
+    __shared__ double h_ws[MODE == 2 ? WARPS : 1][32];
     __shared__ unsigned char h_of[WARPS][32];
+    __shared__ uint32_t stg[WARPS][STG];
     __shared__ unsigned long long s_i;
     if (MODE == 0) {
         for (int i = threadIdx.x; i < A.ng * 32; i += blockDim.x) cc_sh[i] = 0ULL;
@@ -499,6 +709,7 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
     const int done = *(volatile int*)&A.ctl->done;
     const int d = *(volatile int*)&A.ctl->level;
     const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    Stage S{stg[wib], 0};
     if (!done) {
         const LT dl = (LT)d;
         // hub entries: one CTA per entry, warps split the neighbours
@@ -522,11 +733,12 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
             }
             uint64_t acc = 0;
             bool of = false;
-            double lm = -INFINITY, ls = 0.0;
-            fwd_scan<MODE, LT>(A, d, g, gbase, lv, v, act, am, A.row[v], A.row[v + 1], wib, WARPS, acc, of, lm, ls);
+            int we = WEMPTY;
+            double ws = 0.0;
+            fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, v, am, A.row[v], A.row[v + 1], wib, WARPS, acc, of, we, ws);
             if (MODE != 0) {
                 if (MODE == 1) h_acc[wib][t] = acc;
-                else { h_acc[wib][t] = __double_as_longlong(lm); h_ls[wib][t] = ls; }
+                else { h_acc[wib][t] = (uint64_t)(long long)we; h_ws[wib][t] = ws; }
                 h_of[wib][t] = of;
                 __syncthreads();
                 if (wib == 0 && act && d > 0) {
@@ -536,42 +748,53 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
                             of = of || h_of[w][t] || (na < acc);
                             acc = na;
                         } else {
-                            lse_merge(lm, ls, __longlong_as_double(h_acc[w][t]), h_ls[w][t]);
+                            wmerge(ws, we, h_ws[w][t], (int)(long long)h_acc[w][t]);
                         }
                     }
-                    fwd_store<MODE>(A, g, gbase, v, acc, of, lm, ls);
+                    fwd_store<MODE>(A, g, gbase, v, t, acc, of, we, ws);
                 }
                 __syncthreads();
             }
         }
-        // regular entries: each warp fetches FETCH at a time
+        // regular entries: a warp takes FETCH per fetch; light ones are expanded
+        // one per thread, the others by the whole warp in turn
         const unsigned long long e = A.foff[d + 1];
         for (;;) {
             unsigned long long base = 0;
             if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
             base = __shfl_sync(FULL, base, 0);
             if (base >= e) break;
-            const unsigned long long lim = min(base + FETCH, e);
-            for (unsigned long long i = base; i < lim; i++) {
-                const uint32_t ent = A.fq[i];
-                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+            uint32_t ent;
+            unsigned am;
+            long long r0, r1;
+            fetch_entry<LT>(A, d, base + t, e, ent, am, r0, r1);
+            const bool light = am && (long long)__popc(am) * (r1 - r0) <= LIGHT;
+            fwd_light<MODE, LT>(A, S, d, ent, light ? am : 0u, r0, r1, cc_sh);
+            unsigned hv = __ballot_sync(FULL, am && !light);
+            while (hv) {
+                const int k = __ffs(hv) - 1;
+                hv &= hv - 1u;
+                const uint32_t ek = __shfl_sync(FULL, ent, k);
+                const unsigned amk = __shfl_sync(FULL, am, k);
+                const long long k0 = __shfl_sync(FULL, r0, k), k1 = __shfl_sync(FULL, r1, k);
+                const int v = (int)(ek >> 5), g = (int)(ek & 31u);
                 const size_t gbase = (size_t)g * (size_t)A.n;
                 LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 5);
-                const bool act = (lv[((size_t)v << 5) + t] == dl);
-                const unsigned am = __ballot_sync(FULL, act);
-                if (am == 0u) continue;
+                const bool act = (amk >> t) & 1u;
                 if (MODE == 0 && act) {
                     const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
                     atomicAdd(&cc_sh[g * 32 + t], (unsigned long long)c);
                 }
                 uint64_t acc = 0;
                 bool of = false;
-                double lm = -INFINITY, ls = 0.0;
-                fwd_scan<MODE, LT>(A, d, g, gbase, lv, v, act, am, A.row[v], A.row[v + 1], 0, 1, acc, of, lm, ls);
-                if (MODE != 0 && act && d > 0) fwd_store<MODE>(A, g, gbase, v, acc, of, lm, ls);
+                int we = WEMPTY;
+                double ws = 0.0;
+                fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, v, amk, k0, k1, 0, 1, acc, of, we, ws);
+                if (MODE != 0 && act && d > 0) fwd_store<MODE>(A, g, gbase, v, t, acc, of, we, ws);
             }
         }
     }
+    stage_flush(A, S);
     if (MODE == 0) {
         __syncthreads();
         for (int i = threadIdx.x; i < A.ng * 32; i += blockDim.x)
@@ -581,24 +804,24 @@ __global__ void __launch_bounds__(BLOCK) expand_kernel(KArgs A) {
 }
 
 // ---- dependency sweep -------------------------------------------------------
-// LOG: sigma held as log2 and rho as a(w) = log2(1 + delta(w)) - log2 sigma(w),
-// so that sigma(v)/sigma(w) * (1 + delta(w)) = exp2(log2 sigma(v) + a(w)).
-template <bool LOG, typename T, typename LT>
-__device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, int v, bool act,
-                                         unsigned am, double lsv, long long r0, long long r1, int sub, int nsub, T& acc,
-                                         int& pc) {
+// WIDE: sigma in wide form, rho(w) = (1 + delta(w)) / sigma(w) also in wide
+// form, and each successor term sigma(v)*rho(w) formed as a plain T.
+template <bool WIDE, typename T, typename LT>
+__device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, int v, unsigned am, T mv,
+                                         int ev, long long r0, long long r1, int sub, int nsub, T& acc, int& pc) {
     const int t = threadIdx.x & 31;
-    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const LT dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const T* rho = reinterpret_cast<const T*>(A.rho);
-    const double* rhod = reinterpret_cast<const double*>(A.rho);
+    const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
     if (__popc(am) > A.sparse) {
-        bwd_lanes<LOG, T, LT>(A, d, gbase, lv, v, lsv, r0, r1, sub, nsub, acc, pc);
+        bwd_lanes<WIDE, T, LT>(A, d, gbase, lv, v, mv, ev, r0, r1, sub, nsub, acc, pc);
     } else {
         unsigned rem = am;
         while (rem) {
             const int a = __ffs(rem) - 1;
             rem &= rem - 1u;
-            const double lsa = LOG ? __shfl_sync(FULL, lsv, a) : 0.0;
+            const T mva = WIDE ? __shfl_sync(FULL, mv, a) : T(0);
+            const int eva = WIDE ? __shfl_sync(FULL, ev, a) : 0;
             T pacc = T(0);
             int ppc = 0;
             for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
@@ -608,7 +831,7 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
                     const LT Lx = lv[((size_t)x << 5) + a];
                     if (Lx == dnext) {
                         const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                        if (LOG) pacc += (T)exp2(lsa + rhod[xi]);
+                        if (WIDE) pacc += wterm<T>(mva, eva, rw[xi]);
                         else pacc += rho[xi];
                     } else if (Lx == dprev) {
                         ppc++;
@@ -625,36 +848,80 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
     }
 }
 
-// delta, rho and the BC contribution of (v, lane t); warp-summed into bcg.
-template <bool LOG, typename T>
-__device__ __forceinline__ void bwd_finish(const KArgs& A, int g, size_t gbase, int v, bool act, double lsv, T acc,
+// delta and rho of (v, lane a) of group g from the successor sum; returns the
+// lane's BC contribution to v.
+template <bool WIDE, typename T>
+__device__ __forceinline__ double bwd_lane(const KArgs& A, int g, size_t gbase, int v, int a, T mv, int ev, T acc,
+                                           int pc, bool refsem) {
+    const size_t vi = ((gbase + (size_t)v) << 5) + a;
+    // with vertex weights (reach of folded vertices) a target v counts w[v]
+    // times and a source s contributes w[s] times
+    const T tw = A.w ? (T)A.w[v] : T(1);
+    T delta;
+    if (WIDE) {
+        delta = acc;
+        bool of = false;
+        reinterpret_cast<uint64_t*>(A.rho)[vi] = wpack((T)((tw + delta) / mv), -ev, of);
+    } else {
+        const T sv = (T)A.sig[vi];
+        delta = sv * acc;
+        reinterpret_cast<T*>(A.rho)[vi] = (tw + delta) / sv;
+    }
+    return (double)delta * (double)A.srcw[(g << 5) + a] * (refsem ? (double)pc : 1.0);
+}
+
+// Lane t of (v, g), warp-summed into bcg.
+template <bool WIDE, typename T>
+__device__ __forceinline__ void bwd_finish(const KArgs& A, int g, size_t gbase, int v, bool act, T mv, int ev, T acc,
                                            int pc, bool refsem) {
     const int t = threadIdx.x & 31;
-    const size_t vi = ((gbase + (size_t)v) << 5) + t;
-    double contrib = 0.0;
-    if (act) {
-        // with vertex weights (reach of folded vertices) a target v counts w[v]
-        // times and a source s contributes w[s] times
-        const T tw = A.w ? (T)A.w[v] : T(1);
-        const int lane = (g << 5) + t;
-        T delta;
-        if (LOG) {
-            delta = acc;
-            reinterpret_cast<double*>(A.rho)[vi] = log2((double)tw + (double)delta) - lsv;
-        } else {
-            const T sv = (T)A.sig[vi];
-            delta = sv * acc;
-            reinterpret_cast<T*>(A.rho)[vi] = (tw + delta) / sv;
-        }
-        contrib = (double)delta * (double)A.srcw[lane] * (refsem ? (double)pc : 1.0);
-    }
+    double contrib = act ? bwd_lane<WIDE, T>(A, g, gbase, v, t, mv, ev, acc, pc, refsem) : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(FULL, contrib, o);
     if (t == 0) A.bcg[gbase + v] += contrib;
 }
 
-template <bool LOG, typename T, typename LT>
-__global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
+// Light entries, one per thread: lanes in order, neighbours in CSR order.
+template <bool WIDE, typename T, typename LT>
+__device__ __forceinline__ void bwd_light(const KArgs& A, int d, uint32_t ent, unsigned am, long long r0, long long r1,
+                                          bool refsem) {
+    if (!am) return;
+    const LT dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+    const size_t gbase = (size_t)g * (size_t)A.n;
+    const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 5);
+    const T* rho = reinterpret_cast<const T*>(A.rho);
+    const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
+    double contrib = 0.0;
+    for (unsigned rem = am; rem; rem &= rem - 1u) {
+        const int a = __ffs(rem) - 1;
+        T mv = T(0);
+        int ev = 0;
+        if (WIDE) {
+            const uint64_t sw = A.sig[((gbase + (size_t)v) << 5) + a];
+            mv = wmant<T>(sw);
+            ev = wexp(sw);
+        }
+        T acc = T(0);
+        int pc = 0;
+        for (long long j = r0; j < r1; j++) {
+            const int x = A.col[j];
+            const LT Lx = lv[((size_t)x << 5) + a];
+            if (Lx == dnext) {
+                const size_t xi = ((gbase + (size_t)x) << 5) + a;
+                if (WIDE) acc += wterm<T>(mv, ev, rw[xi]);
+                else acc += rho[xi];
+            } else if (Lx == dprev) {
+                pc++;
+            }
+        }
+        contrib += bwd_lane<WIDE, T>(A, g, gbase, v, a, mv, ev, acc, pc, refsem);
+    }
+    A.bcg[gbase + v] += contrib;
+}
+
+template <bool WIDE, typename T, typename LT>
+__global__ void __launch_bounds__(BLOCK, (MINB<LT, WIDE>)) backward_kernel(KArgs A) {
     __shared__ double h_acc[WARPS][32];
     __shared__ int h_pc[WARPS][32];
     __shared__ unsigned long long s_i;
@@ -663,7 +930,6 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
     const bool refsem = (A.semantics == GBC_BC_REFERENCE);
     if (d >= 1) {
         const LT dl = (LT)d;
-        const double* sigd = reinterpret_cast<const double*>(A.sig);
         const unsigned long long he = A.hoff[d + 1];
         for (;;) {
             if (threadIdx.x == 0) s_i = atomicAdd(&A.ctl->hnext, 1ULL);
@@ -678,10 +944,12 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
             const bool act = (lv[((size_t)v << 5) + t] == dl);
             const unsigned am = __ballot_sync(FULL, act);
             if (am == 0u) continue;
-            const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
+            const uint64_t sw = (WIDE && act) ? A.sig[((gbase + (size_t)v) << 5) + t] : 0ULL;
+            const T mv = (WIDE && act) ? wmant<T>(sw) : T(0);
+            const int ev = (WIDE && act) ? wexp(sw) : 0;
             T acc = T(0);
             int pc = 0;
-            bwd_scan<LOG, T, LT>(A, d, gbase, lv, v, act, am, lsv, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+            bwd_scan<WIDE, T, LT>(A, d, gbase, lv, v, am, mv, ev, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
             h_acc[wib][t] = (double)acc;
             h_pc[wib][t] = pc;
             __syncthreads();
@@ -690,7 +958,7 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
                     acc += (T)h_acc[w][t];
                     pc += h_pc[w][t];
                 }
-                bwd_finish<LOG, T>(A, g, gbase, v, act, lsv, acc, pc, refsem);
+                bwd_finish<WIDE, T>(A, g, gbase, v, act, mv, ev, acc, pc, refsem);
             }
             __syncthreads();
         }
@@ -700,20 +968,30 @@ __global__ void __launch_bounds__(BLOCK) backward_kernel(KArgs A) {
             if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
             base = __shfl_sync(FULL, base, 0);
             if (base >= e) break;
-            const unsigned long long lim = min(base + FETCH, e);
-            for (unsigned long long i = base; i < lim; i++) {
-                const uint32_t ent = A.fq[i];
-                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+            uint32_t ent;
+            unsigned am;
+            long long r0, r1;
+            fetch_entry<LT>(A, d, base + t, e, ent, am, r0, r1);
+            const bool light = am && (long long)__popc(am) * (r1 - r0) <= LIGHT;
+            bwd_light<WIDE, T, LT>(A, d, ent, light ? am : 0u, r0, r1, refsem);
+            unsigned hv = __ballot_sync(FULL, am && !light);
+            while (hv) {
+                const int k = __ffs(hv) - 1;
+                hv &= hv - 1u;
+                const uint32_t ek = __shfl_sync(FULL, ent, k);
+                const unsigned amk = __shfl_sync(FULL, am, k);
+                const long long k0 = __shfl_sync(FULL, r0, k), k1 = __shfl_sync(FULL, r1, k);
+                const int v = (int)(ek >> 5), g = (int)(ek & 31u);
                 const size_t gbase = (size_t)g * (size_t)A.n;
                 const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 5);
-                const bool act = (lv[((size_t)v << 5) + t] == dl);
-                const unsigned am = __ballot_sync(FULL, act);
-                if (am == 0u) continue;
-                const double lsv = (LOG && act) ? sigd[((gbase + (size_t)v) << 5) + t] : 0.0;
+                const bool act = (amk >> t) & 1u;
+                const uint64_t sw = (WIDE && act) ? A.sig[((gbase + (size_t)v) << 5) + t] : 0ULL;
+                const T mv = (WIDE && act) ? wmant<T>(sw) : T(0);
+                const int ev = (WIDE && act) ? wexp(sw) : 0;
                 T acc = T(0);
                 int pc = 0;
-                bwd_scan<LOG, T, LT>(A, d, gbase, lv, v, act, am, lsv, A.row[v], A.row[v + 1], 0, 1, acc, pc);
-                bwd_finish<LOG, T>(A, g, gbase, v, act, lsv, acc, pc, refsem);
+                bwd_scan<WIDE, T, LT>(A, d, gbase, lv, v, amk, mv, ev, k0, k1, 0, 1, acc, pc);
+                bwd_finish<WIDE, T>(A, g, gbase, v, act, mv, ev, acc, pc, refsem);
             }
         }
     }
@@ -744,7 +1022,7 @@ __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, in
             if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[i] = 0;
             else reinterpret_cast<uint16_t*>(A.lvl)[i] = 0;
             if (mode == 1) A.sig[i] = 1ULL;
-            else if (mode == 2) reinterpret_cast<double*>(A.sig)[i] = 0.0;
+            else if (mode == 2) A.sig[i] = WONE;
             A.srcw[l] = A.w ? A.w[s] : 1;
             if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
                 const uint32_t ent = ((uint32_t)s << 5) | (uint32_t)g;
@@ -974,45 +1252,49 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
     GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
     bytes_ = cells * 2 + (size_t)ng_ * n * 4 + (fcap_ + hcap_) * 4 + (need_bc ? cells * 16 + (size_t)ng_ * n * 8 : 0);
-    // grid: enough resident CTAs to fill every SM
-    int occ = 0;
-    GBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, expand_kernel<1, uint8_t>, BLOCK, 0));
-    grid_ = sm_count_ * std::max(1, std::min(occ, 8));
     return GBC_OK;
 }
 
 
-// Graph keys: 0..2 expand MODE; 3 + (log*2 + f64)*2 + refsem: backward.
+// Graph keys: 0..2 expand MODE; 3 + (wide*2 + f64)*2 + refsem: backward; +100 with 16-bit levels.
 gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     for (auto& c : graphs_) if (c.key == key) { *out = c.exec; return GBC_OK; }
     KArgs A = LaneAccess::args(*this, (key % 100) >= 3 ? ((((key % 100) - 3) & 1) ? GBC_BC_REFERENCE : GBC_BC_BRANDES)
                                                        : GBC_BC_BRANDES);
+    void (*fn)(KArgs) = nullptr;
+    {
+        const bool lv16 = key >= 100;
+        const int k = key % 100;
+        switch (k) {
+            case 0: fn = lv16 ? expand_kernel<0, uint16_t> : expand_kernel<0, uint8_t>; break;
+            case 1: fn = lv16 ? expand_kernel<1, uint16_t> : expand_kernel<1, uint8_t>; break;
+            case 2: fn = lv16 ? expand_kernel<2, uint16_t> : expand_kernel<2, uint8_t>; break;
+            default: {
+                const int v = (k - 3) >> 1;  // wide sigma * 2 + f64
+                if (lv16) {
+                    if (v == 0) fn = backward_kernel<false, float, uint16_t>;
+                    else if (v == 1) fn = backward_kernel<false, double, uint16_t>;
+                    else if (v == 2) fn = backward_kernel<true, float, uint16_t>;
+                    else fn = backward_kernel<true, double, uint16_t>;
+                } else {
+                    if (v == 0) fn = backward_kernel<false, float, uint8_t>;
+                    else if (v == 1) fn = backward_kernel<false, double, uint8_t>;
+                    else if (v == 2) fn = backward_kernel<true, float, uint8_t>;
+                    else fn = backward_kernel<true, double, uint8_t>;
+                }
+            }
+        }
+    }
+    // one wave: as many CTAs as fit on every SM at once
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, BLOCK, 0) != cudaSuccess) { cudaGetLastError(); occ = 1; }
+    const int grid = sm_count_ * std::max(1, std::min(occ, 8));
     cudaStream_t cs;
     GBC_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     for (int i = 0; i < lpg_ && e == cudaSuccess; i++) {
-        const bool wide = key >= 100;
-        const int k = key % 100;
-        switch (k) {
-            case 0: if (wide) expand_kernel<0, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<0, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
-            case 1: if (wide) expand_kernel<1, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<1, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
-            case 2: if (wide) expand_kernel<2, uint16_t><<<grid_, BLOCK, 0, cs>>>(A); else expand_kernel<2, uint8_t><<<grid_, BLOCK, 0, cs>>>(A); break;
-            default: {
-                const int v = (k - 3) >> 1;  // log*2 + f64
-                if (wide) {
-                    if (v == 0) backward_kernel<false, float, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else if (v == 1) backward_kernel<false, double, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else if (v == 2) backward_kernel<true, float, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else backward_kernel<true, double, uint16_t><<<grid_, BLOCK, 0, cs>>>(A);
-                } else {
-                    if (v == 0) backward_kernel<false, float, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else if (v == 1) backward_kernel<false, double, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else if (v == 2) backward_kernel<true, float, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
-                    else backward_kernel<true, double, uint8_t><<<grid_, BLOCK, 0, cs>>>(A);
-                }
-            }
-        }
+        fn<<<grid, BLOCK, 0, cs>>>(A);
         e = cudaGetLastError();
     }
     cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
@@ -1055,18 +1337,18 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
     if (rq.kb < 1 || rq.kb > lanes_) { set_error("batch of %d sources for %d lanes", rq.kb, lanes_); return GBC_ERR_ARG; }
     const bool bc = rq.job != LaneJob::CC;
     if (bc && !need_bc_) { set_error("engine was initialised without BC state"); return GBC_ERR_ARG; }
-    const int mode = rq.job == LaneJob::CC ? 0 : (rq.sigma_log ? 2 : 1);
+    const int mode = rq.job == LaneJob::CC ? 0 : (rq.sigma_wide ? 2 : 1);
     for (int attempt = 0; attempt < 4; attempt++) {
         KArgs A = LaneAccess::args(*this, rq.semantics);
         GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
         if (mode == 0) GBC_CUDA(cudaMemsetAsync(ccbuf_, 0, lanes_ * sizeof(unsigned long long), stream_));
-        if (mode == 1) GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
+        if (mode != 0) GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
         seed_kernel<<<1, 1024, 0, stream_>>>(A, rq.d_src, rq.kb, mode, lvl_bytes_);
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches += 1;
         cudaGraphExec_t fwd;
-        const int wide = (lvl_bytes_ == 2) ? 100 : 0;
-        GBC_TRY(get_graph(wide + mode, &fwd));
+        const int lv16 = (lvl_bytes_ == 2) ? 100 : 0;
+        GBC_TRY(get_graph(lv16 + mode, &fwd));
         Ctl* h = (Ctl*)ctl_host_;
         int64_t launched = 0;
         GBC_TRY(ensure_events(2));
@@ -1084,7 +1366,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
             res.fwd_ms += ms;
             if (h->done) break;
-            if (h->any_ovf && rq.abort_on_overflow) break;   // the batch is redone in log form anyway
+            if (h->any_ovf && rq.abort_on_overflow) break;   // the batch is redone in wide form anyway
             if (launched > (int64_t)MAX_LEVEL + 2 * lpg_) { set_error("forward level loop did not terminate"); return GBC_ERR_LIMIT; }
         }
         const int maxlevel = h->maxlevel;
@@ -1141,9 +1423,21 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
                 set_error("exact path counts overflowed uint64 in %d lanes", cnt);
                 return GBC_ERR_OVERFLOW;
             }
+        } else if (mode == 2) {
+            uint32_t bits[32] = {};
+            GBC_CUDA(cudaMemcpyAsync(bits, ovf_, ng_ * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+            GBC_CUDA(cudaStreamSynchronize(stream_));
+            int cnt = 0;
+            for (int i = 0; i < ng_; i++) cnt += __builtin_popcount(bits[i]);
+            if (cnt) {
+                cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
+                GBC_CUDA(cudaGetLastError());
+                set_error("path counts exceed 2^524287 in %d lanes", cnt);
+                return GBC_ERR_OVERFLOW;
+            }
         }
         if (rq.job == LaneJob::BC && maxlevel >= 1) {
-            const int key = wide + 3 + ((rq.sigma_log ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
+            const int key = lv16 + 3 + ((rq.sigma_wide ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
                             (rq.semantics == GBC_BC_REFERENCE ? 1 : 0);
             cudaGraphExec_t bwd;
             GBC_TRY(get_graph(key, &bwd));

@@ -500,6 +500,7 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
     GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, R.stream));
     GBC_TRY(R.ceng->bc_begin());
     LaneResult res;
+    bool wide = o.sigma_mode == GBC_SIGMA_WIDE;   // AUTO: later batches start wide after an overflow
     for (int32_t b0 = 0; b0 < nc; b0 += lanes) {
         LaneRequest rq;
         rq.job = LaneJob::BC;
@@ -507,11 +508,12 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
         rq.kb = std::min(lanes, nc - b0);
         rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
         rq.semantics = GBC_BC_BRANDES;
-        rq.sigma_log = o.sigma_mode == GBC_SIGMA_LOG;
-        rq.abort_on_overflow = !rq.sigma_log;
+        rq.sigma_wide = wide;
+        rq.abort_on_overflow = !rq.sigma_wide;
         gbc_status st = R.ceng->run(rq, res);
-        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO) {
-            rq.sigma_log = 1;
+        if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO && !wide) {
+            wide = true;
+            rq.sigma_wide = 1;
             rq.abort_on_overflow = false;
             st = R.ceng->run(rq, res);
         }

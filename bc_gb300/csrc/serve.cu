@@ -260,7 +260,7 @@ void gbc_server_s::run() {
             rq.abort_on_overflow = true;
             if (st == GBC_OK) st = G.eng->run(rq, res);
             if (st == GBC_ERR_OVERFLOW) {
-                rq.sigma_log = 1;
+                rq.sigma_wide = 1;
                 rq.abort_on_overflow = false;
                 st = G.eng->run(rq, res);
             }

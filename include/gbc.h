@@ -53,9 +53,9 @@ enum {
 enum { GBC_DELTA_F32 = 0, GBC_DELTA_F64 = 1 };
 /* Path-count (sigma) representation. */
 enum {
-    GBC_SIGMA_AUTO = 0,     /* exact uint64; on overflow re-run the batch in LOG form */
+    GBC_SIGMA_AUTO = 0,     /* exact uint64; on overflow re-run the batch in WIDE form */
     GBC_SIGMA_EXACT = 1,    /* exact uint64; overflow is an error (GBC_ERR_OVERFLOW) */
-    GBC_SIGMA_LOG = 2       /* log2(sigma) in FP64: any magnitude, ~1e-13 relative */
+    GBC_SIGMA_WIDE = 2      /* 44-bit mantissa, 20-bit exponent: up to 2^524287, ~6e-14 relative */
 };
 /* Engine. */
 enum {
@@ -90,7 +90,7 @@ typedef struct {
     double  kernel_ms;        /* device time of the traversal kernels (CUDA events) */
     double  total_ms;         /* wall time of the call */
     int32_t lanes;            /* lanes per batch actually used */
-    int32_t sigma_mode_used;  /* GBC_SIGMA_EXACT or GBC_SIGMA_LOG */
+    int32_t sigma_mode_used;  /* GBC_SIGMA_EXACT or GBC_SIGMA_WIDE */
     double  fwd_ms;           /* device time of the forward (BFS / path count) level kernels */
     double  bwd_ms;           /* device time of the dependency-sweep level kernels */
     int64_t fwd_kernels;      /* forward level kernels launched (incl. no-op tail launches) */

@@ -12,7 +12,7 @@
  *   - computeBC starts at csr->startNodeID (the reference starts at a global
  *     nextBFS = 0, which reads csrE[-1] for 1-based graphs; Brandes.c:24,249).
  *   - Betweenness is computed in FP64 and added to the caller's float array;
- *     path counts are exact (uint64, or log2 form when they overflow) instead
+ *     path counts are exact (uint64, or a wide-exponent float when they overflow) instead
  *     of FP32 (Brandes.c:226).
  *   - computeCC returns the CCs pointer (the reference returns a freed
  *     buffer, CC.cpp:113-116).

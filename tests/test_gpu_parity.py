@@ -152,9 +152,9 @@ def test_sigma_overflow_log_mode(gpu, orc):
     with gpu.Graph(csr) as G:
         with pytest.raises(gpu.GbcError):
             G.bc(src, sigma_mode=gpu.SIGMA_EXACT)
-        got = G.bc(src)   # AUTO: exact, then log2 form for overflowing batches
+        got = G.bc(src)   # AUTO: exact, then wide form for overflowing batches
         st = G.stats()
-        assert st["sigma_mode_used"] == gpu.SIGMA_LOG
+        assert st["sigma_mode_used"] == gpu.SIGMA_WIDE
         assert relerr(got, ref) < TOL_F64
         dist, sig, ovf = G.sssp(src)
         assert ovf.all()
