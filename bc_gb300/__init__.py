@@ -62,7 +62,7 @@ class ReducedInfo(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_lanes", C.c_int32), ("max_inflight", C.c_int32),
-                ("reserved", C.c_int32 * 8)]
+                ("workers", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")

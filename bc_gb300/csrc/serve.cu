@@ -2,14 +2,17 @@
 // graphs (the query loop the reference does not have; its drivers run one
 // computation per process, Seq_CC/CC.cpp:2687, parallel_CC/para_CC.cu:383).
 //
-// One worker thread owns the device work.  Each registered graph keeps its
-// CSR in HBM and, while it has work, one lane engine.  A lane batch is filled
-// from every admitted request on one graph that wants the same kind of sweep
-// (closeness or betweenness), oldest first; a request takes whole 32-lane
-// groups, so its betweenness partials stay separate and are added into its
-// own FP64 result vector after each batch.  Requests that arrive while a
-// batch runs join the next batch.  Engines are created under an HBM budget
-// and idle ones are released when a new graph needs room.
+// A few worker threads run lane batches; each graph is worked on by at most
+// one of them at a time, on the graph's own stream, so batches of different
+// graphs overlap on the device and in the host gaps between level-loop
+// launches.  Each registered graph keeps its CSR in HBM and, while it has
+// work, one lane engine.  A lane batch is filled from every admitted request
+// on one graph that wants the same kind of sweep (closeness or betweenness),
+// oldest first; a request takes whole 32-lane groups, so its betweenness
+// partials stay separate and are added into its own FP64 result vector after
+// each batch.  Requests that arrive while a batch runs join the next batch.
+// Engines are created under an HBM budget and idle ones are released when a
+// new graph needs room.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,12 +41,15 @@ struct SGraph {
     int32_t lanes = 0;
     int32_t* d_src = nullptr;
     double** d_dst = nullptr;    // device table: lane group -> destination result vector
+    cudaStream_t stream = nullptr;
+    bool running = false;        // a worker holds this graph (its engine, buffers and stream)
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
         cudaFree(g.col);
         cudaFree(d_src);
         cudaFree(d_dst);
+        if (stream) cudaStreamDestroy(stream);
     }
 };
 
@@ -74,7 +80,7 @@ struct gbc_server_s {
     size_t budget = 0;
     int32_t max_lanes = 1024;
     int32_t max_inflight = 64;
-    cudaStream_t stream = nullptr;
+    int32_t nworkers = 4;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::vector<std::unique_ptr<SGraph>> graphs;
@@ -82,11 +88,12 @@ struct gbc_server_s {
     std::deque<int64_t> fifo;    // admitted or queued requests in arrival order
     int64_t next_id = 1;
     bool stop = false;
-    std::thread worker;
+    std::vector<std::thread> workers;
     int32_t rr = 0;              // round-robin position over graphs
-    // counters
+    // counters; busy_ms is the time during which at least one batch ran
     int64_t completed = 0, batches = 0, shared_batches = 0, edges = 0;
-    double busy_ms = 0;
+    double busy_ms = 0, busy_t0 = 0;
+    int32_t active = 0;
 
     void run();
     size_t engines_bytes() const {
@@ -104,7 +111,8 @@ struct gbc_server_s {
 
 namespace {
 
-// Engine for graph gi, making room under the budget by releasing idle engines.
+// Engine for graph gi, making room under the budget by releasing the engines
+// of graphs that neither have pending work nor are held by a worker.
 gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy) {
     SGraph& G = *S->graphs[gi];
     if (G.eng) return GBC_OK;
@@ -124,7 +132,7 @@ gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& g
         lanes = std::max(32, lanes / 2);
     }
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, S->stream));
+    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream));
     if (G.lanes != lanes) {
         cudaFree(G.d_src);
         cudaFree(G.d_dst);
@@ -180,7 +188,7 @@ void gbc_server_s::run() {
                     Req* r = reqs[id].get();
                     if (!r->admitted && inflight < max_inflight) { r->admitted = true; r->state = GBC_REQ_RUNNING; inflight++; }
                 }
-                // pick a graph with pending sources, round robin
+                // pick a graph with pending sources that no other worker holds, round robin
                 std::vector<bool> busy(graphs.size(), false);
                 for (int64_t id : fifo) {
                     Req* r = reqs[id].get();
@@ -188,10 +196,11 @@ void gbc_server_s::run() {
                 }
                 for (size_t k = 0; k < graphs.size(); k++) {
                     const int32_t cand = (int32_t)((rr + k) % graphs.size());
-                    if (busy[cand]) { gi = cand; break; }
+                    if (busy[cand] && !graphs[cand]->running) { gi = cand; break; }
                 }
                 if (gi < 0) { cv_work.wait_for(lk, std::chrono::milliseconds(50)); continue; }
                 rr = gi + 1;
+                for (size_t j = 0; j < graphs.size(); j++) busy[j] = busy[j] || graphs[j]->running;
                 gbc_status st = ensure_engine(this, gi, busy);
                 if (st != GBC_OK) {
                     for (int64_t id : fifo) {
@@ -222,11 +231,14 @@ void gbc_server_s::run() {
                     used += ((take + 31) / 32) * 32;
                 }
                 Gp = graphs[gi].get();
+                Gp->running = true;
+                if (active++ == 0) busy_t0 = now_ms();
                 break;
             }
         }
         // device work outside the lock
         SGraph& G = *Gp;
+        cudaStream_t stream = G.stream;
         const int32_t ng = lanes / 32;
         hsrc.assign(lanes, -1);
         hdst.assign(ng, nullptr);
@@ -237,7 +249,6 @@ void gbc_server_s::run() {
             for (int32_t gg = sl.lane0 / 32; gg < (sl.lane0 + sl.count + 31) / 32; gg++) hdst[gg] = sl.r->d_bc;
             kb = std::max(kb, ((sl.lane0 + sl.count + 31) / 32) * 32);
         }
-        const double t0 = now_ms();
         gbc_status st = GBC_OK;
         if (cudaMemcpyAsync(G.d_src, hsrc.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
             cudaGetLastError();
@@ -275,10 +286,10 @@ void gbc_server_s::run() {
             hcc.assign(kb, 0);
             if (st == GBC_OK) st = G.eng->cc_read(hcc.data(), kb);
         }
-        const double t1 = now_ms();
         {
             std::lock_guard<std::mutex> lk(mu);
-            busy_ms += t1 - t0;
+            G.running = false;
+            if (--active == 0) busy_ms += now_ms() - busy_t0;
             batches++;
             if (slots.size() > 1) shared_batches++;
             for (auto& sl : slots) {
@@ -300,6 +311,7 @@ void gbc_server_s::run() {
             }
         }
         cv_done.notify_all();
+        cv_work.notify_all();
     }
 }
 
@@ -318,12 +330,13 @@ gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out) {
     }
     S->max_lanes = S->cfg.max_lanes ? S->cfg.max_lanes : 1024;
     S->max_inflight = S->cfg.max_inflight > 0 ? S->cfg.max_inflight : 64;
+    if (S->cfg.workers < 0 || S->cfg.workers > 16) { set_error("workers must be in [0,16]"); return GBC_ERR_ARG; }
+    S->nworkers = S->cfg.workers ? S->cfg.workers : 4;
     size_t fr = 0, tot = 0;
     GBC_CUDA(cudaMemGetInfo(&fr, &tot));
     S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : fr / 2;
-    GBC_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     gbc_server_s* raw = S.get();
-    S->worker = std::thread([raw] { raw->run(); });
+    for (int32_t w = 0; w < S->nworkers; w++) S->workers.emplace_back([raw] { raw->run(); });
     *out = S.release();
     return GBC_OK;
 }
@@ -335,10 +348,10 @@ gbc_status gbc_server_destroy(gbc_server s) {
         s->stop = true;
     }
     s->cv_work.notify_all();
-    if (s->worker.joinable()) s->worker.join();
+    for (auto& w : s->workers)
+        if (w.joinable()) w.join();
     s->reqs.clear();
     s->graphs.clear();
-    if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return GBC_OK;
 }
@@ -349,6 +362,7 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     auto G = std::make_unique<SGraph>();
     G->g.n = n;
     G->g.m = row[n];
+    GBC_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
     if (cudaMalloc(&G->g.row, sizeof(int64_t) * (n + 1)) != cudaSuccess ||
         cudaMalloc(&G->g.col, sizeof(int32_t) * std::max<int64_t>(row[n], 1)) != cudaSuccess) {
         cudaGetLastError();
@@ -512,7 +526,7 @@ gbc_status gbc_server_counters(gbc_server s, int64_t* completed, int64_t* batche
     if (batches) *batches = s->batches;
     if (shared) *shared = s->shared_batches;
     if (edges) *edges = s->edges;
-    if (busy_ms) *busy_ms = s->busy_ms;
+    if (busy_ms) *busy_ms = s->busy_ms + (s->active ? now_ms() - s->busy_t0 : 0.0);
     return GBC_OK;
 }
 

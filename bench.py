@@ -57,8 +57,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--serve-seconds", type=float, default=8.0)
-    p.add_argument("--serve-rate", type=float, default=40.0, help="query arrivals per second")
+    p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
+    p.add_argument("--serve-rates", default="10,20,40,80", help="query arrival rates per second, comma-separated")
     p.add_argument("--no-serve", action="store_true")
     return p.parse_args()
 
@@ -176,11 +176,12 @@ def cpu_baseline(csr, sample, n_src, threads):
     return dt
 
 
-def serving(G, seconds, rate, seed=11):
-    """Poisson stream of queries over device-resident graphs (a scaled-down
+def serving(G, seconds, rates, seed=11):
+    """Poisson streams of queries over device-resident graphs (a scaled-down
     version of the 64-graph serving mix): exact CC on the small graphs,
-    k = 64 / 1024 sampled BC everywhere.  Returns p50/p99 latency and the
-    GTEPS the server delivered over the stream."""
+    k = 64 / 1024 sampled BC everywhere.  One stream per arrival rate, on the
+    same server; per rate the p50/p99 latency and the GTEPS delivered over
+    the stream's wall time (first arrival to last completion)."""
     import ctypes as C
     import random
     L = G.lib()
@@ -199,41 +200,56 @@ def serving(G, seconds, rate, seed=11):
         gids.append(gid.value)
     rng = random.Random(seed)
     o = G.options()
-    reqs = []
-    t_end = time.perf_counter() + seconds
-    while time.perf_counter() < t_end:
-        gi = rng.randrange(len(specs))
-        n = specs[gi][1].n
-        r = rng.random()
-        if r < 0.25 and n <= 32768:
-            kind, k = G.Q_CC, 0
-        elif r < 0.7:
-            kind, k = G.Q_BC_SAMPLED, 64
-        else:
-            kind, k = G.Q_BC_SAMPLED, 1024
-        rid = C.c_int64()
-        G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
-        reqs.append((rid.value, gi))
-        time.sleep(rng.expovariate(rate))
-    lats = []
-    for rid, gi in reqs:
-        st = C.c_int32()
-        G.check(L.gbc_server_wait(h, rid, 600000.0, C.byref(st)))
-        n = specs[gi][1].n
-        bc = np.zeros(n)
-        cc = np.zeros(n, np.int64)
-        lat = C.c_double()
-        G.check(L.gbc_server_fetch(h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
-                                   C.byref(lat)))
-        lats.append(lat.value)
-    v = [C.c_int64() for _ in range(4)] + [C.c_double()]
-    G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
+
+    def counters():
+        v = [C.c_int64() for _ in range(4)] + [C.c_double()]
+        G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
+        return [x.value for x in v]
+
+    def stream(rate):
+        reqs = []
+        c0 = counters()
+        t0 = time.perf_counter()
+        t_end = t0 + seconds
+        while time.perf_counter() < t_end:
+            gi = rng.randrange(len(specs))
+            n = specs[gi][1].n
+            r = rng.random()
+            if r < 0.25 and n <= 32768:
+                kind, k = G.Q_CC, 0
+            elif r < 0.7:
+                kind, k = G.Q_BC_SAMPLED, 64
+            else:
+                kind, k = G.Q_BC_SAMPLED, 1024
+            rid = C.c_int64()
+            G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
+            reqs.append((rid.value, gi))
+            time.sleep(rng.expovariate(rate))
+        lats = []
+        for rid, gi in reqs:
+            st = C.c_int32()
+            G.check(L.gbc_server_wait(h, rid, 600000.0, C.byref(st)))
+            n = specs[gi][1].n
+            bc = np.zeros(n)
+            cc = np.zeros(n, np.int64)
+            lat = C.c_double()
+            G.check(L.gbc_server_fetch(h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                                       C.byref(lat)))
+            lats.append(lat.value)
+        wall = time.perf_counter() - t0
+        c1 = counters()
+        lats = np.array(lats)
+        busy = c1[4] - c0[4]
+        return {"rate_per_s": rate, "queries": len(lats), "p50_ms": round(float(np.percentile(lats, 50)), 3),
+                "p99_ms": round(float(np.percentile(lats, 99)), 3), "wall_s": round(wall, 3),
+                "lane_batches": c1[1] - c0[1], "shared_batches": c1[2] - c0[2],
+                "gteps_delivered": round((c1[3] - c0[3]) / wall / 1e9, 3),
+                "busy_frac": round(busy * 1e-3 / wall, 3)}
+
+    points = [stream(r) for r in rates]
     L.gbc_server_destroy(h)
-    lats = np.array(lats)
-    return {"queries": len(lats), "p50_ms": round(float(np.percentile(lats, 50)), 3),
-            "p99_ms": round(float(np.percentile(lats, 99)), 3), "rate_per_s": rate, "graphs": len(specs),
-            "lane_batches": v[1].value, "shared_batches": v[2].value,
-            "gteps_busy": round(v[3].value / (v[4].value * 1e-3) / 1e9, 3) if v[4].value > 0 else None}
+    return {"graphs": len(specs), "workers": 4, "points": points,
+            "mix": "25% exact CC (graphs <= 32K vertices), 45% k=64 and 30% k=1024 sampled BC, uniform over graphs"}
 
 
 def run_reference(args):
@@ -433,7 +449,7 @@ def main():
                    "sample": f"first {n_cpu} of the {args.k} sampled sources, reference semantics, FP64"}
         serve = None
         if not args.no_serve:
-            serve = serving(G, args.serve_seconds, args.serve_rate)
+            serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")])
         out = {"metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",

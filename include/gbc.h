@@ -222,7 +222,7 @@ gbc_status gbc_read_edgelist(const char* path, int64_t** row, int32_t** col, int
 void gbc_free(void* p);
 
 /* ---- serving: continuous batching over device-resident graphs ---------
- * A server owns a set of registered graphs and a worker thread.  Requests
+ * A server owns a set of registered graphs and worker threads.  Requests
  * (exact CC, exact BC, or k-source sampled BC) are admitted while their lane
  * state fits the HBM budget; sources of concurrent requests on the same graph
  * share lane batches.  Results are identical (FP64 tolerance) alone and
@@ -235,7 +235,8 @@ typedef struct {
     size_t  hbm_budget_bytes;   /* lane-state budget; 0 = 50% of free device memory */
     int32_t max_lanes;          /* lanes per shared batch (multiple of 32), 0 = 1024 */
     int32_t max_inflight;       /* requests admitted at once, 0 = 64 */
-    int32_t reserved[8];
+    int32_t workers;            /* lane batches in flight at once, on different graphs; 0 = 4 */
+    int32_t reserved[7];
 } gbc_server_config;
 
 gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out);

@@ -15,13 +15,14 @@ TOL = 1e-9
 
 
 class Server:
-    def __init__(self, gbc, budget=0, max_lanes=0, max_inflight=0):
+    def __init__(self, gbc, budget=0, max_lanes=0, max_inflight=0, workers=0):
         self.g = gbc
         self.L = gbc.lib()
         cfg = gbc.ServerConfig()
         cfg.hbm_budget_bytes = budget
         cfg.max_lanes = max_lanes
         cfg.max_inflight = max_inflight
+        cfg.workers = workers
         self.h = C.c_void_p()
         gbc.check(self.L.gbc_server_create(C.byref(cfg), C.byref(self.h)))
         self.n = {}
@@ -176,3 +177,31 @@ def test_admission_under_small_budget(gpu, orc, graphs):
         og = orc.Graph(csr.row, csr.col)
         assert np.array_equal(cc, orc.cc(og, np.arange(csr.n)))
     S.close()
+
+
+def test_worker_count(gpu, orc, graphs):
+    """One worker and eight workers give the same results on the same
+    stream; out-of-range worker counts are rejected."""
+    cfg = gpu.ServerConfig()
+    cfg.workers = 17
+    h = C.c_void_p()
+    assert gpu.lib().gbc_server_create(C.byref(cfg), C.byref(h)) == 1   # GBC_ERR_ARG
+    out = {}
+    for w in (1, 8):
+        S = Server(gpu, max_lanes=128, workers=w)
+        gids = [S.add(g) for g in graphs]
+        rids = [(gi, S.submit(gids[gi], gpu.Q_BC_SAMPLED, 200, 40 + gi)) for gi in range(len(graphs))]
+        rids += [(1, S.submit(gids[1], gpu.Q_CC))]
+        res = []
+        for gi, rid in rids:
+            assert S.wait(rid) == gpu.REQ_DONE
+            st, bc, cc, _ = S.fetch(rid, gids[gi])
+            assert st == 0
+            res.append((bc, cc))
+        S.close()
+        out[w] = res
+    for (b1, c1), (b8, c8) in zip(out[1], out[8]):
+        assert relerr(b8, b1) < TOL
+        assert np.array_equal(c8, c1)
+    og = orc.Graph(graphs[1].row, graphs[1].col)
+    assert np.array_equal(out[8][-1][1], orc.cc(og, np.arange(graphs[1].n)))
