@@ -35,7 +35,8 @@ class GbcError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("semantics", C.c_int32), ("delta_precision", C.c_int32), ("sigma_mode", C.c_int32),
                 ("engine", C.c_int32), ("lanes", C.c_int32), ("sparse_lanes", C.c_int32),
-                ("levels_per_graph", C.c_int32), ("source_order", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("levels_per_graph", C.c_int32), ("source_order", C.c_int32), ("light_steps", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
 
 
 class RunStats(C.Structure):

@@ -135,10 +135,15 @@ static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requ
 }
 
 static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
-    if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc)) { *out = G->eng.get(); return GBC_OK; }
+    if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc)) {
+        G->eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+        *out = G->eng.get();
+        return GBC_OK;
+    }
     G->eng.reset();
     auto e = std::make_unique<LaneEngine>();
     GBC_TRY(e->init(&G->g, lanes, bc, o.sparse_lanes, o.levels_per_graph, G->stream));
+    e->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
     G->eng = std::move(e);
     *out = G->eng.get();
     return GBC_OK;
@@ -366,6 +371,8 @@ void gbc_options_default(gbc_options* o) {
     o->lanes = 0;
     o->sparse_lanes = -1;
     o->levels_per_graph = 0;
+    o->source_order = 0;
+    o->light_steps = -1;
 }
 
 gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, gbc_graph* out) {

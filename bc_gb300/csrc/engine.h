@@ -36,6 +36,9 @@ struct DevGraph {
     std::vector<int32_t> comp;         // host, per vertex
     std::vector<int64_t> comp_edges;   // host, undirected edges per component
     int32_t max_degree = 0;
+    // Level width new lane engines on this graph start with: 2 once some BFS on
+    // it went deeper than 8-bit levels allow, so later engines skip that pass.
+    mutable int level_bytes_hint = 1;
 };
 
 // Which computation a lane batch performs.
@@ -76,6 +79,9 @@ public:
     // Allocate lane state for `lanes` (multiple of 32, <= 1024) on graph g.
     gbc_status init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
                     cudaStream_t stream);
+    // Expansion tuning (negative = default).  A change drops the captured
+    // level-loop graphs, which hold the old values.
+    void set_tuning(int sparse_lanes, int light_steps, int levels_per_graph);
     // One batch of rq.kb <= lanes sources (forward, then backward for BC).
     gbc_status run(const LaneRequest& rq, LaneResult& res);
     // BC accumulation across batches: zero the per-group partials / reduce them into d_bc[n].
@@ -103,6 +109,7 @@ private:
     int32_t lanes_ = 0, ng_ = 0;
     bool need_bc_ = false;
     int sparse_ = 2;
+    int light_ = 16;
     int lpg_ = 16;
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
     cudaStream_t stream_ = nullptr;

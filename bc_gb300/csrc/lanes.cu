@@ -78,13 +78,13 @@ struct KArgs {
     unsigned long long* cc;
     double* bcg;
     int32_t* srcw;         // per-lane source weight (vertex weight of the lane's source, 1 without weights)
-    int sparse;
+    int sparse;            // entries with <= sparse active lanes expand edge-parallel
+    int light;             // entries with (active lanes x degree) <= light expand one per thread
     int semantics;
 };
 
 constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expanded by a whole CTA
 constexpr int FETCH = 32;       // regular entries a warp takes per fetch, one per thread
-constexpr int LIGHT = 16;       // an entry with (active lanes x degree) <= LIGHT is expanded by one thread
 constexpr int STG = 128;        // regular-queue entries a warp stages in shared memory per append
 constexpr int WARPS = BLOCK / 32;
 // Minimum resident CTAs per SM the level kernels are compiled for.  Deep
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(BLOCK, (MINB<LT, MODE == 2>)) expand_kernel(KA
             unsigned am;
             long long r0, r1;
             fetch_entry<LT>(A, d, base + t, e, ent, am, r0, r1);
-            const bool light = am && (long long)__popc(am) * (r1 - r0) <= LIGHT;
+            const bool light = am && (long long)__popc(am) * (r1 - r0) <= A.light;
             fwd_light<MODE, LT>(A, S, d, ent, light ? am : 0u, r0, r1, cc_sh);
             unsigned hv = __ballot_sync(FULL, am && !light);
             while (hv) {
@@ -972,7 +972,7 @@ __global__ void __launch_bounds__(BLOCK, (MINB<LT, WIDE>)) backward_kernel(KArgs
             unsigned am;
             long long r0, r1;
             fetch_entry<LT>(A, d, base + t, e, ent, am, r0, r1);
-            const bool light = am && (long long)__popc(am) * (r1 - r0) <= LIGHT;
+            const bool light = am && (long long)__popc(am) * (r1 - r0) <= A.light;
             bwd_light<WIDE, T, LT>(A, d, ent, light ? am : 0u, r0, r1, refsem);
             unsigned hv = __ballot_sync(FULL, am && !light);
             while (hv) {
@@ -1139,7 +1139,7 @@ struct LaneAccess {
         A.lvl = e.lvl_; A.sig = e.sig_; A.rho = e.rho_; A.vmark = e.vmark_;
         A.fq = e.fq_; A.fcap = e.fcap_; A.foff = e.foff_; A.ctl = (Ctl*)e.ctl_; A.ovf = e.ovf_;
         A.hq = e.hq_; A.hcap = e.hcap_; A.hoff = e.hoff_;
-        A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.semantics = semantics;
+        A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.light = e.light_; A.semantics = semantics;
         A.srcw = e.srcw_;
         return A;
     }
@@ -1208,9 +1208,8 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     lanes_ = lanes;
     ng_ = lanes / 32;
     need_bc_ = need_bc;
-    lvl_bytes_ = 1;
-    sparse_ = sparse_lanes < 0 ? 2 : sparse_lanes;
-    lpg_ = levels_per_graph > 0 ? levels_per_graph : 16;
+    lvl_bytes_ = g->level_bytes_hint == 2 ? 2 : 1;
+    set_tuning(sparse_lanes, -1, levels_per_graph);
     stream_ = stream;
     int dev = 0;
     GBC_CUDA(cudaGetDevice(&dev));
@@ -1255,6 +1254,18 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     return GBC_OK;
 }
 
+
+void LaneEngine::set_tuning(int sparse_lanes, int light_steps, int levels_per_graph) {
+    const int sp = sparse_lanes < 0 ? 2 : sparse_lanes;
+    const int li = light_steps < 0 ? 16 : light_steps;
+    const int lp = levels_per_graph > 0 ? levels_per_graph : 16;
+    if (sp == sparse_ && li == light_ && lp == lpg_) return;
+    sparse_ = sp;
+    light_ = li;
+    lpg_ = lp;
+    for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
+    graphs_.clear();
+}
 
 // Graph keys: 0..2 expand MODE; 3 + (wide*2 + f64)*2 + refsem: backward; +100 with 16-bit levels.
 gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
@@ -1389,6 +1400,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             if (lvl_bytes_ == 1) {
                 // deeper than 8-bit levels allow: switch this engine to 16-bit levels, redo
                 lvl_bytes_ = 2;
+                g_->level_bytes_hint = 2;
                 GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
                 GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
                 GBC_CUDA(cudaStreamSynchronize(stream_));

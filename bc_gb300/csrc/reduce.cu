@@ -345,6 +345,7 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
         R.eng = std::make_unique<LaneEngine>();
         GBC_TRY(R.eng->init(R.dg.get(), lanes, false, o.sparse_lanes, o.levels_per_graph, R.stream));
     }
+    R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
     int32_t* d_src = nullptr;
     unsigned long long* d_cc = nullptr;
     if (cudaMalloc(&d_src, sizeof(int32_t) * ns) != cudaSuccess || cudaMalloc(&d_cc, sizeof(unsigned long long) * ns) != cudaSuccess) {
@@ -485,6 +486,7 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
         R.ceng = std::make_unique<LaneEngine>();
         GBC_TRY(R.ceng->init(R.cdg.get(), lanes, true, o.sparse_lanes, o.levels_per_graph, R.stream));
     }
+    R.ceng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
     int32_t* d_src = nullptr;
     double* d_bc = nullptr;
     if (cudaMalloc(&d_src, sizeof(int32_t) * nc) != cudaSuccess || cudaMalloc(&d_bc, sizeof(double) * nc) != cudaSuccess) {

@@ -75,7 +75,9 @@ typedef struct {
     int32_t levels_per_graph; /* level kernels per captured CUDA graph; 0 = default */
     int32_t source_order;     /* 0: group sources with similar BFS level profiles into the same
                                  lane group (results do not depend on it); 1: lanes in the order given */
-    int32_t reserved[8];
+    int32_t light_steps;      /* a frontier task with (active lanes x degree) <= this is expanded by a
+                                 single thread, 32 tasks per warp; 0 = never; -1 = autotune */
+    int32_t reserved[7];
 } gbc_options;
 
 typedef struct {

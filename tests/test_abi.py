@@ -37,7 +37,7 @@ def test_exports_every_declared_symbol(gbc):
 def test_version_and_options(gbc):
     assert b"sm_103a" in gbc.lib().gbc_version()
     o = gbc.options()
-    assert (o.semantics, o.delta_precision, o.sigma_mode, o.engine, o.lanes, o.sparse_lanes) == (0, 1, 0, 0, 0, -1)
+    assert (o.semantics, o.delta_precision, o.sigma_mode, o.engine, o.lanes, o.sparse_lanes, o.light_steps) == (0, 1, 0, 0, 0, -1, -1)
     assert gbc.device_count() >= 0
 
 

@@ -160,19 +160,26 @@ def test_sigma_overflow_log_mode(gpu, orc):
         assert ovf.all()
 
 
-@pytest.mark.parametrize("sparse", [0, 32])
-def test_expansion_modes_agree(gpu, orc, graphs, sparse):
-    """Lane-parallel only (sparse=0) and edge-parallel only (sparse=32) give
-    the same exact results."""
+@pytest.mark.parametrize("sparse,light", [(0, 0), (32, 0), (2, 0), (2, 1 << 20), (-1, -1)])
+def test_expansion_modes_agree(gpu, orc, graphs, sparse, light):
+    """Lane-parallel only (sparse=0), edge-parallel only (sparse=32), no
+    one-thread tasks (light=0), one-thread tasks for every non-hub entry and
+    the defaults all give the same exact results, also after switching modes
+    on one engine."""
     csr = graphs["star+grid"]
     og = to_orc(orc, csr)
     src = sources_of(csr, 400, seed=9)
     ref, _ = orc.bc(og, src, semantics=1)
     refcc = orc.cc(og, src)
     with gpu.Graph(csr) as G:
-        got = G.bc(src, semantics=1, sparse_lanes=sparse, lanes=96)
+        G.bc(src[:64], semantics=1, lanes=96)   # capture with the defaults first
+        got = G.bc(src, semantics=1, sparse_lanes=sparse, light_steps=light, lanes=96)
         assert relerr(got, ref) < TOL_F64
-        assert np.array_equal(G.cc(src, sparse_lanes=sparse, lanes=96), refcc)
+        assert np.array_equal(G.cc(src, sparse_lanes=sparse, light_steps=light, lanes=96), refcc)
+        dist, sig, _ = G.sssp(src[:32], light_steps=light, sparse_lanes=sparse)
+        for i, s in enumerate(src[:32]):
+            rd, rs, _, _ = orc.sssp(og, int(s))
+            assert np.array_equal(dist[i], rd) and np.array_equal(sig[i], rs)
 
 
 def test_deep_graph_switches_level_width(gpu, orc):
