@@ -393,10 +393,14 @@ def main():
         # precision: the step's sources with FP32 and FP64 dependency sweeps
         s0 = step_sources(args.warmup)
         bc32 = graph.bc(s0, **{**opt, "delta_precision": G.DELTA_F32})
+        st32 = graph.stats()
         bc64 = graph.bc(s0, **{**opt, "delta_precision": G.DELTA_F64})
+        st64 = graph.stats()
         nz = bc64 > 0
         prec = {"delta_f32_rel_err_vs_f64": float(np.max(np.abs(bc32 - bc64) / np.maximum(np.abs(bc64), 1.0))),
                 "delta_f32_rel_err_vs_f64_nonzero": float(np.max(np.abs(bc32[nz] - bc64[nz]) / bc64[nz])) if nz.any() else 0.0,
+                "gteps_f32_delta": round(st32["edges_traversed"] / (st32["kernel_ms"] * 1e-3) / 1e9, 3),
+                "gteps_f64_delta": round(st64["edges_traversed"] / (st64["kernel_ms"] * 1e-3) / 1e9, 3),
                 "sources": int(B),
                 "note": "rel err = max|a-b|/max(|b|,1) as in the tests; the FP64-delta path is checked against the "
                         "FP64 oracle to 1e-9 in tests"}
