@@ -80,6 +80,7 @@ _PROTOS = [
     ("gbc_last_error", C.c_char_p, []),
     ("gbc_version", C.c_char_p, []),
     ("gbc_device_count", C.c_int, []),
+    ("gbc_release_cached_memory", _st, []),
     ("gbc_graph_create", _st, [_i64p, _i32p, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_create_device", _st, [_vp, _vp, C.c_int32, C.c_int64, C.POINTER(_vp)]),
     ("gbc_graph_destroy", _st, [_vp]),

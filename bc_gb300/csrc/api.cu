@@ -127,8 +127,7 @@ static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requ
     int32_t lanes = (int32_t)std::min<int64_t>(1024, ((k + 31) / 32) * 32);
     lanes = std::max(lanes, 32);
     if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes) return G->eng->lanes();
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    const size_t fr = dev_free_bytes();
     const size_t budget = (fr + (G->eng ? G->eng->device_bytes() : 0)) / 2;
     while (lanes > 32 && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= 32;
     return lanes;

@@ -25,6 +25,15 @@ namespace gbc {
         if (s_ != GBC_OK) return s_;          \
     } while (0)
 
+// Device-buffer cache for lane state (devmem.cpp): dev_alloc takes a cached
+// block of the same size (or at most 25% larger) or calls cudaMalloc;
+// dev_release returns a block whose work has finished to the cache.
+cudaError_t dev_alloc(void** p, size_t bytes);
+void dev_release(void* p, size_t bytes);
+size_t dev_cached_bytes();
+// cudaMemGetInfo's free bytes plus the cached ones.
+size_t dev_free_bytes();
+
 // Device CSR (+ host-side component information for the GTEPS numerator).
 struct DevGraph {
     int32_t n = 0;
@@ -112,6 +121,7 @@ private:
     int light_ = 16;
     int lpg_ = 16;
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
+    size_t lvl_sz_ = 0, vmark_sz_ = 0, sig_sz_ = 0, rho_sz_ = 0, bcg_sz_ = 0;   // bytes of the cached buffers
     cudaStream_t stream_ = nullptr;
     size_t bytes_ = 0;
     uint16_t* lvl_ = nullptr;

@@ -74,15 +74,35 @@ static void parallel_for(int64_t n, F f) {
 }
 
 // --------------------------------------------------------- CSR build ----
+// First index in [0, count) where bad(i) holds, or count; chunks are scanned
+// in parallel and the smallest hit wins, so the answer does not depend on the
+// thread count.
+template <class F>
+static int64_t first_bad(int64_t count, F bad) {
+    std::atomic<int64_t> best(count);
+    parallel_for(count, [&](int64_t a, int64_t b) {
+        for (int64_t i = a; i < b; i++) {
+            if (i >= best.load(std::memory_order_relaxed)) return;
+            if (bad(i)) {
+                int64_t cur = best.load(std::memory_order_relaxed);
+                while (i < cur && !best.compare_exchange_weak(cur, i, std::memory_order_relaxed)) {
+                }
+                return;
+            }
+        }
+    });
+    return best.load();
+}
+
 gbc_status validate_csr(const int64_t* row, const int32_t* col, int32_t n) {
     if (n <= 0 || !row || (row[n] > 0 && !col)) { set_error("invalid CSR arguments (n=%d)", n); return GBC_ERR_ARG; }
     if (row[0] != 0) { set_error("row[0] must be 0"); return GBC_ERR_ARG; }
-    for (int32_t v = 0; v < n; v++)
-        if (row[v + 1] < row[v]) { set_error("row offsets decrease at %d", v); return GBC_ERR_ARG; }
+    const int64_t dv = first_bad(n, [&](int64_t v) { return row[v + 1] < row[v]; });
+    if (dv < n) { set_error("row offsets decrease at %lld", (long long)dv); return GBC_ERR_ARG; }
     int64_t m = row[n];
     if (m >= ((int64_t)1 << 31)) { set_error("more than 2^31-1 directed edges (%lld)", (long long)m); return GBC_ERR_ARG; }
-    for (int64_t e = 0; e < m; e++)
-        if ((uint32_t)col[e] >= (uint32_t)n) { set_error("col[%lld]=%d out of range", (long long)e, col[e]); return GBC_ERR_ARG; }
+    const int64_t be = first_bad(m, [&](int64_t e) { return (uint32_t)col[e] >= (uint32_t)n; });
+    if (be < m) { set_error("col[%lld]=%d out of range", (long long)be, col[be]); return GBC_ERR_ARG; }
     return GBC_OK;
 }
 

@@ -1155,14 +1155,24 @@ size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc) {
 void LaneEngine::release() {
     for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
     graphs_.clear();
-    cudaFree(lvl_); cudaFree(sig_); cudaFree(rho_); cudaFree(vmark_); cudaFree(fq_); cudaFree(foff_);
-    cudaFree(hq_); cudaFree(hoff_);
+    // work on these buffers must be finished before they go back to the cache
+    if (stream_) cudaStreamSynchronize(stream_);
+    dev_release(lvl_, lvl_sz_);
+    dev_release(sig_, sig_sz_);
+    dev_release(rho_, rho_sz_);
+    dev_release(vmark_, vmark_sz_);
+    dev_release(fq_, fcap_ * sizeof(uint32_t));
+    dev_release(hq_, hcap_ * sizeof(uint32_t));
+    dev_release(bcg_, bcg_sz_);
+    fcap_ = hcap_ = 0;
+    dev_release(foff_, (MAX_LEVEL + 2) * sizeof(unsigned long long));
+    dev_release(hoff_, (MAX_LEVEL + 2) * sizeof(unsigned long long));
     hq_ = nullptr; hoff_ = nullptr;
-    cudaFree(ctl_); cudaFree(ovf_);
+    dev_release(ctl_, sizeof(Ctl));
+    dev_release(ovf_, 32 * sizeof(uint32_t));
     if (ctl_host_) cudaFreeHost(ctl_host_);
-    cudaFree(bcg_);
-    cudaFree(ccbuf_);
-    cudaFree(srcw_);
+    dev_release(ccbuf_, 1024 * sizeof(unsigned long long));
+    dev_release(srcw_, 1024 * sizeof(int32_t));
     srcw_ = nullptr;
     lvl_ = nullptr; sig_ = nullptr; rho_ = nullptr; vmark_ = nullptr; fq_ = nullptr; foff_ = nullptr;
     ctl_ = nullptr; ovf_ = nullptr; ctl_host_ = nullptr; bcg_ = nullptr; ccbuf_ = nullptr;
@@ -1183,11 +1193,14 @@ gbc_status LaneEngine::ensure_events(size_t count) {
 }
 
 gbc_status LaneEngine::alloc_queue(unsigned long long cap, unsigned long long hcap) {
-    cudaFree(fq_);
-    cudaFree(hq_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    dev_release(fq_, fcap_ * sizeof(uint32_t));
+    dev_release(hq_, hcap_ * sizeof(uint32_t));
     fq_ = nullptr;
     hq_ = nullptr;
-    if (cudaMalloc(&fq_, cap * sizeof(uint32_t)) != cudaSuccess || cudaMalloc(&hq_, hcap * sizeof(uint32_t)) != cudaSuccess) {
+    fcap_ = hcap_ = 0;
+    if (dev_alloc((void**)&fq_, cap * sizeof(uint32_t)) != cudaSuccess ||
+        dev_alloc((void**)&hq_, hcap * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
         set_error("frontier queue allocation of %llu + %llu entries failed", cap, hcap);
         return GBC_ERR_NOMEM;
@@ -1217,19 +1230,24 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     const size_t n = (size_t)g->n;
     const size_t cells = (size_t)lanes * n;
     bool ok = true;
-    ok &= cudaMalloc(&lvl_, cells * sizeof(uint16_t)) == cudaSuccess;
-    ok &= cudaMalloc(&vmark_, (size_t)ng_ * n * sizeof(int32_t)) == cudaSuccess;
-    ok &= cudaMalloc(&foff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
-    ok &= cudaMalloc(&hoff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
-    ok &= cudaMalloc(&ctl_, sizeof(Ctl)) == cudaSuccess;
-    ok &= cudaMalloc(&ovf_, 32 * sizeof(uint32_t)) == cudaSuccess;
-    ok &= cudaMalloc(&ccbuf_, 1024 * sizeof(unsigned long long)) == cudaSuccess;
-    ok &= cudaMalloc(&srcw_, 1024 * sizeof(int32_t)) == cudaSuccess;
+    lvl_sz_ = cells * sizeof(uint16_t);
+    vmark_sz_ = (size_t)ng_ * n * sizeof(int32_t);
+    ok &= dev_alloc((void**)&lvl_, lvl_sz_) == cudaSuccess;
+    ok &= dev_alloc((void**)&vmark_, vmark_sz_) == cudaSuccess;
+    ok &= dev_alloc((void**)&foff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
+    ok &= dev_alloc((void**)&hoff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
+    ok &= dev_alloc((void**)&ctl_, sizeof(Ctl)) == cudaSuccess;
+    ok &= dev_alloc((void**)&ovf_, 32 * sizeof(uint32_t)) == cudaSuccess;
+    ok &= dev_alloc((void**)&ccbuf_, 1024 * sizeof(unsigned long long)) == cudaSuccess;
+    ok &= dev_alloc((void**)&srcw_, 1024 * sizeof(int32_t)) == cudaSuccess;
     ok &= cudaMallocHost(&ctl_host_, sizeof(Ctl)) == cudaSuccess;
     if (need_bc) {
-        ok &= cudaMalloc(&sig_, cells * sizeof(uint64_t)) == cudaSuccess;
-        ok &= cudaMalloc(&rho_, cells * sizeof(double)) == cudaSuccess;
-        ok &= cudaMalloc(&bcg_, (size_t)ng_ * n * sizeof(double)) == cudaSuccess;
+        sig_sz_ = cells * sizeof(uint64_t);
+        rho_sz_ = cells * sizeof(double);
+        bcg_sz_ = (size_t)ng_ * n * sizeof(double);
+        ok &= dev_alloc((void**)&sig_, sig_sz_) == cudaSuccess;
+        ok &= dev_alloc((void**)&rho_, rho_sz_) == cudaSuccess;
+        ok &= dev_alloc((void**)&bcg_, bcg_sz_) == cudaSuccess;
     }
     if (!ok) {
         cudaGetLastError();

@@ -338,8 +338,7 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
     D.assign(ns, 0);
     if (ns == 0) return GBC_OK;
     int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + 31) / 32) * 32);
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    const size_t fr = dev_free_bytes();
     while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(ns, lanes, false) > fr / 2) lanes -= 32;
     if (!R.eng || R.eng->lanes() != lanes) {
         R.eng = std::make_unique<LaneEngine>();
@@ -479,8 +478,7 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
     out.assign(nc, 0.0);
     if (nc == 0) return GBC_OK;
     int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((nc + 31) / 32) * 32);
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); fr = (size_t)8 << 30; }
+    const size_t fr = dev_free_bytes();
     while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(nc, lanes, true) > fr / 2) lanes -= 32;
     if (!R.ceng || R.ceng->lanes() != lanes) {
         R.ceng = std::make_unique<LaneEngine>();

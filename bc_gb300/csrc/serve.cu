@@ -332,9 +332,7 @@ gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out) {
     S->max_inflight = S->cfg.max_inflight > 0 ? S->cfg.max_inflight : 64;
     if (S->cfg.workers < 0 || S->cfg.workers > 16) { set_error("workers must be in [0,16]"); return GBC_ERR_ARG; }
     S->nworkers = S->cfg.workers ? S->cfg.workers : 4;
-    size_t fr = 0, tot = 0;
-    GBC_CUDA(cudaMemGetInfo(&fr, &tot));
-    S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : fr / 2;
+    S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : dev_free_bytes() / 2;
     gbc_server_s* raw = S.get();
     for (int32_t w = 0; w < S->nworkers; w++) S->workers.emplace_back([raw] { raw->run(); });
     *out = S.release();

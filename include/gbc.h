@@ -223,6 +223,13 @@ gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, i
 gbc_status gbc_read_edgelist(const char* path, int64_t** row, int32_t** col, int32_t* n, int32_t* start);
 void gbc_free(void* p);
 
+/* Lane-state buffers of destroyed graphs and engines are kept for reuse by
+ * later engines of the same size (creating and destroying graphs in a loop
+ * then costs no cudaMalloc/cudaFree).  This returns the cached buffers of the
+ * current device to the driver.  Cached bytes count as free when the library
+ * sizes its own engines. */
+gbc_status gbc_release_cached_memory(void);
+
 /* ---- serving: continuous batching over device-resident graphs ---------
  * A server owns a set of registered graphs and worker threads.  Requests
  * (exact CC, exact BC, or k-source sampled BC) are admitted while their lane

@@ -218,3 +218,22 @@ def test_reduced_bc_host_logic(gbc, orc, datasets, case):
     assert len(vert) == info["alive"] and int(w.sum()) == csr.n - csr.start   # reach covers every vertex once
     got = R.assemble_bc(_weighted_brandes(core, w))
     assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+
+
+def test_validation_reports_first_bad_entry(gbc):
+    """Large CSRs are validated by several threads; the error still names the
+    first offending entry."""
+    L = gbc.lib()
+    n = 1000
+    m = 400_000
+    row = np.linspace(0, m, n + 1).astype(np.int64)
+    col = (np.arange(m) % n).astype(np.int32)
+    col[150_001] = n + 5
+    col[390_000] = -1
+    h = C.c_void_p()
+    assert L.gbc_graph_create(row, col, n, C.byref(h)) == 1
+    assert b"col[150001]" in L.gbc_last_error()
+    rowbad = row.copy()
+    rowbad[700] = rowbad[702] + 1
+    assert L.gbc_graph_create(rowbad, np.zeros(m, np.int32), n, C.byref(h)) == 1
+    assert b"decrease at 700" in L.gbc_last_error()

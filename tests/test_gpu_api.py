@@ -153,3 +153,27 @@ def test_c2_config_reduction_full_size(gpu, orc):
     og = orc.Graph(csr.row, csr.col)
     pick = np.random.default_rng(2).choice(csr.n, 300, replace=False).astype(np.int32)
     assert np.array_equal(cc_red[pick], orc.cc(og, pick, nthreads=8))
+
+
+def test_cached_lane_state_reused_and_released(gpu, orc):
+    """Destroyed graphs leave their lane state in the library's cache; a new
+    graph of the same size reuses it with identical results, and
+    gbc_release_cached_memory returns it to the driver."""
+    torch = pytest.importorskip("torch")
+    csr = gpu.gen_rmat(14, 8, seed=11)
+    src = np.arange(0, csr.n, 37, dtype=np.int32)[:256]
+    gpu.check(gpu.lib().gbc_release_cached_memory())
+    free0 = torch.cuda.mem_get_info()[0]
+    with gpu.Graph(csr) as G:
+        a = G.bc(src, lanes=256)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 < free0 - (64 << 20)          # the engine's buffers stayed allocated (cached)
+    with gpu.Graph(csr) as G:
+        b = G.bc(src, lanes=256)
+    assert np.array_equal(a, b)
+    assert torch.cuda.mem_get_info()[0] >= free1 - (16 << 20)   # reused, not allocated again
+    gpu.check(gpu.lib().gbc_release_cached_memory())
+    assert torch.cuda.mem_get_info()[0] > free1 + (64 << 20)
+    og = orc.Graph(csr.row, csr.col)
+    ref, _ = orc.bc(og, src)
+    assert np.max(np.abs(a - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
