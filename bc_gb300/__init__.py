@@ -81,6 +81,7 @@ _PROTOS = [
     ("gbc_version", C.c_char_p, []),
     ("gbc_device_count", C.c_int, []),
     ("gbc_release_cached_memory", _st, []),
+    ("gbc_autotune", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), C.POINTER(Options)]),
     ("gbc_graph_create", _st, [_i64p, _i32p, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_create_device", _st, [_vp, _vp, C.c_int32, C.c_int64, C.POINTER(_vp)]),
     ("gbc_graph_destroy", _st, [_vp]),
@@ -265,6 +266,15 @@ class Graph:
         p, k, keep = self._src(sources)
         check(lib().gbc_bc(self.h, p, k, C.byref(options(**opt)), out))
         return out
+
+    def autotune(self, sources=None, **opt) -> dict:
+        """Time candidate expansion settings on these sources; later calls
+        that leave them to autotuning use the fastest.  Returns the chosen
+        lanes / sparse_lanes / light_steps / levels_per_graph."""
+        p, k, keep = self._src(sources)
+        ch = Options()
+        check(lib().gbc_autotune(self.h, p, k, C.byref(options(**opt)), C.byref(ch)))
+        return {f: getattr(ch, f) for f in ("lanes", "sparse_lanes", "light_steps", "levels_per_graph")}
 
     def cc(self, sources=None, **opt) -> np.ndarray:
         p, k, keep = self._src(sources)

@@ -30,6 +30,11 @@ struct gbc_graph_s {
     std::vector<int32_t> deg;
     int32_t* d_pos = nullptr;
     int64_t pos_cap = 0;
+    // settings chosen by gbc_autotune; used where the options ask for autotuning
+    struct {
+        bool done = false;
+        int32_t lanes = 0, sparse = -1, light = -1, lpg = 0;
+    } tuned;
     ~gbc_graph_s() {
         eng.reset();
         cudaFree(g.row);
@@ -124,7 +129,7 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
 static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested) {
     if (requested) return requested;
     const DevGraph& g = G->g;
-    int32_t lanes = (int32_t)std::min<int64_t>(1024, ((k + 31) / 32) * 32);
+    int32_t lanes = (int32_t)std::min<int64_t>(G->tuned.lanes ? G->tuned.lanes : 1024, ((k + 31) / 32) * 32);
     lanes = std::max(lanes, 32);
     if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes) return G->eng->lanes();
     const size_t fr = dev_free_bytes();
@@ -133,16 +138,27 @@ static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requ
     return lanes;
 }
 
+// Expansion settings of a call: the options' values, or the graph's tuned ones
+// where the options leave them to autotuning.
+static void tuning_of(const gbc_graph_s* G, const gbc_options& o, int& sparse, int& light, int& lpg) {
+    const bool t = G->tuned.done;
+    sparse = (o.sparse_lanes < 0 && t) ? G->tuned.sparse : o.sparse_lanes;
+    light = (o.light_steps < 0 && t) ? G->tuned.light : o.light_steps;
+    lpg = (o.levels_per_graph <= 0 && t) ? G->tuned.lpg : o.levels_per_graph;
+}
+
 static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
+    int sparse, light, lpg;
+    tuning_of(G, o, sparse, light, lpg);
     if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc)) {
-        G->eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+        G->eng->set_tuning(sparse, light, lpg);
         *out = G->eng.get();
         return GBC_OK;
     }
     G->eng.reset();
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G->g, lanes, bc, o.sparse_lanes, o.levels_per_graph, G->stream));
-    e->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+    GBC_TRY(e->init(&G->g, lanes, bc, sparse, lpg, G->stream));
+    e->set_tuning(sparse, light, lpg);
     G->eng = std::move(e);
     *out = G->eng.get();
     return GBC_OK;
@@ -487,6 +503,95 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     float ms = 0;
     cudaEventElapsedTime(&ms, G->ev0, G->ev1);
     finish_stats(G, res, k, batches, lanes, sig, hsrc, ms, now_ms() - t0);
+    return GBC_OK;
+}
+
+// Device time (forward + dependency sweep) of one betweenness batch of the
+// staged sources d_src[0..kb) with the given expansion settings.
+static gbc_status tune_batch(gbc_graph_s* G, int32_t lanes, int32_t kb, const gbc_options& o, int sparse, int light,
+                             int lpg, double& ms) {
+    LaneEngine* E = nullptr;
+    GBC_TRY(get_engine(G, lanes, true, o, &E));
+    E->set_tuning(sparse, light, lpg);
+    GBC_TRY(E->bc_begin());
+    LaneRequest rq;
+    rq.job = LaneJob::BC;
+    rq.d_src = G->d_src;
+    rq.kb = kb;
+    rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
+    rq.semantics = o.semantics;
+    rq.sigma_wide = o.sigma_mode == GBC_SIGMA_WIDE;
+    rq.abort_on_overflow = !rq.sigma_wide;
+    LaneResult res;
+    gbc_status st = E->run(rq, res);
+    if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO) {
+        rq.sigma_wide = 1;
+        rq.abort_on_overflow = false;
+        LaneResult r2;
+        st = E->run(rq, r2);
+        res = r2;
+    }
+    if (st != GBC_OK) return st;
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    ms = res.fwd_ms + res.bwd_ms;
+    return GBC_OK;
+}
+
+gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gbc_options* opt, gbc_options* chosen) {
+    if (!G) { set_error("graph is NULL"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    gbc_options o;
+    GBC_TRY(resolve_options(opt, o));
+    if (o.engine == GBC_ENGINE_PLAIN) { set_error("autotuning applies to the lane engine"); return GBC_ERR_ARG; }
+    std::vector<int32_t> hsrc, pos;
+    GBC_TRY(resolve_sources(G, sources, k, hsrc));
+    G->tuned.done = false;
+    const int32_t k0 = (int32_t)hsrc.size();
+    int32_t lanes = pick_lanes(G, k0, true, o.lanes);
+    GBC_TRY(order_sources(G, o, true, hsrc, pos));
+    GBC_TRY(upload_sources(G, hsrc));
+    // candidate settings; the options' explicit values are kept fixed
+    const int sp0 = o.sparse_lanes >= 0 ? o.sparse_lanes : 2;
+    const int li0 = o.light_steps >= 0 ? o.light_steps : 16;
+    const int lp0 = o.levels_per_graph > 0 ? o.levels_per_graph : 16;
+    int best_sp = sp0, best_li = li0, best_lp = lp0;
+    double best = 0;
+    const int32_t kb = std::min(lanes, k0);
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, best));   // warm-up: level width, queue size, graph capture
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, best));
+    auto consider = [&](int sp, int li, int lp) -> gbc_status {
+        double ms = 0;
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp, li, lp, ms));
+        if (ms < best) { best = ms; best_sp = sp; best_li = li; best_lp = lp; }
+        return GBC_OK;
+    };
+    // one-thread tasks, then the edge-parallel threshold, then the level-loop graph length
+    if (o.light_steps < 0)
+        for (int li : {0, 8, 32}) GBC_TRY(consider(best_sp, li, best_lp));
+    if (o.sparse_lanes < 0)
+        for (int sp : {1, 4}) GBC_TRY(consider(sp, best_li, best_lp));
+    if (o.levels_per_graph <= 0 && G->eng && G->eng->level_bytes() == 2) GBC_TRY(consider(best_sp, best_li, 64));
+    // batch width: half the lanes, compared per source
+    int32_t best_lanes = lanes;
+    if (o.lanes == 0 && lanes >= 64 && kb == lanes) {
+        double ms = 0;
+        const int32_t half = lanes / 2;
+        GBC_TRY(tune_batch(G, half, half, o, best_sp, best_li, best_lp, ms));   // warm-up of the narrower engine
+        GBC_TRY(tune_batch(G, half, half, o, best_sp, best_li, best_lp, ms));
+        if (2.0 * ms < best) best_lanes = half;
+    }
+    G->tuned.done = true;
+    G->tuned.lanes = o.lanes ? 0 : best_lanes;
+    G->tuned.sparse = best_sp;
+    G->tuned.light = best_li;
+    G->tuned.lpg = best_lp;
+    if (chosen) {
+        *chosen = o;
+        chosen->lanes = best_lanes;
+        chosen->sparse_lanes = best_sp;
+        chosen->light_steps = best_li;
+        chosen->levels_per_graph = best_lp;
+    }
     return GBC_OK;
 }
 

@@ -101,6 +101,7 @@ public:
     // Per-lane distance sums of the last CC batch (lanes entries) to the host.
     gbc_status cc_read(unsigned long long* h_cc, int32_t count);
     int32_t lanes() const { return lanes_; }
+    int level_bytes() const { return lvl_bytes_; }
     bool has_bc() const { return need_bc_; }
     const DevGraph* graph() const { return g_; }
     cudaStream_t stream() const { return stream_; }

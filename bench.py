@@ -55,6 +55,7 @@ def parse():
                    help="dependency-sweep precision (FP32 delta with FP64 BC sums is the default design)")
     p.add_argument("--plain-sources", type=int, default=16)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-tune", action="store_true", help="skip gbc_autotune; use the default expansion settings")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
@@ -331,6 +332,8 @@ def main():
         G.check(L.gbc_graph_last_stats(g.h, C.byref(st)))
         return st
 
+    # autotune the expansion settings on the first step's sources (lanes stay at B)
+    tuning = None if args.no_tune else graph.autotune(step_sources(0), **opt)
     for i in range(args.warmup):
         run_step(i)
     torch.cuda.synchronize()
@@ -461,7 +464,8 @@ def main():
                "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor,
                           "n": n, "m_directed": M, "lanes_per_step": B, "sources": args.k,
                           "parallelism": f"sources sharded over {ws} GPU(s)",
-                          "l2": "inputs larger than L2 (lane state ~16*B*n bytes per sweep)"},
+                          "l2": "inputs larger than L2 (lane state ~16*B*n bytes per sweep)",
+                          "tuning": tuning},
                "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
                "plain": None if plain_gteps is None else {
                    "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),

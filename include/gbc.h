@@ -128,6 +128,17 @@ gbc_status gbc_bc(gbc_graph g, const int32_t* sources, int32_t k, const gbc_opti
 gbc_status gbc_bc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const gbc_options* opt,
                          double* d_bc, void* stream);
 
+/* Autotuner: time one betweenness batch of the given sources (k = 0: all
+ * vertices) per candidate expansion setting -- one-thread task threshold
+ * (light_steps 0/8/16/32), edge-parallel threshold (sparse_lanes 1/2/4), level
+ * kernels per captured graph (16/64, deep graphs) and batch width (lanes, lanes/2),
+ * one at a time -- and keep the fastest on the graph.  Later calls whose
+ * options leave a setting to autotuning (-1 / 0) use the tuned value; values
+ * set in the options are not tuned.  *chosen (nullable) receives the options
+ * with the chosen settings filled in.  Results do not depend on the settings
+ * beyond FP64 summation order. */
+gbc_status gbc_autotune(gbc_graph g, const int32_t* sources, int32_t k, const gbc_options* opt, gbc_options* chosen);
+
 /* ---- closeness (distance sums) -----------------------------------------
  * cc[i] = sum of hop distances from sources[i] to every vertex it reaches
  * (Seq_CC/CC.cpp:76-100); k = 0 with sources = NULL means all n vertices. */

@@ -177,3 +177,23 @@ def test_cached_lane_state_reused_and_released(gpu, orc):
     og = orc.Graph(csr.row, csr.col)
     ref, _ = orc.bc(og, src)
     assert np.max(np.abs(a - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+
+
+def test_autotune_choices_and_results(gpu, orc):
+    """The autotuner returns valid settings, leaves explicit options alone,
+    and later calls that use the tuned settings stay within tolerance of the
+    oracle."""
+    csr = gpu.gen_grid(60, 60, 0.05, seed=4)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.arange(0, csr.n, 7, dtype=np.int32)[:256]
+    ref, _ = orc.bc(og, src, scaled=True)
+    with gpu.Graph(csr) as G:
+        ch = G.autotune(src, light_steps=8)
+        assert ch["light_steps"] == 8
+        assert ch["sparse_lanes"] in (1, 2, 4) and ch["levels_per_graph"] in (16, 64)
+        assert ch["lanes"] in (128, 256)
+        got = G.bc(src)
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+        ch2 = G.autotune(src)
+        assert ch2["light_steps"] in (0, 8, 16, 32)
+        assert np.array_equal(G.cc(src), orc.cc(og, src))
