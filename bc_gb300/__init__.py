@@ -112,6 +112,7 @@ _PROTOS = [
                                C.POINTER(_vp), C.POINTER(C.c_int32)]),
     ("gbc_read_edgelist", _st, [C.c_char_p, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32)]),
+    ("gbc_write_scores", _st, [C.c_char_p, _f64p, C.c_int32, C.c_int32, C.c_int32]),
     ("gbc_free", None, [_vp]),
     ("gbc_server_create", _st, [C.POINTER(ServerConfig), C.POINTER(_vp)]),
     ("gbc_server_destroy", _st, [_vp]),
@@ -161,6 +162,14 @@ def options(**kw) -> Options:
             raise KeyError(k)
         setattr(o, k, int(v))
     return o
+
+
+def write_scores(path: str, values: np.ndarray, start: int, end: int, append: bool = False):
+    """values[start..end] in the reference's BC_Score.txt layout."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    if end >= len(v):
+        raise ValueError("end past the values")
+    check(lib().gbc_write_scores(path.encode(), v, int(start), int(end), int(bool(append))))
 
 
 def device_count() -> int:

@@ -383,6 +383,19 @@ gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, i
     return export_csr(g, row_out, col_out);
 }
 
+// "start end" header, then one "%f" line per vertex of values rounded to FP32
+// (the reference prints its float BC array this way).
+gbc_status gbc_write_scores(const char* path, const double* values, int32_t start, int32_t end, int32_t append) {
+    if (!path || !values || start < 0 || end < start - 1) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    FILE* f = fopen(path, append ? "a" : "w");
+    if (!f) { set_error("cannot open %s", path); return GBC_ERR_ARG; }
+    bool ok = fprintf(f, "%d %d\n", start, end) > 0;
+    for (int32_t v = start; v <= end && ok; v++) ok = fprintf(f, "%f\n", (double)(float)values[v]) > 0;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) { set_error("write to %s failed", path); return GBC_ERR_ARG; }
+    return GBC_OK;
+}
+
 // Text edge list, as Lib/AdjList/AdjList.c:13-150 reads it: header "n m",
 // then m lines "u v"; 0-based when any endpoint is 0, else slot 0 is a
 // phantom vertex.  Both directions kept in file order, then each list is

@@ -232,6 +232,11 @@ gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, i
  * Lib/AdjList/AdjList.c:13) -> CSR over n (0-based) or n+1 (1-based) slots;
  * *start = 0 or 1.  Neighbours ordered by neighbour degree ascending. */
 gbc_status gbc_read_edgelist(const char* path, int64_t** row, int32_t** col, int32_t* n, int32_t* start);
+/* Score file in the reference's BC_Score.txt layout (Seq_Brandes/Brandes.c:2318-2321):
+ * a "start end" line, then values[v] for v = start..end, one "%f" per line,
+ * each rounded to FP32 first as the reference's float arrays are.  append != 0
+ * appends as the reference's "a" mode does. */
+gbc_status gbc_write_scores(const char* path, const double* values, int32_t start, int32_t end, int32_t append);
 void gbc_free(void* p);
 
 /* Lane-state buffers of destroyed graphs and engines are kept for reuse by

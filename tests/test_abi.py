@@ -237,3 +237,22 @@ def test_validation_reports_first_bad_entry(gbc):
     rowbad[700] = rowbad[702] + 1
     assert L.gbc_graph_create(rowbad, np.zeros(m, np.int32), n, C.byref(h)) == 1
     assert b"decrease at 700" in L.gbc_last_error()
+
+
+def test_score_file_matches_reference_layout(gbc, orc, datasets, tmp_path):
+    """gbc_write_scores writes the reference's BC_Score.txt layout: karate BC
+    (reference semantics, from the oracle) against the reference's golden
+    file, line by line."""
+    csr = gbc.read_edgelist(datasets["karate.txt"])
+    og = orc.Graph(csr.row, csr.col, csr.start)
+    bc, _ = orc.bc(og, np.arange(csr.start, csr.n), semantics=orc.BC_REFERENCE)
+    out = tmp_path / "BC_Score.txt"
+    gbc.write_scores(str(out), bc, csr.start, csr.n - 1)
+    got = out.read_text().splitlines()
+    gold = open(os.path.join(GOLDEN, "karate_BC_Score.txt")).read().splitlines()
+    assert got[0] == gold[0] == "1 34" and len(got) == len(gold)
+    for a, b in zip(got[1:], gold[1:]):
+        assert len(a.split(".")[1]) == 6                 # "%f"
+        assert abs(float(a) - float(b)) <= 2e-6 * max(1.0, float(b))
+    gbc.write_scores(str(out), bc, csr.start, csr.start, append=True)
+    assert out.read_text().splitlines()[-2:] == ["1 1", got[1]]
