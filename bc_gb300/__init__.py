@@ -85,6 +85,9 @@ _PROTOS = [
     ("gbc_graph_create", _st, [_i64p, _i32p, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_create_device", _st, [_vp, _vp, C.c_int32, C.c_int64, C.POINTER(_vp)]),
     ("gbc_graph_destroy", _st, [_vp]),
+    ("gbc_graph_from_edges", _st, [_i32p, _i32p, C.c_int64, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_graph_from_edges_device", _st, [_vp, _vp, C.c_int64, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_graph_export", _st, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
     ("gbc_graph_info", _st, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_size_t)]),
     ("gbc_graph_last_stats", _st, [_vp, C.POINTER(RunStats)]),
     ("gbc_bc", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _f64p]),
@@ -246,6 +249,27 @@ class Graph:
         h = _vp()
         check(lib().gbc_graph_create(csr.row, csr.col, csr.n, C.byref(h)))
         self.h = h
+
+    @classmethod
+    def from_edges(cls, u, v, n: int) -> "Graph":
+        """Build the CSR on the device from an edge list (gbc_graph_from_edges)."""
+        uu = np.ascontiguousarray(u, dtype=np.int32)
+        vv = np.ascontiguousarray(v, dtype=np.int32)
+        if len(uu) != len(vv):
+            raise ValueError("u and v differ in length")
+        h = _vp()
+        check(lib().gbc_graph_from_edges(uu, vv, len(uu), int(n), C.byref(h)))
+        g = cls.__new__(cls)
+        g.h = h
+        g.n = int(n)
+        g.csr = g.export()
+        return g
+
+    def export(self) -> CSR:
+        """The device CSR, copied to the host."""
+        rp, cp, n = _vp(), _vp(), C.c_int32()
+        check(lib().gbc_graph_export(self.h, C.byref(rp), C.byref(cp), C.byref(n)))
+        return _take_csr(rp, cp, n.value)
 
     def close(self):
         if getattr(self, "h", None):

@@ -401,6 +401,60 @@ gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, g
     return GBC_OK;
 }
 
+gbc_status gbc_graph_from_edges_device(const int32_t* d_u, const int32_t* d_v, int64_t m, int32_t n, gbc_graph* out) {
+    if (!out || n <= 0 || m < 0 || (m > 0 && (!d_u || !d_v))) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    GBC_TRY(ensure_device());
+    auto G = std::make_unique<gbc_graph_s>();
+    GBC_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    GBC_CUDA(cudaEventCreate(&G->ev0));
+    GBC_CUDA(cudaEventCreate(&G->ev1));
+    int64_t M = 0;
+    GBC_TRY(csr_from_edges_device(d_u, d_v, m, n, G->stream, &G->g.row, &G->g.col, &M));
+    G->g.n = n;
+    G->g.m = M;
+    *out = G.release();
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_from_edges(const int32_t* u, const int32_t* v, int64_t m, int32_t n, gbc_graph* out) {
+    if (!out || n <= 0 || m < 0 || (m > 0 && (!u || !v))) { set_error("bad arguments"); return GBC_ERR_ARG; }
+    GBC_TRY(ensure_device());
+    int32_t *du = nullptr, *dv = nullptr;
+    if (cudaMalloc(&du, sizeof(int32_t) * std::max<int64_t>(m, 1)) != cudaSuccess ||
+        cudaMalloc(&dv, sizeof(int32_t) * std::max<int64_t>(m, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(du);
+        set_error("edge list upload buffers");
+        return GBC_ERR_NOMEM;
+    }
+    gbc_status st = GBC_OK;
+    if (m && (cudaMemcpy(du, u, sizeof(int32_t) * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+              cudaMemcpy(dv, v, sizeof(int32_t) * m, cudaMemcpyHostToDevice) != cudaSuccess)) {
+        cudaGetLastError();
+        set_error("edge list upload failed");
+        st = GBC_ERR_CUDA;
+    }
+    if (st == GBC_OK) st = gbc_graph_from_edges_device(du, dv, m, n, out);
+    cudaFree(du);
+    cudaFree(dv);
+    return st;
+}
+
+gbc_status gbc_graph_export(gbc_graph G, int64_t** row, int32_t** col, int32_t* n) {
+    if (!G || !row || !col || !n) { set_error("NULL argument"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    HostCSR h;
+    h.n = G->g.n;
+    h.row.resize((size_t)G->g.n + 1);
+    h.col.resize(std::max<int64_t>(G->g.m, 1));
+    GBC_CUDA(cudaMemcpy(h.row.data(), G->g.row, sizeof(int64_t) * (G->g.n + 1), cudaMemcpyDeviceToHost));
+    if (G->g.m) GBC_CUDA(cudaMemcpy(h.col.data(), G->g.col, sizeof(int32_t) * G->g.m, cudaMemcpyDeviceToHost));
+    h.col.resize(G->g.m);
+    *n = G->g.n;
+    return export_csr(h, row, col);
+}
+
 gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t m, gbc_graph* out) {
     if (!out || !d_row || (m > 0 && !d_col) || n <= 0 || m < 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
     *out = nullptr;

@@ -34,6 +34,12 @@ size_t dev_cached_bytes();
 // cudaMemGetInfo's free bytes plus the cached ones.
 size_t dev_free_bytes();
 
+// Edge list on the device -> symmetric, deduplicated CSR without self-loops,
+// rows in ascending neighbour order (ingest.cu).  *d_row / *d_col are
+// cudaMalloc'd; *M = directed entries.
+gbc_status csr_from_edges_device(const int32_t* d_u, const int32_t* d_v, int64_t m, int32_t n, cudaStream_t s,
+                                 int64_t** d_row, int32_t** d_col, int64_t* M);
+
 // Device CSR (+ host-side component information for the GTEPS numerator).
 struct DevGraph {
     int32_t n = 0;

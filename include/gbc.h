@@ -116,6 +116,16 @@ gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, g
 gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, int32_t n,
                                    int64_t m_directed, gbc_graph* out);
 gbc_status gbc_graph_destroy(gbc_graph g);
+/* Device-side ingest: edge list (u[i], v[i]), i < m, ids in [0, n) -> the
+ * symmetric CSR without self-loops or repeated edges, rows in ascending
+ * neighbour order, built on the GPU (radix sort of both directions, unique,
+ * row offsets).  Replaces buildGraph + createCSR (Lib/AdjList/AdjList.c:13,
+ * Lib/CSR/CSR.c:9) for callers that hold an edge list.  _device takes device
+ * arrays; the host variant copies them first. */
+gbc_status gbc_graph_from_edges(const int32_t* u, const int32_t* v, int64_t m, int32_t n, gbc_graph* out);
+gbc_status gbc_graph_from_edges_device(const int32_t* d_u, const int32_t* d_v, int64_t m, int32_t n, gbc_graph* out);
+/* The graph's CSR copied to malloc'd host arrays (free with gbc_free). */
+gbc_status gbc_graph_export(gbc_graph g, int64_t** row, int32_t** col, int32_t* n);
 gbc_status gbc_graph_info(gbc_graph g, int32_t* n, int64_t* m_directed, size_t* device_bytes);
 /* Statistics of the last compute call on this graph. */
 gbc_status gbc_graph_last_stats(gbc_graph g, gbc_run_stats* st);

@@ -197,3 +197,53 @@ def test_autotune_choices_and_results(gpu, orc):
         ch2 = G.autotune(src)
         assert ch2["light_steps"] in (0, 8, 16, 32)
         assert np.array_equal(G.cc(src), orc.cc(og, src))
+
+
+def _canonical_csr(u, v, n):
+    """Symmetric CSR without self-loops or repeats, rows ascending (numpy)."""
+    a = np.concatenate([u, v]).astype(np.int64)
+    b = np.concatenate([v, u]).astype(np.int64)
+    keep = a != b
+    key = np.unique(a[keep] * n + b[keep])
+    row = np.concatenate([[0], np.cumsum(np.bincount(key // n, minlength=n))]).astype(np.int64)
+    return row, (key % n).astype(np.int32)
+
+
+@pytest.mark.parametrize("case", ["rmat", "grid", "er+noise", "empty", "datasets"])
+def test_device_ingest_matches_host_csr(gpu, orc, datasets, case):
+    """gbc_graph_from_edges builds on the GPU exactly the canonical CSR
+    (symmetric, no self-loops or repeats, rows ascending) from edge lists in
+    any order with repeats, reversed duplicates and self-loops."""
+    rng = np.random.default_rng(3)
+    if case == "datasets":
+        cases = [gpu.read_edgelist(p) for p in datasets.values()]
+    elif case == "rmat":
+        cases = [gpu.gen_rmat(15, 8, seed=2)]
+    elif case == "grid":
+        cases = [gpu.gen_grid(80, 90, 0.1, seed=5, largest_only=False)]
+    elif case == "er+noise":
+        cases = [gpu.gen_er(5000, 6.0, seed=9)]
+    else:
+        cases = [gpu.CSR(np.zeros(11, np.int64), np.zeros(0, np.int32))]
+    for csr in cases:
+        u = np.repeat(np.arange(csr.n, dtype=np.int32), np.diff(csr.row))
+        v = csr.col.copy()
+        if case == "er+noise":
+            extra = rng.integers(0, len(u), len(u) // 3)
+            loops = np.arange(0, csr.n, 50, dtype=np.int32)
+            u, v = np.concatenate([u, v[extra], loops]), np.concatenate([v, u[extra], loops])
+        perm = rng.permutation(len(u))
+        u, v = u[perm], v[perm]
+        row, col = _canonical_csr(u, v, csr.n)
+        if case in ("rmat", "grid", "er+noise"):
+            assert np.array_equal(row, csr.row)      # generators already emit the canonical form
+        with gpu.Graph.from_edges(u, v, csr.n) as G:
+            got = G.csr
+            assert got.n == csr.n
+            assert np.array_equal(got.row, row) and np.array_equal(got.col, col)
+            if 0 < csr.n <= 6000 and len(col):
+                src_s = np.arange(0, csr.n, max(1, csr.n // 64), dtype=np.int32)
+                og = orc.Graph(row, col)
+                assert np.array_equal(G.cc(src_s), orc.cc(og, src_s))
+    with pytest.raises(gpu.GbcError):
+        gpu.Graph.from_edges(np.array([0, 5], np.int32), np.array([1, 12], np.int32), 10)
