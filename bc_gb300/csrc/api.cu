@@ -30,6 +30,11 @@ struct gbc_graph_s {
     std::vector<int32_t> deg;
     int32_t* d_pos = nullptr;
     int64_t pos_cap = 0;
+    // internal ids are by descending degree: order[new] = old, inv[old] = new
+    int32_t* d_order = nullptr;
+    int32_t* d_inv = nullptr;
+    std::vector<int32_t> h_inv;
+    double* d_bc_out = nullptr;   // BC in the caller's ids (gbc_bc)
     // settings chosen by gbc_autotune; used where the options ask for autotuning
     struct {
         bool done = false;
@@ -43,6 +48,9 @@ struct gbc_graph_s {
         cudaFree(d_ccb);
         cudaFree(d_bc);
         cudaFree(d_pos);
+        cudaFree(d_order);
+        cudaFree(d_inv);
+        cudaFree(d_bc_out);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -256,6 +264,26 @@ static gbc_status resolve_sources(gbc_graph_s* G, const int32_t* sources, int32_
         for (int32_t i = 0; i < k; i++)
             if (hsrc[i] < 0 || hsrc[i] >= g.n) { set_error("source %d out of range [0,%d)", hsrc[i], g.n); return GBC_ERR_ARG; }
     }
+    for (auto& x : hsrc) x = G->h_inv[x];   // to internal ids
+    return GBC_OK;
+}
+
+// Caller's source ids (already range-checked) to internal ids.
+static void map_sources(const gbc_graph_s* G, std::vector<int32_t>& hsrc) {
+    for (auto& x : hsrc) x = G->h_inv[x];
+}
+
+// After the CSR is on the device: degree relabelling and the id maps.
+static gbc_status finish_graph(gbc_graph_s* G) {
+    GBC_TRY(relabel_by_degree(G->g, G->stream, &G->d_order, &G->d_inv));
+    G->h_inv.resize(G->g.n);
+    GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * G->g.n, cudaMemcpyDeviceToHost));
+    return GBC_OK;
+}
+
+static gbc_status ensure_bc_buffer(double** p, int32_t n) {
+    if (*p) return GBC_OK;
+    if (cudaMalloc(p, sizeof(double) * n) != cudaSuccess) { cudaGetLastError(); set_error("bc buffer"); return GBC_ERR_NOMEM; }
     return GBC_OK;
 }
 
@@ -397,6 +425,7 @@ gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, g
     GBC_TRY(ensure_device());
     auto G = std::make_unique<gbc_graph_s>();
     GBC_TRY(graph_upload(row, col, n, G.get()));
+    GBC_TRY(finish_graph(G.get()));
     *out = G.release();
     return GBC_OK;
 }
@@ -413,6 +442,7 @@ gbc_status gbc_graph_from_edges_device(const int32_t* d_u, const int32_t* d_v, i
     GBC_TRY(csr_from_edges_device(d_u, d_v, m, n, G->stream, &G->g.row, &G->g.col, &M));
     G->g.n = n;
     G->g.m = M;
+    GBC_TRY(finish_graph(G.get()));
     *out = G.release();
     return GBC_OK;
 }
@@ -444,14 +474,28 @@ gbc_status gbc_graph_from_edges(const int32_t* u, const int32_t* v, int64_t m, i
 gbc_status gbc_graph_export(gbc_graph G, int64_t** row, int32_t** col, int32_t* n) {
     if (!G || !row || !col || !n) { set_error("NULL argument"); return GBC_ERR_ARG; }
     std::lock_guard<std::mutex> lk(G->mu);
+    const int32_t nn = G->g.n;
+    std::vector<int64_t> irow((size_t)nn + 1);
+    std::vector<int32_t> icol(std::max<int64_t>(G->g.m, 1)), order(nn);
+    GBC_CUDA(cudaMemcpy(irow.data(), G->g.row, sizeof(int64_t) * (nn + 1), cudaMemcpyDeviceToHost));
+    if (G->g.m) GBC_CUDA(cudaMemcpy(icol.data(), G->g.col, sizeof(int32_t) * G->g.m, cudaMemcpyDeviceToHost));
+    GBC_CUDA(cudaMemcpy(order.data(), G->d_order, sizeof(int32_t) * nn, cudaMemcpyDeviceToHost));
+    // rows back in the caller's ids, ascending
     HostCSR h;
-    h.n = G->g.n;
-    h.row.resize((size_t)G->g.n + 1);
-    h.col.resize(std::max<int64_t>(G->g.m, 1));
-    GBC_CUDA(cudaMemcpy(h.row.data(), G->g.row, sizeof(int64_t) * (G->g.n + 1), cudaMemcpyDeviceToHost));
-    if (G->g.m) GBC_CUDA(cudaMemcpy(h.col.data(), G->g.col, sizeof(int32_t) * G->g.m, cudaMemcpyDeviceToHost));
+    h.n = nn;
+    h.row.assign((size_t)nn + 1, 0);
+    for (int32_t v = 0; v < nn; v++) {
+        const int32_t u = G->h_inv[v];
+        h.row[v + 1] = h.row[v] + (irow[u + 1] - irow[u]);
+    }
     h.col.resize(G->g.m);
-    *n = G->g.n;
+    for (int32_t v = 0; v < nn; v++) {
+        const int32_t u = G->h_inv[v];
+        int32_t* dst = h.col.data() + h.row[v];
+        for (int64_t j = irow[u]; j < irow[u + 1]; j++) *dst++ = order[icol[j]];
+        std::sort(h.col.data() + h.row[v], dst);
+    }
+    *n = nn;
     return export_csr(h, row, col);
 }
 
@@ -467,6 +511,7 @@ gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, i
     GBC_TRY(validate_csr(row.data(), col.data(), n));
     auto G = std::make_unique<gbc_graph_s>();
     GBC_TRY(graph_upload(row.data(), col.data(), n, G.get()));
+    GBC_TRY(finish_graph(G.get()));
     *out = G.release();
     return GBC_OK;
 }
@@ -509,17 +554,17 @@ gbc_status gbc_bc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     GBC_TRY(order_sources(G, o, true, hsrc, pos));
     GBC_TRY(upload_sources(G, hsrc));
     const int32_t kk = (int32_t)hsrc.size();
-    if (!G->d_bc) {
-        if (cudaMalloc(&G->d_bc, sizeof(double) * G->g.n) != cudaSuccess) { cudaGetLastError(); set_error("bc buffer"); return GBC_ERR_NOMEM; }
-    }
+    GBC_TRY(ensure_bc_buffer(&G->d_bc, G->g.n));
+    GBC_TRY(ensure_bc_buffer(&G->d_bc_out, G->g.n));
     LaneResult res;
     int32_t lanes = 0;
     int sig = 0;
     int64_t batches = 0;
     GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
     GBC_TRY(bc_core(G, G->d_src, kk, o, G->d_bc, res, lanes, sig, batches));
+    GBC_TRY(gather_to_caller<double>(G->d_bc, G->d_inv, G->g.n, 1, G->d_bc_out, G->stream));
     GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
-    GBC_CUDA(cudaMemcpyAsync(bc, G->d_bc, sizeof(double) * G->g.n, cudaMemcpyDeviceToHost, G->stream));
+    GBC_CUDA(cudaMemcpyAsync(bc, G->d_bc_out, sizeof(double) * G->g.n, cudaMemcpyDeviceToHost, G->stream));
     GBC_CUDA(cudaStreamSynchronize(G->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, G->ev0, G->ev1);
@@ -543,6 +588,7 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     GBC_CUDA(cudaStreamSynchronize(G->stream));
     for (int32_t i = 0; i < k; i++)
         if (hsrc[i] < 0 || hsrc[i] >= G->g.n) { set_error("source %d out of range [0,%d)", hsrc[i], G->g.n); return GBC_ERR_ARG; }
+    map_sources(G, hsrc);
     GBC_TRY(order_sources(G, o, true, hsrc, pos));
     GBC_TRY(upload_sources(G, hsrc));
     LaneResult res;
@@ -550,7 +596,9 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     int sig = 0;
     int64_t batches = 0;
     GBC_CUDA(cudaEventRecord(G->ev0, G->stream));
-    GBC_TRY(bc_core(G, G->d_src, k, o, d_bc, res, lanes, sig, batches));
+    GBC_TRY(ensure_bc_buffer(&G->d_bc, G->g.n));
+    GBC_TRY(bc_core(G, G->d_src, k, o, G->d_bc, res, lanes, sig, batches));
+    GBC_TRY(gather_to_caller<double>(G->d_bc, G->d_inv, G->g.n, 1, d_bc, G->stream));
     GBC_CUDA(cudaEventRecord(G->ev1, G->stream));
     GBC_CUDA(cudaStreamWaitEvent(us, G->ev1, 0));
     GBC_CUDA(cudaEventSynchronize(G->ev1));
@@ -699,6 +747,7 @@ gbc_status gbc_cc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     GBC_CUDA(cudaStreamSynchronize(G->stream));
     for (int32_t i = 0; i < k; i++)
         if (hsrc[i] < 0 || hsrc[i] >= G->g.n) { set_error("source %d out of range [0,%d)", hsrc[i], G->g.n); return GBC_ERR_ARG; }
+    map_sources(G, hsrc);
     GBC_TRY(order_sources(G, o, false, hsrc, pos));
     GBC_TRY(upload_sources(G, hsrc));
     if (k > G->ccb_cap) {
@@ -746,7 +795,7 @@ gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_op
     int32_t* d_dist = nullptr;
     uint64_t* d_sig = nullptr;
     const size_t cells = (size_t)std::min(lanes, k) * n;
-    if (cudaMalloc(&d_dist, cells * sizeof(int32_t)) != cudaSuccess || cudaMalloc(&d_sig, cells * sizeof(uint64_t)) != cudaSuccess) {
+    if (cudaMalloc(&d_dist, 2 * cells * sizeof(int32_t)) != cudaSuccess || cudaMalloc(&d_sig, 2 * cells * sizeof(uint64_t)) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(d_dist);
         set_error("sssp output buffers");
@@ -764,8 +813,11 @@ gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_op
         rq.d_sigma = d_sig;
         GBC_TRY(E->run(rq, res));
         const size_t c = (size_t)rq.kb * n;
-        if (dist) GBC_CUDA(cudaMemcpyAsync(dist + (size_t)b0 * n, d_dist, c * sizeof(int32_t), cudaMemcpyDeviceToHost, G->stream));
-        if (sigma) GBC_CUDA(cudaMemcpyAsync(sigma + (size_t)b0 * n, d_sig, c * sizeof(uint64_t), cudaMemcpyDeviceToHost, G->stream));
+        // per-vertex rows back to the caller's ids, through the second halves of the buffers
+        GBC_TRY(gather_to_caller<int32_t>(d_dist, G->d_inv, n, rq.kb, d_dist + cells, G->stream));
+        GBC_TRY(gather_to_caller<uint64_t>(d_sig, G->d_inv, n, rq.kb, d_sig + cells, G->stream));
+        if (dist) GBC_CUDA(cudaMemcpyAsync(dist + (size_t)b0 * n, d_dist + cells, c * sizeof(int32_t), cudaMemcpyDeviceToHost, G->stream));
+        if (sigma) GBC_CUDA(cudaMemcpyAsync(sigma + (size_t)b0 * n, d_sig + cells, c * sizeof(uint64_t), cudaMemcpyDeviceToHost, G->stream));
         GBC_CUDA(cudaStreamSynchronize(G->stream));
         if (ovf)
             for (int32_t l = 0; l < rq.kb; l++) ovf[b0 + l] = (res.ovf_bits[l >> 5] >> (l & 31)) & 1u;

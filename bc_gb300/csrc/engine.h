@@ -40,6 +40,14 @@ size_t dev_free_bytes();
 gbc_status csr_from_edges_device(const int32_t* d_u, const int32_t* d_v, int64_t m, int32_t n, cudaStream_t s,
                                  int64_t** d_row, int32_t** d_col, int64_t* M);
 
+struct DevGraph;
+// Reassign vertex ids by descending degree and rewrite the rows (relabel.cu).
+// g.row / g.col are replaced; *d_order[new] = old, *d_inv[old] = new.
+gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order, int32_t** d_inv);
+// out[r*n + v] = in[r*n + inv[v]], r < rows.
+template <typename T>
+gbc_status gather_to_caller(const T* d_in, const int32_t* d_inv, int32_t n, int64_t rows, T* d_out, cudaStream_t s);
+
 // Device CSR (+ host-side component information for the GTEPS numerator).
 struct DevGraph {
     int32_t n = 0;

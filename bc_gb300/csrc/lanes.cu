@@ -87,13 +87,14 @@ constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expande
 constexpr int FETCH = 32;       // regular entries a warp takes per fetch, one per thread
 constexpr int STG = 128;        // regular-queue entries a warp stages in shared memory per append
 constexpr int WARPS = BLOCK / 32;
-// Minimum resident CTAs per SM the level kernels are compiled for.  Deep
-// graphs (16-bit levels) have small, latency-bound levels and need 4 (64
-// registers); so do the wide-sigma variants, which would otherwise take over
-// 100 registers.  For exact sigma on 8-bit levels 0 leaves the choice to the
-// compiler, which also lands on 64 registers and measured 4-6% faster on
-// R-MAT scale 22 than forcing 4 or 5 (48 registers); unbounded (113+
-// registers, 2 CTAs) is 35% slower.
+// Minimum resident CTAs per SM of the forward kernels.  Deep graphs (16-bit
+// levels) have small, latency-bound levels and need 4 (64 registers); so do
+// the wide-sigma variants, which would otherwise take over 100 registers.
+// For exact sigma on 8-bit levels 0 leaves the choice to the compiler, which
+// also lands on 64 registers and measured 4-6% faster on R-MAT scale 22 than
+// forcing 4 or 5 (48 registers); unbounded (113+ registers, 2 CTAs) is 35%
+// slower.  The dependency sweep is always compiled for 4 (its compensated
+// sums would otherwise take 80 registers, 5% slower on R-MAT scale 22).
 template <typename LT, bool WIDE> constexpr int MINB = (sizeof(LT) == 2 || WIDE) ? 4 : 0;
 
 __device__ __forceinline__ size_t sidx(int g, int n, int v, int t) {
@@ -181,6 +182,29 @@ template <typename T>
 __device__ __forceinline__ T wterm(T mv, int ev, uint64_t r) {
     return pow2s(mv * wmant<T>(r), ev + wexp(r));
 }
+
+// Running sum of the dependency sweep: compensated (Neumaier) in FP32, so a
+// hub's sum over thousands of successor terms keeps FP32-ulp accuracy instead
+// of losing ~sqrt(terms) ulps; plain in FP64.
+template <typename T>
+struct Sum {
+    T s = T(0), c = T(0);
+    __device__ __forceinline__ void add(T x) {
+        if (sizeof(T) == 4) {
+            const T t = s + x;
+            c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+            s = t;
+        } else {
+            s += x;
+        }
+    }
+    // add another partial (its sum, then its carried compensation)
+    __device__ __forceinline__ void merge(T s2, T c2) {
+        add(s2);
+        c += c2;
+    }
+    __device__ __forceinline__ T value() const { return s + c; }
+};
 
 // ---- frontier appends ------------------------------------------------------
 // A warp stages the regular entries it discovers in shared memory and appends
@@ -454,7 +478,8 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
     using Sd = Simd<LT>;
     constexpr int LPW = Sd::LPW, WPV = 32 / LPW, SLOTS = 32 / WPV, ITER = 32 / SLOTS;
     constexpr unsigned PAIR = (LPW == 4) ? 0xFFFFu : 0xFFFFFFFFu;
-    __shared__ double part_a[WARPS][SLOTS][32];
+    __shared__ T part_s[WARPS][SLOTS][32];
+    __shared__ T part_c[WARPS][SLOTS][32];
     __shared__ int part_p[WARPS][SLOTS][32];
     const int t = threadIdx.x & 31, s = t / WPV, w = t % WPV, wib = threadIdx.x >> 5;
     const unsigned* lvw = reinterpret_cast<const unsigned*>(lv);
@@ -462,13 +487,12 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
     const unsigned act4 = Sd::eq(lvw[(size_t)v * WPV + w], d4);
     const T* rh = reinterpret_cast<const T*>(A.rho) + (gbase << 5) + w * LPW;
     const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho) + (gbase << 5) + w * LPW;
-    T a[LPW];
+    Sum<T> a[LPW];
     int pcs[LPW];
     T mj[LPW];
     int ej[LPW];
 #pragma unroll
     for (int j = 0; j < LPW; j++) {
-        a[j] = T(0);
         pcs[j] = 0;
         mj[j] = WIDE ? __shfl_sync(FULL, mvt, w * LPW + j) : T(0);
         ej[j] = WIDE ? __shfl_sync(FULL, evt, w * LPW + j) : 0;
@@ -500,7 +524,7 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
                 const float v4[4] = {vv.x, vv.y, vv.z, vv.w};
 #pragma unroll
                 for (int j = 0; j < LPW; j++)
-                    if (Sd::has(sm, j)) a[j] += (T)v4[j];
+                    if (Sd::has(sm, j)) a[j].add((T)v4[j]);
             } else {
 #pragma unroll
                 for (int pr = 0; pr < LPW / 2; pr++) {
@@ -511,19 +535,19 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
                         const uint64_t v2[2] = {vv.x, vv.y};
 #pragma unroll
                         for (int h = 0; h < 2; h++)
-                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += wterm<T>(mj[2 * pr + h], ej[2 * pr + h], v2[h]);
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h].add(wterm<T>(mj[2 * pr + h], ej[2 * pr + h], v2[h]));
                     } else if (sizeof(T) == 8) {
                         const double2 vv = *reinterpret_cast<const double2*>(reinterpret_cast<const double*>(rh) + xo + 2 * pr);
                         const double v2[2] = {vv.x, vv.y};
 #pragma unroll
                         for (int h = 0; h < 2; h++)
-                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h].add((T)v2[h]);
                     } else {
                         const float2 vv = *reinterpret_cast<const float2*>(rh + xo + 2 * pr);
                         const float v2[2] = {vv.x, vv.y};
 #pragma unroll
                         for (int h = 0; h < 2; h++)
-                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h] += (T)v2[h];
+                            if (Sd::has(sm, 2 * pr + h)) a[2 * pr + h].add((T)v2[h]);
                     }
                 }
             }
@@ -531,18 +555,21 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
     }
 #pragma unroll
     for (int j = 0; j < LPW; j++) {
-        part_a[wib][s][w * LPW + j] = (double)a[j];
+        part_s[wib][s][w * LPW + j] = a[j].s;
+        part_c[wib][s][w * LPW + j] = a[j].c;
         part_p[wib][s][w * LPW + j] = pcs[j];
     }
     __syncwarp();
-    T r = (T)part_a[wib][0][t];
+    Sum<T> r;
+    r.s = part_s[wib][0][t];
+    r.c = part_c[wib][0][t];
     int p = part_p[wib][0][t];
 #pragma unroll
     for (int k = 1; k < SLOTS; k++) {
-        r += (T)part_a[wib][k][t];
+        r.merge(part_s[wib][k][t], part_c[wib][k][t]);
         p += part_p[wib][k][t];
     }
-    acc = r;
+    acc = r.value();
     pc = p;
     __syncwarp();
 }
@@ -822,7 +849,7 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
             rem &= rem - 1u;
             const T mva = WIDE ? __shfl_sync(FULL, mv, a) : T(0);
             const int eva = WIDE ? __shfl_sync(FULL, ev, a) : 0;
-            T pacc = T(0);
+            Sum<T> ps;
             int ppc = 0;
             for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
                 const long long j = jb + t;
@@ -831,8 +858,7 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
                     const LT Lx = lv[((size_t)x << 5) + a];
                     if (Lx == dnext) {
                         const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                        if (WIDE) pacc += wterm<T>(mva, eva, rw[xi]);
-                        else pacc += rho[xi];
+                        ps.add(WIDE ? wterm<T>(mva, eva, rw[xi]) : rho[xi]);
                     } else if (Lx == dprev) {
                         ppc++;
                     }
@@ -840,10 +866,11 @@ __device__ __forceinline__ void bwd_scan(const KArgs& A, int d, size_t gbase, co
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                pacc += __shfl_xor_sync(FULL, pacc, o);
+                const T s2 = __shfl_xor_sync(FULL, ps.s, o), c2 = __shfl_xor_sync(FULL, ps.c, o);
+                ps.merge(s2, c2);
                 ppc += __shfl_xor_sync(FULL, ppc, o);
             }
-            if (t == a) { acc = pacc; pc = ppc; }
+            if (t == a) { acc = ps.value(); pc = ppc; }
         }
     }
 }
@@ -902,26 +929,25 @@ __device__ __forceinline__ void bwd_light(const KArgs& A, int d, uint32_t ent, u
             mv = wmant<T>(sw);
             ev = wexp(sw);
         }
-        T acc = T(0);
+        Sum<T> acc;
         int pc = 0;
         for (long long j = r0; j < r1; j++) {
             const int x = A.col[j];
             const LT Lx = lv[((size_t)x << 5) + a];
             if (Lx == dnext) {
                 const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                if (WIDE) acc += wterm<T>(mv, ev, rw[xi]);
-                else acc += rho[xi];
+                acc.add(WIDE ? wterm<T>(mv, ev, rw[xi]) : rho[xi]);
             } else if (Lx == dprev) {
                 pc++;
             }
         }
-        contrib += bwd_lane<WIDE, T>(A, g, gbase, v, a, mv, ev, acc, pc, refsem);
+        contrib += bwd_lane<WIDE, T>(A, g, gbase, v, a, mv, ev, acc.value(), pc, refsem);
     }
     A.bcg[gbase + v] += contrib;
 }
 
 template <bool WIDE, typename T, typename LT>
-__global__ void __launch_bounds__(BLOCK, (MINB<LT, WIDE>)) backward_kernel(KArgs A) {
+__global__ void __launch_bounds__(BLOCK, 4) backward_kernel(KArgs A) {
     __shared__ double h_acc[WARPS][32];
     __shared__ int h_pc[WARPS][32];
     __shared__ unsigned long long s_i;
