@@ -47,6 +47,7 @@ struct Reduction {
     std::vector<int32_t> core_w;      // reach of each core vertex
     std::unique_ptr<DevGraph> cdg;
     int32_t* d_cw = nullptr;
+    int32_t* d_cinv = nullptr;        // core id -> internal id of the degree-relabelled device core graph
     std::unique_ptr<LaneEngine> ceng;
     int32_t n_hub = 0;
     // connected components of the folded graph (alive vertices)
@@ -70,6 +71,7 @@ struct Reduction {
     // device copy of the block graph
     std::unique_ptr<DevGraph> dg;
     int32_t* d_w = nullptr;
+    std::vector<int32_t> b_inv;       // slot -> internal id of the degree-relabelled device block graph
     cudaStream_t stream = nullptr;
     std::unique_ptr<LaneEngine> eng;
     std::mutex mu;
@@ -80,6 +82,7 @@ struct Reduction {
         if (cdg) { cudaFree(cdg->row); cudaFree(cdg->col); }
         cudaFree(d_w);
         cudaFree(d_cw);
+        cudaFree(d_cinv);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -310,6 +313,24 @@ static gbc_status split(const int64_t* row, Reduction& R, const std::vector<int3
     return GBC_OK;
 }
 
+// Degree relabelling of a weighted device graph: the weights move with their
+// vertices; inv[old] = new on the host.
+static gbc_status relabel_weighted(DevGraph& g, cudaStream_t s, int32_t** d_w, std::vector<int32_t>& inv) {
+    inv.resize(g.n);
+    if (g.n == 0) return GBC_OK;
+    int32_t *d_order = nullptr, *d_inv = nullptr, *w2 = nullptr;
+    GBC_TRY(relabel_by_degree(g, s, &d_order, &d_inv));
+    std::unique_ptr<void, void (*)(void*)> f1(d_order, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_inv, [](void* p) { cudaFree(p); });
+    if (cudaMalloc(&w2, sizeof(int32_t) * g.n) != cudaSuccess) { cudaGetLastError(); set_error("weights"); return GBC_ERR_NOMEM; }
+    GBC_TRY(gather_to_caller<int32_t>(*d_w, d_order, g.n, 1, w2, s));   // w2[new] = w[order[new]]
+    GBC_CUDA(cudaMemcpyAsync(inv.data(), d_inv, sizeof(int32_t) * g.n, cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    cudaFree(*d_w);
+    *d_w = w2;
+    return GBC_OK;
+}
+
 static gbc_status upload(Reduction& R) {
     if (R.dg) return GBC_OK;
     int nd = 0;
@@ -325,6 +346,7 @@ static gbc_status upload(Reduction& R) {
     GBC_CUDA(cudaMemcpy(g->row, R.bg.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
     if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.bg.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
     GBC_CUDA(cudaMemcpy(R.d_w, R.slot_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
+    GBC_TRY(relabel_weighted(*g, R.stream, &R.d_w, R.b_inv));
     g->w = R.d_w;
     g->ff = nullptr;
     R.dg = std::move(g);
@@ -356,7 +378,7 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
     std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
     std::unique_ptr<void, void (*)(void*)> f2(d_cc, [](void* p) { cudaFree(p); });
     std::vector<int32_t> src(ns);
-    for (int32_t i = 0; i < ns; i++) src[i] = i;
+    for (int32_t i = 0; i < ns; i++) src[i] = R.b_inv[i];   // lane i holds slot i
     GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, R.stream));
     LaneResult res;
     for (int32_t b0 = 0; b0 < ns; b0 += lanes) {
@@ -465,6 +487,12 @@ static gbc_status core_upload(Reduction& R) {
     GBC_CUDA(cudaMemcpy(g->row, R.core.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
     if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.core.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
     if (g->n) GBC_CUDA(cudaMemcpy(R.d_cw, R.core_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
+    std::vector<int32_t> cinv;
+    GBC_TRY(relabel_weighted(*g, R.stream, &R.d_cw, cinv));
+    if (g->n) {
+        if (cudaMalloc(&R.d_cinv, sizeof(int32_t) * g->n) != cudaSuccess) { cudaGetLastError(); set_error("core id map"); return GBC_ERR_NOMEM; }
+        GBC_CUDA(cudaMemcpy(R.d_cinv, cinv.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
+    }
     g->w = R.d_cw;
     g->ff = nullptr;
     R.cdg = std::move(g);
@@ -520,7 +548,12 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
         if (st != GBC_OK) return st;
     }
     GBC_TRY(R.ceng->bc_finish(d_bc));
-    GBC_CUDA(cudaMemcpyAsync(out.data(), d_bc, sizeof(double) * nc, cudaMemcpyDeviceToHost, R.stream));
+    // core BC in internal ids -> core ids
+    double* d_bc2 = nullptr;
+    if (cudaMalloc(&d_bc2, sizeof(double) * nc) != cudaSuccess) { cudaGetLastError(); set_error("core buffers"); return GBC_ERR_NOMEM; }
+    std::unique_ptr<void, void (*)(void*)> f3(d_bc2, [](void* p) { cudaFree(p); });
+    GBC_TRY(gather_to_caller<double>(d_bc, R.d_cinv, nc, 1, d_bc2, R.stream));
+    GBC_CUDA(cudaMemcpyAsync(out.data(), d_bc2, sizeof(double) * nc, cudaMemcpyDeviceToHost, R.stream));
     GBC_CUDA(cudaStreamSynchronize(R.stream));
     return GBC_OK;
 }

@@ -43,12 +43,18 @@ struct SGraph {
     double** d_dst = nullptr;    // device table: lane group -> destination result vector
     cudaStream_t stream = nullptr;
     bool running = false;        // a worker holds this graph (its engine, buffers and stream)
+    // the device CSR is relabelled by descending degree: inv[caller id] = internal id
+    int32_t* d_order = nullptr;
+    int32_t* d_inv = nullptr;
+    std::vector<int32_t> h_inv;
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
         cudaFree(g.col);
         cudaFree(d_src);
         cudaFree(d_dst);
+        cudaFree(d_order);
+        cudaFree(d_inv);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -245,7 +251,7 @@ void gbc_server_s::run() {
         int32_t kb = 0;
         const bool bc_batch = kind > 0;
         for (auto& sl : slots) {
-            for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = sl.r->src[sl.first + i];
+            for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = G.h_inv[sl.r->src[sl.first + i]];
             for (int32_t gg = sl.lane0 / 32; gg < (sl.lane0 + sl.count + 31) / 32; gg++) hdst[gg] = sl.r->d_bc;
             kb = std::max(kb, ((sl.lane0 + sl.count + 31) / 32) * 32);
         }
@@ -369,6 +375,9 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     }
     GBC_CUDA(cudaMemcpy(G->g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     if (row[n]) GBC_CUDA(cudaMemcpy(G->g.col, col, sizeof(int32_t) * row[n], cudaMemcpyHostToDevice));
+    GBC_TRY(relabel_by_degree(G->g, G->stream, &G->d_order, &G->d_inv));
+    G->h_inv.resize(n);
+    GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
@@ -483,7 +492,19 @@ gbc_status gbc_server_fetch(gbc_server s, int64_t id, double* bc, int64_t* cc, d
         n = s->graphs[r->gid]->g.n;
     }
     if (latency_ms) *latency_ms = r->t_done - r->t_submit;
-    if (r->bc() && bc) GBC_CUDA(cudaMemcpy(bc, r->d_bc, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (r->bc() && bc) {
+        // the result accumulated in internal ids: gather to the caller's, through a scratch vector
+        double* tmp = nullptr;
+        if (cudaMalloc(&tmp, sizeof(double) * n) != cudaSuccess) { cudaGetLastError(); set_error("fetch buffer"); return GBC_ERR_NOMEM; }
+        std::unique_ptr<double, void (*)(double*)> ft(tmp, [](double* p) { cudaFree(p); });
+        const int32_t* d_inv = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            d_inv = s->graphs[r->gid]->d_inv;
+        }
+        GBC_TRY(gather_to_caller<double>(r->d_bc, d_inv, n, 1, tmp, 0));
+        GBC_CUDA(cudaMemcpy(bc, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
     if (!r->bc() && cc) std::memcpy(cc, r->cc.data(), sizeof(int64_t) * n);
     return GBC_OK;
 }
