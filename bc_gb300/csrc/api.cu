@@ -673,14 +673,18 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
     if (o.sparse_lanes < 0)
         for (int sp : {1, 4}) GBC_TRY(consider(sp, best_li, best_lp));
     if (o.levels_per_graph <= 0 && G->eng && G->eng->level_bytes() == 2) GBC_TRY(consider(best_sp, best_li, 64));
-    // batch width: half the lanes, compared per source
+    // batch width: halve while the time per source drops (down to 32 lanes)
     int32_t best_lanes = lanes;
-    if (o.lanes == 0 && lanes >= 64 && kb == lanes) {
-        double ms = 0;
-        const int32_t half = lanes / 2;
-        GBC_TRY(tune_batch(G, half, half, o, best_sp, best_li, best_lp, ms));   // warm-up of the narrower engine
-        GBC_TRY(tune_batch(G, half, half, o, best_sp, best_li, best_lp, ms));
-        if (2.0 * ms < best) best_lanes = half;
+    if (o.lanes == 0 && kb == lanes) {
+        double per_src = best / lanes;
+        for (int32_t w = lanes / 2; w >= 32; w /= 2) {
+            double ms = 0;
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, ms));   // warm-up of the narrower engine
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, ms));
+            if (ms / w >= per_src) break;
+            per_src = ms / w;
+            best_lanes = w;
+        }
     }
     G->tuned.done = true;
     G->tuned.lanes = o.lanes ? 0 : best_lanes;

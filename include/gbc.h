@@ -141,8 +141,9 @@ gbc_status gbc_bc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const
 /* Autotuner: time one betweenness batch of the given sources (k = 0: all
  * vertices) per candidate expansion setting -- one-thread task threshold
  * (light_steps 0/8/16/32), edge-parallel threshold (sparse_lanes 1/2/4), level
- * kernels per captured graph (16/64, deep graphs) and batch width (lanes, lanes/2),
- * one at a time -- and keep the fastest on the graph.  Later calls whose
+ * kernels per captured graph (16/64, deep graphs) and batch width (halved from the
+ * widest while the time per source drops, down to 32 lanes), one at a time -- and
+ * keep the fastest on the graph.  Later calls whose
  * options leave a setting to autotuning (-1 / 0) use the tuned value; values
  * set in the options are not tuned.  *chosen (nullable) receives the options
  * with the chosen settings filled in.  Results do not depend on the settings
