@@ -5,9 +5,10 @@
 // that create and destroy graph handles in a loop (the drop-in path builds a
 // CSR per call) would pay it every time.  Freed engine buffers therefore go to
 // a per-device cache and are handed to the next engine that asks for the same
-// size (or at most 25% less).  gbc_release_cached_memory() returns them to the
-// driver; a failed cudaMalloc also does, then retries.  Cached bytes count as
-// free when engines are sized (dev_free_bytes).
+// size (or at most 25% less).  At most 40% of the device's memory is kept
+// cached; past that, freed buffers go straight back.  gbc_release_cached_memory()
+// returns them to the driver; a failed cudaMalloc also does, then retries.
+// Cached bytes count as free when engines are sized (dev_free_bytes).
 #include <cuda_runtime.h>
 
 #include <map>
@@ -23,6 +24,7 @@ struct Cache {
     std::mutex mu;
     std::multimap<size_t, void*> blocks[64];   // per device: size -> block
     size_t bytes[64] = {};
+    size_t limit[64] = {};
 };
 
 Cache& cache() {
@@ -75,9 +77,21 @@ void dev_release(void* p, size_t bytes) {
     if (!p) return;
     if (bytes == 0) bytes = 1;
     Cache& c = cache();
-    std::lock_guard<std::mutex> lk(c.mu);
-    c.blocks[current_device()].emplace(bytes, p);
-    c.bytes[current_device()] += bytes;
+    const int d = current_device();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (c.limit[d] == 0) {
+            size_t fr = 0, tot = 0;
+            if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); tot = (size_t)16 << 30; }
+            c.limit[d] = tot / 5 * 2;   // at most 40% of the device stays cached
+        }
+        if (c.bytes[d] + bytes <= c.limit[d]) {
+            c.blocks[d].emplace(bytes, p);
+            c.bytes[d] += bytes;
+            return;
+        }
+    }
+    cudaFree(p);
 }
 
 size_t dev_cached_bytes() {
