@@ -199,3 +199,38 @@ def test_deep_graph_switches_level_width(gpu, orc):
         assert np.array_equal(G.cc(src), orc.cc(og, src))
         dist, _, _ = G.sssp(src)
         assert dist[0, 699] == 699
+
+
+def test_edge_cases(gpu, orc):
+    """A single vertex, isolated vertices, repeated sources, the all-sources
+    call and a hub that is not vertex 0 (the device relabels by degree) all
+    agree with the oracle."""
+    one = gpu.CSR(np.zeros(2, np.int64), np.zeros(0, np.int32))
+    with gpu.Graph(one) as G:
+        assert np.array_equal(G.bc(), np.zeros(1)) and np.array_equal(G.cc(), np.zeros(1, np.int64))
+        dist, sig, _ = G.sssp(np.array([0], np.int32))
+        assert dist[0, 0] == 0 and sig[0, 0] == 1
+    # path 0-1-2 plus isolated 3, and a star centred on the last vertex
+    n = 12
+    edges = [(0, 1), (1, 2)] + [(i, n - 1) for i in range(4, n - 1)]
+    u = np.array([a for a, b in edges] + [b for a, b in edges], np.int32)
+    v = np.array([b for a, b in edges] + [a for a, b in edges], np.int32)
+    o = np.lexsort((v, u))
+    row = np.concatenate([[0], np.cumsum(np.bincount(u, minlength=n))]).astype(np.int64)
+    csr = gpu.CSR(row, v[o])
+    og = to_orc(orc, csr)
+    for src in (np.array([0, 0, 3, n - 1, n - 1, 5], np.int32), np.arange(n, dtype=np.int32)):
+        ref, _ = orc.bc(og, src)
+        refr, _ = orc.bc(og, src, semantics=1)
+        with gpu.Graph(csr) as G:
+            assert relerr(G.bc(src), ref) < TOL_F64
+            assert relerr(G.bc(src, semantics=1, delta_precision=gpu.DELTA_F32), refr) < TOL_F32
+            assert np.array_equal(G.cc(src), orc.cc(og, src))
+            dist, sig, _ = G.sssp(src)
+            for i, s in enumerate(src):
+                d0, s0, _, _ = orc.sssp(og, int(s))
+                assert np.array_equal(dist[i], d0) and np.array_equal(sig[i], s0)
+    with gpu.Graph(csr) as G:
+        ref, _ = orc.bc(og, np.arange(n))
+        assert relerr(G.bc(), ref) < TOL_F64
+        assert np.array_equal(G.cc(), orc.cc(og, np.arange(n)))
