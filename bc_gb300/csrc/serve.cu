@@ -6,9 +6,9 @@
 // one of them at a time, on the graph's own stream, so batches of different
 // graphs overlap on the device and in the host gaps between level-loop
 // launches.  Each registered graph keeps its CSR in HBM and, while it has
-// work, one lane engine.  A lane batch is filled from every admitted request
-// on one graph that wants the same kind of sweep (closeness or betweenness),
-// oldest first; a request takes whole 32-lane groups, so its betweenness
+// work, one lane engine sized to its pending sources.  A lane batch is filled
+// from every admitted request on one graph that wants the same kind of sweep
+// (closeness or betweenness), oldest first; a request takes whole 32-lane groups, so its betweenness
 // partials stay separate and are added into its own FP64 result vector after
 // each batch.  Requests that arrive while a batch runs join the next batch.
 // Engines are created under an HBM budget and idle ones are released when a
@@ -117,12 +117,16 @@ struct gbc_server_s {
 
 namespace {
 
-// Engine for graph gi, making room under the budget by releasing the engines
-// of graphs that neither have pending work nor are held by a worker.
-gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy) {
+// Engine for graph gi, as wide as its pending sources need (up to max_lanes),
+// making room under the budget by releasing the engines of graphs that
+// neither have pending work nor are held by a worker.  A narrower engine is
+// replaced when more sources wait than it holds; its buffers go to the cache.
+gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy, int64_t pending) {
     SGraph& G = *S->graphs[gi];
-    if (G.eng) return GBC_OK;
-    int32_t lanes = S->max_lanes;
+    const int32_t want = (int32_t)std::min<int64_t>(S->max_lanes, std::max<int64_t>(32, (pending + 31) / 32 * 32));
+    if (G.eng && (G.eng->lanes() >= want || G.eng->lanes() >= S->max_lanes)) return GBC_OK;
+    G.eng.reset();
+    int32_t lanes = want;
     for (;;) {
         const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true);
         size_t used = S->engines_bytes();
@@ -207,7 +211,12 @@ void gbc_server_s::run() {
                 if (gi < 0) { cv_work.wait_for(lk, std::chrono::milliseconds(50)); continue; }
                 rr = gi + 1;
                 for (size_t j = 0; j < graphs.size(); j++) busy[j] = busy[j] || graphs[j]->running;
-                gbc_status st = ensure_engine(this, gi, busy);
+                int64_t pending = 0;
+                for (int64_t id : fifo) {
+                    Req* r = reqs[id].get();
+                    if (r->gid == gi && r->admitted) pending += (int64_t)(r->src.size() - r->next);
+                }
+                gbc_status st = ensure_engine(this, gi, busy, pending);
                 if (st != GBC_OK) {
                     for (int64_t id : fifo) {
                         Req* r = reqs[id].get();

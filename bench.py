@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
-    p.add_argument("--serve-rates", default="10,20,40,80", help="query arrival rates per second, comma-separated")
+    p.add_argument("--serve-rates", default="5,10,20", help="query arrival rates per second, comma-separated")
     p.add_argument("--no-serve", action="store_true")
     return p.parse_args()
 
@@ -178,18 +178,30 @@ def cpu_baseline(csr, sample, n_src, threads):
 
 
 def serving(G, seconds, rates, seed=11):
-    """Poisson streams of queries over device-resident graphs (a scaled-down
-    version of the 64-graph serving mix): exact CC on the small graphs,
-    k = 64 / 1024 sampled BC everywhere.  One stream per arrival rate, on the
-    same server; per rate the p50/p99 latency and the GTEPS delivered over
-    the stream's wall time (first arrival to last completion)."""
+    """The serving mix: a Poisson stream of queries over 64 device-resident
+    graphs of 1K-2M vertices (BA m=2-8, Erdos-Renyi average degree 4-32,
+    square grids, R-MAT scale 10-21; seeded sizes, log-uniform).  Queries:
+    exact CC and exact BC on the smaller graphs, k = 64 / 1024 sampled BC
+    everywhere.  One stream per arrival rate, on the same server; per rate the
+    p50/p99 latency and the GTEPS delivered over the stream's wall time
+    (first arrival to last completion)."""
     import ctypes as C
     import random
     L = G.lib()
-    specs = [("ba", G.gen_ba(4096, 2, 1)), ("ba", G.gen_ba(65536, 8, 2)), ("er", G.gen_er(32768, 4.0, 3)),
-             ("er", G.gen_er(131072, 32.0, 4)), ("grid", G.gen_grid(128, 128, 0.0, 5)),
-             ("rmat", G.gen_rmat(10, 16, seed=6)), ("rmat", G.gen_rmat(16, 16, seed=7)),
-             ("rmat", G.gen_rmat(18, 16, seed=8))]
+    grng = np.random.default_rng(5)
+    specs = []
+    for i in range(64):
+        n = int(np.exp(grng.uniform(np.log(1000), np.log(2_000_000))))
+        fam = i % 4
+        if fam == 0:
+            specs.append(("ba", G.gen_ba(n, int(grng.integers(2, 9)), i)))
+        elif fam == 1:
+            specs.append(("er", G.gen_er(n, float(grng.uniform(4, 32)), i)))
+        elif fam == 2:
+            side = max(8, int(np.sqrt(n)))
+            specs.append(("grid", G.gen_grid(side, side, 0.0, i)))
+        else:
+            specs.append(("rmat", G.gen_rmat(int(np.clip(round(np.log2(n)), 10, 21)), 16, seed=i)))
     cfg = G.ServerConfig()
     cfg.max_lanes = 1024
     h = C.c_void_p()
@@ -216,9 +228,11 @@ def serving(G, seconds, rates, seed=11):
             gi = rng.randrange(len(specs))
             n = specs[gi][1].n
             r = rng.random()
-            if r < 0.25 and n <= 32768:
+            if r < 0.15 and n <= 32768:
                 kind, k = G.Q_CC, 0
-            elif r < 0.7:
+            elif r < 0.25 and n <= 16384:
+                kind, k = G.Q_BC, 0
+            elif r < 0.65:
                 kind, k = G.Q_BC_SAMPLED, 64
             else:
                 kind, k = G.Q_BC_SAMPLED, 1024
@@ -249,8 +263,10 @@ def serving(G, seconds, rates, seed=11):
 
     points = [stream(r) for r in rates]
     L.gbc_server_destroy(h)
-    return {"graphs": len(specs), "workers": 4, "points": points,
-            "mix": "25% exact CC (graphs <= 32K vertices), 45% k=64 and 30% k=1024 sampled BC, uniform over graphs"}
+    return {"graphs": len(specs), "vertices": [min(c.n for _, c in specs), max(c.n for _, c in specs)],
+            "directed_entries": int(sum(c.m for _, c in specs)), "workers": 4, "points": points,
+            "mix": "uniform over graphs: 15% exact CC (graphs <= 32K vertices), 10% exact BC (<= 16K), "
+                   "40% k=64 and 35% k=1024 sampled BC"}
 
 
 def run_reference(args):
