@@ -3,17 +3,20 @@
 // B sources ("lanes") of one batch run level-synchronous BFS together.  Lane
 // state is lane-interleaved: for lane group g (32 lanes, one per warp thread)
 // and vertex v the 32 entries lvl/sigma/rho[g][v][0..31] are contiguous, so a
-// warp that visits a neighbour x touches one 64-byte (lvl) or 256-byte
-// (sigma, rho) segment for all 32 lanes of its group.  The frontier of level
-// d is a list of (vertex, group) entries; the lists of all levels are kept
-// (fq + foff) and replayed in reverse by the dependency sweep.
+// warp that visits a neighbour x touches one 32- or 64-byte (lvl, 8/16-bit)
+// and one 128/256-byte (sigma, rho) segment for all 32 lanes of its group.
+// The frontier of level d is a list of (vertex, group) entries; the lists of
+// all levels are kept (fq + foff) and replayed in reverse by the dependency
+// sweep.
 //
 // Forward, one kernel per level (expand): for every entry (v,g) of F_d and
 // every lane with lvl == d, pull sigma(v) from the level-(d-1) neighbours
 // (no atomics, deterministic) and discover level d+1 among the neighbours
-// (plain store of d+1, enqueue once per (x,g) via vmark).  A task whose active
-// lanes are few expands edge-parallel (threads over neighbours, lanes in
-// turn), otherwise lane-parallel (threads over lanes, neighbours in turn).
+// (plain store of d+1, enqueue once per (x,g) via vmark).  A task with little
+// work (active lanes x degree) is expanded by one thread, 32 tasks per warp; a
+// task whose active lanes are few expands edge-parallel (threads over
+// neighbours, lanes in turn); the rest lane-parallel (threads over lanes,
+// neighbours in turn).  Hubs (degree > 1024) take a whole CTA.
 // Backward, one kernel per level (pull): delta(v) = sigma(v) * sum over
 // successors w of rho(w), rho(v) = (1 + delta(v)) / sigma(v); per-group FP64
 // partials of BC accumulate without atomics.  Levels are read from a device

@@ -88,7 +88,7 @@ typedef struct {
     int64_t graph_launches;   /* CUDA graph launches in the last call */
     int64_t edges_traversed;  /* sum over sources of undirected edges in the source's component */
     int64_t frontier_entries; /* (vertex, lane-group) frontier entries over all levels */
-    int64_t sigma_overflow_lanes; /* lanes whose exact sigma overflowed (before any LOG re-run) */
+    int64_t sigma_overflow_lanes; /* lanes whose exact sigma overflowed (before any wide re-run) */
     double  kernel_ms;        /* device time of the traversal kernels (CUDA events) */
     double  total_ms;         /* wall time of the call */
     int32_t lanes;            /* lanes per batch actually used */
