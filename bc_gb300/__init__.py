@@ -36,7 +36,7 @@ class Options(C.Structure):
     _fields_ = [("semantics", C.c_int32), ("delta_precision", C.c_int32), ("sigma_mode", C.c_int32),
                 ("engine", C.c_int32), ("lanes", C.c_int32), ("sparse_lanes", C.c_int32),
                 ("levels_per_graph", C.c_int32), ("source_order", C.c_int32), ("light_steps", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("group_lanes", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class RunStats(C.Structure):
@@ -307,7 +307,7 @@ class Graph:
         p, k, keep = self._src(sources)
         ch = Options()
         check(lib().gbc_autotune(self.h, p, k, C.byref(options(**opt)), C.byref(ch)))
-        return {f: getattr(ch, f) for f in ("lanes", "sparse_lanes", "light_steps", "levels_per_graph")}
+        return {f: getattr(ch, f) for f in ("lanes", "sparse_lanes", "light_steps", "levels_per_graph", "group_lanes")}
 
     def cc(self, sources=None, **opt) -> np.ndarray:
         p, k, keep = self._src(sources)

@@ -28,6 +28,7 @@ struct gbc_graph_s {
     // lane assignment: per-vertex level-profile key and degree (computed once)
     std::vector<uint32_t> key;
     std::vector<int32_t> deg;
+    int32_t key_depth = 0;        // levels of that BFS (0: not run)
     int32_t* d_pos = nullptr;
     int64_t pos_cap = 0;
     // internal ids are by descending degree: order[new] = old, inv[old] = new
@@ -38,7 +39,7 @@ struct gbc_graph_s {
     // settings chosen by gbc_autotune; used where the options ask for autotuning
     struct {
         bool done = false;
-        int32_t lanes = 0, sparse = -1, light = -1, lpg = 0;
+        int32_t lanes = 0, sparse = -1, light = -1, lpg = 0, group = 0;
     } tuned;
     ~gbc_graph_s() {
         eng.reset();
@@ -129,20 +130,35 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (o.sigma_mode < GBC_SIGMA_AUTO || o.sigma_mode > GBC_SIGMA_WIDE) { set_error("bad sigma mode"); return GBC_ERR_ARG; }
     if (o.engine < GBC_ENGINE_AUTO || o.engine > GBC_ENGINE_LANES) { set_error("bad engine"); return GBC_ERR_ARG; }
     if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("lanes must be 0 or a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
+    if (o.group_lanes != 0 && o.group_lanes != 32 && o.group_lanes != 128) { set_error("group_lanes must be 0, 32 or 128"); return GBC_ERR_ARG; }
+    if (o.group_lanes == 128 && o.lanes % 128) { set_error("group_lanes 128 needs lanes = 0 or a multiple of 128"); return GBC_ERR_ARG; }
     return GBC_OK;
 }
 
 // Autotune lanes: as wide as the sources and the memory budget allow; an
 // existing engine that is wide enough is kept.
-static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested) {
+// Lanes per group of a call: the option, else the tuned value, else 128 on
+// small-world graphs (the source-ordering BFS from the hubs ended within 32
+// levels: sources grouped by level profile keep many lanes active per task;
+// R-MAT scale 22 BC 103 -> 126 GTEPS, closeness 258 -> 490 GTEPS) and 32
+// otherwise, where a task usually has one active lane and the one-thread light
+// path of 32-lane groups matters (grids, meshes, roads).
+static int32_t group_of(const gbc_graph_s* G, const gbc_options& o) {
+    if (o.group_lanes) return o.group_lanes;
+    if (G->tuned.done && G->tuned.group) return G->tuned.group;
+    return (G->key_depth > 0 && G->key_depth <= 32) ? 128 : 32;
+}
+
+static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested, int32_t group) {
     if (requested) return requested;
     const DevGraph& g = G->g;
-    int32_t lanes = (int32_t)std::min<int64_t>(G->tuned.lanes ? G->tuned.lanes : 1024, ((k + 31) / 32) * 32);
-    lanes = std::max(lanes, 32);
-    if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes) return G->eng->lanes();
+    int32_t lanes = (int32_t)std::min<int64_t>(G->tuned.lanes ? G->tuned.lanes : 1024, ((k + group - 1) / group) * group);
+    lanes = std::max(lanes, group);
+    if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes && G->eng->group_lanes() == group)
+        return G->eng->lanes();
     const size_t fr = dev_free_bytes();
     const size_t budget = (fr + (G->eng ? G->eng->device_bytes() : 0)) / 2;
-    while (lanes > 32 && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= 32;
+    while (lanes > group && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= group;
     return lanes;
 }
 
@@ -158,14 +174,15 @@ static void tuning_of(const gbc_graph_s* G, const gbc_options& o, int& sparse, i
 static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
     int sparse, light, lpg;
     tuning_of(G, o, sparse, light, lpg);
-    if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc)) {
+    const int32_t group = (lanes % 128 == 0) ? group_of(G, o) : 32;
+    if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc) && G->eng->group_lanes() == group) {
         G->eng->set_tuning(sparse, light, lpg);
         *out = G->eng.get();
         return GBC_OK;
     }
     G->eng.reset();
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G->g, lanes, bc, sparse, lpg, G->stream));
+    GBC_TRY(e->init(&G->g, lanes, bc, sparse, lpg, G->stream, group));
     e->set_tuning(sparse, light, lpg);
     G->eng = std::move(e);
     *out = G->eng.get();
@@ -174,9 +191,12 @@ static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_o
 
 // Level-profile key of every vertex: one forward batch from the 32 highest-
 // degree vertices; key = (level from the top vertex, nearest of the others).
-static gbc_status ensure_order_key(gbc_graph_s* G, LaneEngine* E) {
+static gbc_status ensure_order_key(gbc_graph_s* G) {
     if (!G->key.empty()) return GBC_OK;
     const DevGraph& g = G->g;
+    // its own narrow engine: the main engine's group width depends on the depth found here
+    LaneEngine E;
+    GBC_TRY(E.init(&g, 32, false, -1, 0, G->stream, 32));
     std::vector<int64_t> row(g.n + 1);
     GBC_CUDA(cudaMemcpy(row.data(), g.row, sizeof(int64_t) * (g.n + 1), cudaMemcpyDeviceToHost));
     G->deg.resize(g.n);
@@ -203,7 +223,8 @@ static gbc_status ensure_order_key(gbc_graph_s* G, LaneEngine* E) {
     rq.kb = kb;
     rq.d_profile_key = d_key;
     LaneResult res;
-    GBC_TRY(E->run(rq, res));
+    GBC_TRY(E.run(rq, res));
+    G->key_depth = (int32_t)res.levels;
     G->key.resize(g.n);
     GBC_CUDA(cudaMemcpyAsync(G->key.data(), d_key, sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, G->stream));
     GBC_CUDA(cudaStreamSynchronize(G->stream));
@@ -219,9 +240,7 @@ static gbc_status order_sources(gbc_graph_s* G, const gbc_options& o, bool bc, s
     pos.resize(k);
     for (int64_t i = 0; i < k; i++) pos[i] = (int32_t)i;
     if (o.engine == GBC_ENGINE_PLAIN || o.source_order != 0 || k <= 32) return GBC_OK;
-    LaneEngine* E = nullptr;
-    GBC_TRY(get_engine(G, pick_lanes(G, k, bc, o.lanes), bc, o, &E));
-    GBC_TRY(ensure_order_key(G, E));
+    GBC_TRY(ensure_order_key(G));
     const std::vector<uint32_t>& key = G->key;
     const std::vector<int32_t>& deg = G->deg;
     std::stable_sort(pos.begin(), pos.end(), [&](int32_t a, int32_t b) {
@@ -329,7 +348,7 @@ static gbc_status bc_core(gbc_graph_s* G, const int32_t* d_src, int32_t k, const
         }
         return GBC_OK;
     }
-    const int32_t lanes = pick_lanes(G, k, true, o.lanes);
+    const int32_t lanes = pick_lanes(G, k, true, o.lanes, group_of(G, o));
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, true, o, &E));
     lanes_used = lanes;
@@ -371,7 +390,7 @@ static gbc_status cc_core(gbc_graph_s* G, const int32_t* d_src, const int32_t* h
         batches = k;
         return GBC_OK;
     }
-    const int32_t lanes = pick_lanes(G, k, false, o.lanes);
+    const int32_t lanes = pick_lanes(G, k, false, o.lanes, group_of(G, o));
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, false, o, &E));
     lanes_used = lanes;
@@ -416,6 +435,7 @@ void gbc_options_default(gbc_options* o) {
     o->levels_per_graph = 0;
     o->source_order = 0;
     o->light_steps = -1;
+    o->group_lanes = 0;
 }
 
 gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, gbc_graph* out) {
@@ -611,9 +631,11 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
 // Device time (forward + dependency sweep) of one betweenness batch of the
 // staged sources d_src[0..kb) with the given expansion settings.
 static gbc_status tune_batch(gbc_graph_s* G, int32_t lanes, int32_t kb, const gbc_options& o, int sparse, int light,
-                             int lpg, double& ms) {
+                             int lpg, int group, double& ms) {
     LaneEngine* E = nullptr;
-    GBC_TRY(get_engine(G, lanes, true, o, &E));
+    gbc_options og = o;
+    og.group_lanes = group;
+    GBC_TRY(get_engine(G, lanes, true, og, &E));
     E->set_tuning(sparse, light, lpg);
     GBC_TRY(E->bc_begin());
     LaneRequest rq;
@@ -649,24 +671,32 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
     G->tuned.done = false;
     const int32_t k0 = (int32_t)hsrc.size();
-    int32_t lanes = pick_lanes(G, k0, true, o.lanes);
+    int32_t lanes = pick_lanes(G, k0, true, o.lanes, group_of(G, o));
     GBC_TRY(order_sources(G, o, true, hsrc, pos));
     GBC_TRY(upload_sources(G, hsrc));
     // candidate settings; the options' explicit values are kept fixed
     const int sp0 = o.sparse_lanes >= 0 ? o.sparse_lanes : 2;
     const int li0 = o.light_steps >= 0 ? o.light_steps : 16;
     const int lp0 = o.levels_per_graph > 0 ? o.levels_per_graph : 16;
-    int best_sp = sp0, best_li = li0, best_lp = lp0;
+    const int gr0 = o.group_lanes ? o.group_lanes : 32;
+    int best_sp = sp0, best_li = li0, best_lp = lp0, best_gr = gr0;
     double best = 0;
     const int32_t kb = std::min(lanes, k0);
-    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, best));   // warm-up: level width, queue size, graph capture
-    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, best));
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, best));   // warm-up: level width, queue size, graph capture
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, best));
     auto consider = [&](int sp, int li, int lp) -> gbc_status {
         double ms = 0;
-        GBC_TRY(tune_batch(G, lanes, kb, o, sp, li, lp, ms));
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp, li, lp, best_gr, ms));
         if (ms < best) { best = ms; best_sp = sp; best_li = li; best_lp = lp; }
         return GBC_OK;
     };
+    // lanes per group first: 128-lane groups (four lanes per thread) against 32
+    if (o.group_lanes == 0 && lanes % 128 == 0) {
+        double ms = 0;
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, ms));   // warm-up of the 128-lane engine
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, ms));
+        if (ms < best) { best = ms; best_gr = 128; }
+    }
     // one-thread tasks, then the edge-parallel threshold, then the level-loop graph length
     if (o.light_steps < 0)
         for (int li : {0, 8, 32}) GBC_TRY(consider(best_sp, li, best_lp));
@@ -679,8 +709,9 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         double per_src = best / lanes;
         for (int32_t w = lanes / 2; w >= 32; w /= 2) {
             double ms = 0;
-            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, ms));   // warm-up of the narrower engine
-            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, ms));
+            const int gw = (w % 128 == 0) ? best_gr : 32;
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, ms));   // warm-up of the narrower engine
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, ms));
             if (ms / w >= per_src) break;
             per_src = ms / w;
             best_lanes = w;
@@ -691,12 +722,14 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
     G->tuned.sparse = best_sp;
     G->tuned.light = best_li;
     G->tuned.lpg = best_lp;
+    G->tuned.group = best_gr;
     if (chosen) {
         *chosen = o;
         chosen->lanes = best_lanes;
         chosen->sparse_lanes = best_sp;
         chosen->light_steps = best_li;
         chosen->levels_per_graph = best_lp;
+        chosen->group_lanes = best_gr;
     }
     return GBC_OK;
 }
@@ -793,7 +826,8 @@ gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_op
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
     GBC_TRY(upload_sources(G, hsrc));
     const int32_t n = G->g.n;
-    const int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((k + 31) / 32) * 32);
+    const int32_t grp = group_of(G, o);
+    const int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((k + grp - 1) / grp) * grp);
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, true, o, &E));
     int32_t* d_dist = nullptr;

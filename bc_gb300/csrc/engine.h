@@ -100,8 +100,9 @@ public:
     LaneEngine(const LaneEngine&) = delete;
     LaneEngine& operator=(const LaneEngine&) = delete;
     // Allocate lane state for `lanes` (multiple of 32, <= 1024) on graph g.
+    // group_lanes: sources per lane group (32: one per warp thread; 128: four per thread).
     gbc_status init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
-                    cudaStream_t stream);
+                    cudaStream_t stream, int group_lanes = 32);
     // Expansion tuning (negative = default).  A change drops the captured
     // level-loop graphs, which hold the old values.
     void set_tuning(int sparse_lanes, int light_steps, int levels_per_graph);
@@ -115,6 +116,7 @@ public:
     // Per-lane distance sums of the last CC batch (lanes entries) to the host.
     gbc_status cc_read(unsigned long long* h_cc, int32_t count);
     int32_t lanes() const { return lanes_; }
+    int32_t group_lanes() const { return 1 << gs_; }
     int level_bytes() const { return lvl_bytes_; }
     bool has_bc() const { return need_bc_; }
     const DevGraph* graph() const { return g_; }
@@ -131,6 +133,7 @@ private:
 
     const DevGraph* g_ = nullptr;
     int32_t lanes_ = 0, ng_ = 0;
+    int gs_ = 5;          // lanes per group = 1 << gs_
     bool need_bc_ = false;
     int sparse_ = 2;
     int light_ = 16;

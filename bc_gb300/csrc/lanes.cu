@@ -84,6 +84,7 @@ struct KArgs {
     int sparse;            // entries with <= sparse active lanes expand edge-parallel
     int light;             // entries with (active lanes x degree) <= light expand one per thread
     int semantics;
+    int gs;                // lanes per group = 1 << gs (5: 32 lanes, one per thread; 7: 128, four per thread)
 };
 
 constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expanded by a whole CTA
@@ -100,8 +101,8 @@ constexpr int WARPS = BLOCK / 32;
 // sums would otherwise take 80 registers, 5% slower on R-MAT scale 22).
 template <typename LT, bool WIDE> constexpr int MINB = (sizeof(LT) == 2 || WIDE) ? 4 : 0;
 
-__device__ __forceinline__ size_t sidx(int g, int n, int v, int t) {
-    return ((((size_t)g * (size_t)n) + (size_t)v) << 5) + (size_t)t;
+__device__ __forceinline__ size_t sidx(int g, int n, int v, int t, int gs) {
+    return ((((size_t)g * (size_t)n) + (size_t)v) << gs) + (size_t)t;
 }
 
 __device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > HUB_DEG; }
@@ -1040,14 +1041,576 @@ __global__ void __launch_bounds__(BLOCK, 4) backward_kernel(KArgs A) {
     }
 }
 
+// ---- 128-lane groups ---------------------------------------------------------
+// A lane group of 128 sources: thread t of a warp owns lanes 4t..4t+3, so one
+// warp-wide load of a neighbour's level row (128 B with 8-bit levels) serves
+// the whole group, and a thread keeps its four lanes' sums to itself (no
+// cross-thread combine).  With lanes that move together (sources grouped by
+// level profile on a power-law graph), 128-lane groups carry the same work
+// in about 0.3x the frontier entries and neighbour visits of 32-lane groups.
+
+// The four levels of lanes 4t..4t+3 in one row, and 4-bit lane masks of them.
+template <typename LT> struct Quad;
+template <> struct Quad<uint8_t> {
+    unsigned w;
+    __device__ static __forceinline__ Quad load(const uint8_t* row, int t) {
+        return {reinterpret_cast<const unsigned*>(row)[t]};
+    }
+    __device__ static __forceinline__ Quad none() { return {0xFFFFFFFFu}; }
+    __device__ static __forceinline__ unsigned bits(unsigned m) { return ((m & 0x80808080u) * 0x00204081u) >> 28; }
+    __device__ __forceinline__ unsigned eq(int d) const { return bits(__vcmpeq4(w, Simd<uint8_t>::bc(d))); }
+    __device__ __forceinline__ unsigned gt(int d) const { return bits(__vcmpgtu4(w, Simd<uint8_t>::bc(d))); }
+    __device__ __forceinline__ unsigned unreached() const { return bits(__vcmpeq4(w, 0xFFFFFFFFu)); }
+};
+template <> struct Quad<uint16_t> {
+    uint2 w;
+    __device__ static __forceinline__ Quad load(const uint16_t* row, int t) {
+        return {reinterpret_cast<const uint2*>(row)[t]};
+    }
+    __device__ static __forceinline__ Quad none() { return {make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu)}; }
+    __device__ static __forceinline__ unsigned bits(unsigned m) { return ((m & 0x80008000u) * 0x8001u) >> 30; }
+    __device__ __forceinline__ unsigned eq(int d) const {
+        const unsigned b = Simd<uint16_t>::bc(d);
+        return bits(__vcmpeq2(w.x, b)) | (bits(__vcmpeq2(w.y, b)) << 2);
+    }
+    __device__ __forceinline__ unsigned gt(int d) const {
+        const unsigned b = Simd<uint16_t>::bc(d);
+        return bits(__vcmpgtu2(w.x, b)) | (bits(__vcmpgtu2(w.y, b)) << 2);
+    }
+    __device__ __forceinline__ unsigned unreached() const {
+        return bits(__vcmpeq2(w.x, 0xFFFFFFFFu)) | (bits(__vcmpeq2(w.y, 0xFFFFFFFFu)) << 2);
+    }
+};
+
+constexpr int Q_ITER = 8;   // neighbours whose level quads are loaded before any is used
+
+// Forward scan of one (v, g) task over neighbour chunks r0 + 32*sub, step
+// 32*nsub: thread t pulls sigma for its active lanes (act4) and discovers
+// level d+1.  Results stay in the thread: acc/ofm (exact) or ws/we (wide).
+template <int MODE, typename LT>
+__device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, unsigned act4,
+                                           long long r0, long long r1, int sub, int nsub, uint64_t (&acc)[4],
+                                           unsigned& ofm, int (&we)[4], double (&ws)[4]) {
+    const int t = threadIdx.x & 31;
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+        const int cnt = (int)min(32LL, r1 - jb);
+        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        for (int k0 = 0; k0 < cnt; k0 += Q_ITER) {          // uniform across the warp
+            Quad<LT> q[Q_ITER];
+            int xs[Q_ITER];
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                xs[i] = __shfl_sync(FULL, xm, (k0 + i) & 31);
+                q[i] = (k0 + i < cnt && act4) ? Quad<LT>::load(lv + ((size_t)xs[i] << 7), t) : Quad<LT>::none();
+            }
+            if (MODE != 0 && d > 0) {
+#pragma unroll
+                for (int i = 0; i < Q_ITER; i++) {
+                    const unsigned pm = (k0 + i < cnt) ? (q[i].eq(d - 1) & act4) : 0u;
+                    if (!pm) continue;
+                    const uint64_t* sg = A.sig + ((gbase + (size_t)xs[i]) << 7) + 4 * t;
+#pragma unroll
+                    for (int pr = 0; pr < 2; pr++) {
+                        if (!((pm >> (2 * pr)) & 3u)) continue;
+                        const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(sg + 2 * pr);
+                        const uint64_t v2[2] = {vv.x, vv.y};
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const int j = 2 * pr + h;
+                            if (!((pm >> j) & 1u)) continue;
+                            if (MODE == 1) {
+                                const uint64_t na = acc[j] + v2[h];
+                                ofm |= (unsigned)(na < acc[j]) << j;
+                                acc[j] = na;
+                            } else {
+                                wadd(ws[j], we[j], v2[h]);
+                            }
+                        }
+                    }
+                }
+            }
+            // discovery: store d+1 in the unreached active lanes; thread i claims neighbour i
+            unsigned want = 0;
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                const bool inr = k0 + i < cnt;
+                const unsigned un = inr ? (q[i].unreached() & act4) : 0u;
+                if (un) {
+                    LT* px = lv + ((size_t)xs[i] << 7) + 4 * t;
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if ((un >> j) & 1u) px[j] = (LT)(d + 1);
+                }
+                const unsigned gm = inr ? (q[i].gt(d) & act4) : 0u;
+                if (__ballot_sync(FULL, gm != 0u)) want |= 1u << i;
+            }
+            const int xi = __shfl_sync(FULL, xm, (k0 + (t & (Q_ITER - 1))) & 31);
+            const bool has = (t < Q_ITER) && ((want >> t) & 1u) && claim(A, gbase, xi, d + 1);
+            warp_append(A, S, has, has && is_hub(A, xi), ((uint32_t)xi << 5) | (uint32_t)g);
+        }
+    }
+}
+
+// Store sigma of thread t's active lanes of (v, g); flag lanes past the range.
+template <int MODE>
+__device__ __forceinline__ void q_fwd_store(const KArgs& A, int g, size_t gbase, int v, unsigned act4,
+                                            const uint64_t (&acc)[4], unsigned ofm, const int (&we)[4],
+                                            const double (&ws)[4]) {
+    const int t = threadIdx.x & 31;
+    uint64_t* sv = A.sig + ((gbase + (size_t)v) << 7) + 4 * t;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (!((act4 >> j) & 1u)) continue;
+        bool of = (ofm >> j) & 1u;
+        sv[j] = MODE == 2 ? wpack(ws[j], we[j], of) : acc[j];
+        if (of) {
+            const int lane = (g << 7) + 4 * t + j;
+            atomicOr(&A.ovf[lane >> 5], 1u << (lane & 31));
+            A.ctl->any_ovf = 1;
+        }
+    }
+}
+
+// Edge-parallel forward for tasks with few active lanes: threads over
+// neighbours, one active lane at a time; the lane's owner keeps the sum.
+template <int MODE, typename LT>
+__device__ __forceinline__ void q_fwd_edges(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, unsigned act4,
+                                            long long r0, long long r1, int sub, int nsub, uint64_t (&acc)[4],
+                                            unsigned& ofm, int (&we)[4], double (&ws)[4]) {
+    constexpr LT INF = (LT)Lv<LT>::INF;
+    const int t = threadIdx.x & 31;
+    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        unsigned owners = __ballot_sync(FULL, (act4 >> j) & 1u);
+        while (owners) {
+            const int o = __ffs(owners) - 1;
+            owners &= owners - 1u;
+            const int a = 4 * o + j;
+            uint64_t pacc = 0;
+            bool pof = false;
+            int pe = WEMPTY;
+            double ps = 0.0;
+            for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+                const long long jj = jb + t;
+                bool has = false;
+                int x = 0;
+                if (jj < r1) {
+                    x = A.col[jj];
+                    LT* px = lv + ((size_t)x << 7) + a;
+                    const LT Lx = *px;
+                    if (MODE != 0 && d > 0 && Lx == dprev) {
+                        const uint64_t sv = A.sig[((gbase + (size_t)x) << 7) + a];
+                        if (MODE == 1) {
+                            const uint64_t na = pacc + sv;
+                            pof |= (na < pacc);
+                            pacc = na;
+                        } else {
+                            wadd(ps, pe, sv);
+                        }
+                    }
+                    if (Lx > dl) {
+                        if (Lx == INF) *px = dnext;
+                        has = claim(A, gbase, x, d + 1);
+                    }
+                }
+                warp_append(A, S, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
+            }
+            if (MODE == 1) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const uint64_t p2 = __shfl_xor_sync(FULL, pacc, off);
+                    const int f2 = __shfl_xor_sync(FULL, (int)pof, off);
+                    const uint64_t na = pacc + p2;
+                    pof = pof || f2 || (na < pacc);
+                    pacc = na;
+                }
+                if (t == o) {
+                    acc[j] = pacc;
+                    ofm |= (unsigned)pof << j;
+                }
+            } else if (MODE == 2) {
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const int e2 = __shfl_xor_sync(FULL, pe, off);
+                    const double s2 = __shfl_xor_sync(FULL, ps, off);
+                    wmerge(ps, pe, s2, e2);
+                }
+                if (t == o) { we[j] = pe; ws[j] = ps; }
+            }
+        }
+    }
+}
+
+template <int MODE, typename LT>
+__device__ __forceinline__ void q_cc_add(const KArgs& A, unsigned long long* cc_sh, int d, int g, int v, unsigned act4) {
+    if (MODE != 0 || !act4) return;
+    const int t = threadIdx.x & 31;
+    const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if ((act4 >> j) & 1u) atomicAdd(&cc_sh[(g << 7) + 4 * t + j], (unsigned long long)c);
+}
+
+// Forward level kernel, 128-lane groups.
+template <int MODE, typename LT>
+__global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
+    __shared__ unsigned long long cc_sh[MODE == 0 ? 1024 : 1];
+    __shared__ uint64_t h_acc[MODE != 0 ? WARPS : 1][128];
+    __shared__ double h_ws[MODE == 2 ? WARPS : 1][128];
+    __shared__ unsigned char h_of[MODE != 0 ? WARPS : 1][128];
+    __shared__ uint32_t stg[WARPS][STG];
+    __shared__ unsigned long long s_i;
+    if (MODE == 0) {
+        for (int i = threadIdx.x; i < (A.ng << 7); i += blockDim.x) cc_sh[i] = 0ULL;
+        __syncthreads();
+    }
+    const int done = *(volatile int*)&A.ctl->done;
+    const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    Stage S{stg[wib], 0};
+    if (!done) {
+        // hub entries: one CTA per entry, warps split the neighbours
+        const unsigned long long he = A.hoff[d + 1];
+        for (;;) {
+            if (threadIdx.x == 0) s_i = atomicAdd(&A.ctl->hnext, 1ULL);
+            __syncthreads();
+            const unsigned long long i = s_i;
+            __syncthreads();
+            if (i >= he) break;
+            const uint32_t ent = A.hq[i];
+            const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+            const size_t gbase = (size_t)g * (size_t)A.n;
+            LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 7);
+            const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+            const int nact = __reduce_add_sync(FULL, __popc(act4));
+            if (nact == 0) continue;   // uniform across the CTA
+            if (wib == 0) q_cc_add<MODE, LT>(A, cc_sh, d, g, v, act4);
+            uint64_t acc[4] = {0, 0, 0, 0};
+            unsigned ofm = 0;
+            int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
+            double ws[4] = {0.0, 0.0, 0.0, 0.0};
+            if (nact > A.sparse) q_fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
+            else q_fwd_edges<MODE, LT>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
+            if (MODE != 0) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int l = 4 * t + j;
+                    if (MODE == 1) h_acc[wib][l] = acc[j];
+                    else { h_acc[wib][l] = (uint64_t)(long long)we[j]; h_ws[wib][l] = ws[j]; }
+                    h_of[wib][l] = (ofm >> j) & 1u;
+                }
+                __syncthreads();
+                if (wib == 0 && act4 && d > 0) {
+                    for (int w = 1; w < WARPS; w++) {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int l = 4 * t + j;
+                            if (MODE == 1) {
+                                const uint64_t na = acc[j] + h_acc[w][l];
+                                ofm |= (unsigned)(h_of[w][l] || (na < acc[j])) << j;
+                                acc[j] = na;
+                            } else {
+                                wmerge(ws[j], we[j], h_ws[w][l], (int)(long long)h_acc[w][l]);
+                            }
+                        }
+                    }
+                    q_fwd_store<MODE>(A, g, gbase, v, act4, acc, ofm, we, ws);
+                }
+                __syncthreads();
+            }
+        }
+        // regular entries: a warp takes FETCH at a time and expands them in turn
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const unsigned long long my = base + t;
+            const uint32_t ment = my < e ? A.fq[my] : 0u;
+            const long long m0 = my < e ? A.row[ment >> 5] : 0, m1 = my < e ? A.row[(ment >> 5) + 1] : 0;
+            const int cntE = (int)min((unsigned long long)FETCH, e - base);
+            for (int k = 0; k < cntE; k++) {
+                const uint32_t ent = __shfl_sync(FULL, ment, k);
+                const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
+                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+                const size_t gbase = (size_t)g * (size_t)A.n;
+                LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 7);
+                const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+                const int nact = __reduce_add_sync(FULL, __popc(act4));
+                if (nact == 0) continue;
+                q_cc_add<MODE, LT>(A, cc_sh, d, g, v, act4);
+                uint64_t acc[4] = {0, 0, 0, 0};
+                unsigned ofm = 0;
+                int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
+                double ws[4] = {0.0, 0.0, 0.0, 0.0};
+                if (nact > A.sparse) q_fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
+                else q_fwd_edges<MODE, LT>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
+                if (MODE != 0 && d > 0) q_fwd_store<MODE>(A, g, gbase, v, act4, acc, ofm, we, ws);
+            }
+        }
+    }
+    stage_flush(A, S);
+    if (MODE == 0) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < (A.ng << 7); i += blockDim.x)
+            if (cc_sh[i]) atomicAdd(&A.cc[i], cc_sh[i]);
+    }
+    fwd_last_block(A, d, done, Lv<LT>::MAXD);
+}
+
+// Dependency-sweep scan of one (v, g) task: per active lane of thread t, the
+// compensated sum of rho (or sigma(v)*rho in wide form) over successors and
+// the predecessor count.
+template <bool WIDE, typename T, typename LT>
+__device__ __forceinline__ void q_bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, unsigned act4,
+                                           const T (&mv)[4], const int (&ev)[4], long long r0, long long r1, int sub,
+                                           int nsub, Sum<T> (&acc)[4], int (&pc)[4]) {
+    const int t = threadIdx.x & 31;
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+        const int cnt = (int)min(32LL, r1 - jb);
+        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        for (int k0 = 0; k0 < cnt; k0 += Q_ITER) {
+            Quad<LT> q[Q_ITER];
+            int xs[Q_ITER];
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                xs[i] = __shfl_sync(FULL, xm, (k0 + i) & 31);
+                q[i] = (k0 + i < cnt && act4) ? Quad<LT>::load(lv + ((size_t)xs[i] << 7), t) : Quad<LT>::none();
+            }
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                if (k0 + i >= cnt) continue;
+                const unsigned sm = q[i].eq(d + 1) & act4;
+                const unsigned pm = q[i].eq(d - 1) & act4;
+#pragma unroll
+                for (int j = 0; j < 4; j++) pc[j] += (pm >> j) & 1u;
+                if (!sm) continue;
+                const size_t xo = ((gbase + (size_t)xs[i]) << 7) + 4 * t;
+                if (WIDE) {
+                    const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho) + xo;
+#pragma unroll
+                    for (int pr = 0; pr < 2; pr++) {
+                        if (!((sm >> (2 * pr)) & 3u)) continue;
+                        const ulonglong2 vv = *reinterpret_cast<const ulonglong2*>(rw + 2 * pr);
+                        if ((sm >> (2 * pr)) & 1u) acc[2 * pr].add(wterm<T>(mv[2 * pr], ev[2 * pr], vv.x));
+                        if ((sm >> (2 * pr + 1)) & 1u) acc[2 * pr + 1].add(wterm<T>(mv[2 * pr + 1], ev[2 * pr + 1], vv.y));
+                    }
+                } else if (sizeof(T) == 4) {
+                    const float4 vv = *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(A.rho) + xo);
+                    const float v4[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if ((sm >> j) & 1u) acc[j].add((T)v4[j]);
+                } else {
+                    const double* rd = reinterpret_cast<const double*>(A.rho) + xo;
+#pragma unroll
+                    for (int pr = 0; pr < 2; pr++) {
+                        if (!((sm >> (2 * pr)) & 3u)) continue;
+                        const double2 vv = *reinterpret_cast<const double2*>(rd + 2 * pr);
+                        if ((sm >> (2 * pr)) & 1u) acc[2 * pr].add((T)vv.x);
+                        if ((sm >> (2 * pr + 1)) & 1u) acc[2 * pr + 1].add((T)vv.y);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Edge-parallel sweep for tasks with few active lanes.
+template <bool WIDE, typename T, typename LT>
+__device__ __forceinline__ void q_bwd_edges(const KArgs& A, int d, size_t gbase, const LT* lv, unsigned act4,
+                                            const T (&mv)[4], const int (&ev)[4], long long r0, long long r1, int sub,
+                                            int nsub, Sum<T> (&acc)[4], int (&pc)[4]) {
+    const int t = threadIdx.x & 31;
+    const LT dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    const T* rho = reinterpret_cast<const T*>(A.rho);
+    const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        unsigned owners = __ballot_sync(FULL, (act4 >> j) & 1u);
+        while (owners) {
+            const int o = __ffs(owners) - 1;
+            owners &= owners - 1u;
+            const int a = 4 * o + j;
+            const T mva = WIDE ? __shfl_sync(FULL, mv[j], o) : T(0);
+            const int eva = WIDE ? __shfl_sync(FULL, ev[j], o) : 0;
+            Sum<T> ps;
+            int ppc = 0;
+            for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+                const long long jj = jb + t;
+                if (jj < r1) {
+                    const int x = A.col[jj];
+                    const LT Lx = lv[((size_t)x << 7) + a];
+                    if (Lx == dnext) {
+                        const size_t xi = ((gbase + (size_t)x) << 7) + a;
+                        ps.add(WIDE ? wterm<T>(mva, eva, rw[xi]) : rho[xi]);
+                    } else if (Lx == dprev) {
+                        ppc++;
+                    }
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const T s2 = __shfl_xor_sync(FULL, ps.s, off), c2 = __shfl_xor_sync(FULL, ps.c, off);
+                ps.merge(s2, c2);
+                ppc += __shfl_xor_sync(FULL, ppc, off);
+            }
+            if (t == o) {
+                acc[j].merge(ps.s, ps.c);
+                pc[j] += ppc;
+            }
+        }
+    }
+}
+
+// delta, rho and BC contributions of thread t's active lanes of (v, g),
+// warp-summed into bcg.
+template <bool WIDE, typename T>
+__device__ __forceinline__ void q_bwd_finish(const KArgs& A, int g, size_t gbase, int v, unsigned act4, const T (&mv)[4],
+                                             const int (&ev)[4], const Sum<T> (&acc)[4], const int (&pc)[4], bool refsem) {
+    const int t = threadIdx.x & 31;
+    double contrib = 0.0;
+    const size_t vb = ((gbase + (size_t)v) << 7) + 4 * t;
+    const T tw = A.w ? (T)A.w[v] : T(1);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (!((act4 >> j) & 1u)) continue;
+        T delta;
+        if (WIDE) {
+            delta = acc[j].value();
+            bool of = false;
+            reinterpret_cast<uint64_t*>(A.rho)[vb + j] = wpack((T)((tw + delta) / mv[j]), -ev[j], of);
+        } else {
+            const T sv = (T)A.sig[vb + j];
+            delta = sv * acc[j].value();
+            reinterpret_cast<T*>(A.rho)[vb + j] = (tw + delta) / sv;
+        }
+        contrib += (double)delta * (double)A.srcw[(g << 7) + 4 * t + j] * (refsem ? (double)pc[j] : 1.0);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) contrib += __shfl_xor_sync(FULL, contrib, off);
+    if (t == 0) A.bcg[gbase + v] += contrib;
+}
+
+template <bool WIDE, typename T>
+__device__ __forceinline__ void q_sigma_of(const KArgs& A, size_t gbase, int v, unsigned act4, T (&mv)[4], int (&ev)[4]) {
+    const int t = threadIdx.x & 31;
+#pragma unroll
+    for (int j = 0; j < 4; j++) { mv[j] = T(0); ev[j] = 0; }
+    if (!WIDE || !act4) return;
+    const uint64_t* sv = A.sig + ((gbase + (size_t)v) << 7) + 4 * t;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if ((act4 >> j) & 1u) { mv[j] = wmant<T>(sv[j]); ev[j] = wexp(sv[j]); }
+}
+
+// Dependency-sweep level kernel, 128-lane groups.
+template <bool WIDE, typename T, typename LT>
+__global__ void __launch_bounds__(BLOCK, 4) backward_q_kernel(KArgs A) {
+    __shared__ T h_s[WARPS][128];
+    __shared__ T h_c[WARPS][128];
+    __shared__ int h_pc[WARPS][128];
+    __shared__ unsigned long long s_i;
+    const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const bool refsem = (A.semantics == GBC_BC_REFERENCE);
+    if (d >= 1) {
+        const unsigned long long he = A.hoff[d + 1];
+        for (;;) {
+            if (threadIdx.x == 0) s_i = atomicAdd(&A.ctl->hnext, 1ULL);
+            __syncthreads();
+            const unsigned long long i = s_i;
+            __syncthreads();
+            if (i >= he) break;
+            const uint32_t ent = A.hq[i];
+            const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+            const size_t gbase = (size_t)g * (size_t)A.n;
+            const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 7);
+            const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+            const int nact = __reduce_add_sync(FULL, __popc(act4));
+            if (nact == 0) continue;
+            T mv[4];
+            int ev[4];
+            q_sigma_of<WIDE, T>(A, gbase, v, act4, mv, ev);
+            Sum<T> acc[4];
+            int pc[4] = {0, 0, 0, 0};
+            if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+            else q_bwd_edges<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                h_s[wib][4 * t + j] = acc[j].s;
+                h_c[wib][4 * t + j] = acc[j].c;
+                h_pc[wib][4 * t + j] = pc[j];
+            }
+            __syncthreads();
+            if (wib == 0) {
+                for (int w = 1; w < WARPS; w++) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        acc[j].merge(h_s[w][4 * t + j], h_c[w][4 * t + j]);
+                        pc[j] += h_pc[w][4 * t + j];
+                    }
+                }
+                q_bwd_finish<WIDE, T>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
+            }
+            __syncthreads();
+        }
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const unsigned long long my = base + t;
+            const uint32_t ment = my < e ? A.fq[my] : 0u;
+            const long long m0 = my < e ? A.row[ment >> 5] : 0, m1 = my < e ? A.row[(ment >> 5) + 1] : 0;
+            const int cntE = (int)min((unsigned long long)FETCH, e - base);
+            for (int k = 0; k < cntE; k++) {
+                const uint32_t ent = __shfl_sync(FULL, ment, k);
+                const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
+                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+                const size_t gbase = (size_t)g * (size_t)A.n;
+                const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 7);
+                const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+                const int nact = __reduce_add_sync(FULL, __popc(act4));
+                if (nact == 0) continue;
+                T mv[4];
+                int ev[4];
+                q_sigma_of<WIDE, T>(A, gbase, v, act4, mv, ev);
+                Sum<T> acc[4];
+                int pc[4] = {0, 0, 0, 0};
+                if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
+                else q_bwd_edges<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
+                q_bwd_finish<WIDE, T>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&A.ctl->blocks, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            A.ctl->blocks = 0;
+            if (d >= 1) {
+                A.ctl->level = d - 1;
+                A.ctl->next = A.foff[d - 1];
+                A.ctl->hnext = A.hoff[d - 1];
+            }
+        }
+    }
+}
+
 // One CTA: place each lane's source at level 0 and build F_0.
 __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, int mode, int lvl_bytes) {
     const int l = threadIdx.x;
     if (l < kb) {
-        const int g = l >> 5, t = l & 31;
+        const int g = l >> A.gs, t = l & ((1 << A.gs) - 1);
         const int s = src[l];
         if (s >= 0 && s < A.n) {
-            const size_t i = sidx(g, A.n, s, t);
+            const size_t i = sidx(g, A.n, s, t, A.gs);
             if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[i] = 0;
             else reinterpret_cast<uint16_t*>(A.lvl)[i] = 0;
             if (mode == 1) A.sig[i] = 1ULL;
@@ -1090,14 +1653,14 @@ __global__ void bw_begin_kernel(KArgs A) {
 __global__ void cleanup_kernel(KArgs A, unsigned long long count, unsigned long long hcount, int lvl_bytes) {
     const unsigned long long tid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-    const unsigned long long total = (count + hcount) * 32ULL;
+    const unsigned long long total = (count + hcount) << A.gs;
     for (unsigned long long k = tid; k < total; k += stride) {
-        const unsigned long long i = k >> 5;
-        const int t = (int)(k & 31ULL);
+        const unsigned long long i = k >> A.gs;
+        const int t = (int)(k & ((1ULL << A.gs) - 1ULL));
         const uint32_t ent = (i < count) ? A.fq[i] : A.hq[i - count];
         const int v = (int)(ent >> 5), g = (int)(ent & 31u);
-        if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[sidx(g, A.n, v, t)] = 0xFFu;
-        else reinterpret_cast<uint16_t*>(A.lvl)[sidx(g, A.n, v, t)] = 0xFFFFu;
+        if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[sidx(g, A.n, v, t, A.gs)] = 0xFFu;
+        else reinterpret_cast<uint16_t*>(A.lvl)[sidx(g, A.n, v, t, A.gs)] = 0xFFFFu;
         if (t == 0) A.vmark[(size_t)g * A.n + v] = -1;
     }
 }
@@ -1107,7 +1670,7 @@ __global__ void sssp_out_kernel(KArgs A, int kb, int32_t* dist, uint64_t* sigma,
     const size_t total = (size_t)kb * A.n;
     for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
         const int l = (int)(k / A.n), v = (int)(k % A.n);
-        const size_t i = sidx(l >> 5, A.n, v, l & 31);
+        const size_t i = sidx(l >> A.gs, A.n, v, l & ((1 << A.gs) - 1), A.gs);
         int L;
         bool unreached;
         if (lvl_bytes == 1) { L = reinterpret_cast<const uint8_t*>(A.lvl)[i]; unreached = (L == 0xFF); }
@@ -1124,7 +1687,7 @@ __global__ void profile_key_kernel(KArgs A, int lvl_bytes, uint32_t* __restrict_
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.n; v += gridDim.x * blockDim.x) {
         unsigned l0 = 0xFFFFu, lm = 0xFFFFu;
         for (int t = 0; t < 32; t++) {
-            const size_t i = sidx(0, A.n, v, t);
+            const size_t i = sidx(0, A.n, v, t, A.gs);
             unsigned L = lvl_bytes == 1 ? reinterpret_cast<const uint8_t*>(A.lvl)[i] : reinterpret_cast<const uint16_t*>(A.lvl)[i];
             if (lvl_bytes == 1 && L == 0xFFu) L = 0xFFFFu;
             if (t == 0) l0 = L;
@@ -1169,6 +1732,7 @@ struct LaneAccess {
         A.fq = e.fq_; A.fcap = e.fcap_; A.foff = e.foff_; A.ctl = (Ctl*)e.ctl_; A.ovf = e.ovf_;
         A.hq = e.hq_; A.hcap = e.hcap_; A.hoff = e.hoff_;
         A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.light = e.light_; A.semantics = semantics;
+        A.gs = e.gs_;
         A.srcw = e.srcw_;
         return A;
     }
@@ -1242,13 +1806,18 @@ gbc_status LaneEngine::alloc_queue(unsigned long long cap, unsigned long long hc
 }
 
 gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, int group_lanes) {
     release();
-    if (lanes < 32 || lanes > 1024 || lanes % 32) { set_error("lanes must be a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
+    if (group_lanes != 32 && group_lanes != 128) { set_error("lanes per group must be 32 or 128"); return GBC_ERR_ARG; }
+    if (lanes < group_lanes || lanes > 1024 || lanes % group_lanes) {
+        set_error("lanes must be a multiple of %d in [%d,1024]", group_lanes, group_lanes);
+        return GBC_ERR_ARG;
+    }
     if (g->n >= (1 << 27)) { set_error("lane engine supports fewer than 2^27 vertices"); return GBC_ERR_ARG; }
     g_ = g;
     lanes_ = lanes;
-    ng_ = lanes / 32;
+    gs_ = group_lanes == 128 ? 7 : 5;
+    ng_ = lanes >> gs_;
     need_bc_ = need_bc;
     lvl_bytes_ = g->level_bytes_hint == 2 ? 2 : 1;
     set_tuning(sparse_lanes, -1, levels_per_graph);
@@ -1320,7 +1889,29 @@ gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     KArgs A = LaneAccess::args(*this, (key % 100) >= 3 ? ((((key % 100) - 3) & 1) ? GBC_BC_REFERENCE : GBC_BC_BRANDES)
                                                        : GBC_BC_BRANDES);
     void (*fn)(KArgs) = nullptr;
-    {
+    if (gs_ == 7) {
+        const bool lv16 = key >= 100;
+        const int k = key % 100;
+        switch (k) {
+            case 0: fn = lv16 ? expand_q_kernel<0, uint16_t> : expand_q_kernel<0, uint8_t>; break;
+            case 1: fn = lv16 ? expand_q_kernel<1, uint16_t> : expand_q_kernel<1, uint8_t>; break;
+            case 2: fn = lv16 ? expand_q_kernel<2, uint16_t> : expand_q_kernel<2, uint8_t>; break;
+            default: {
+                const int v = (k - 3) >> 1;  // wide sigma * 2 + f64
+                if (lv16) {
+                    if (v == 0) fn = backward_q_kernel<false, float, uint16_t>;
+                    else if (v == 1) fn = backward_q_kernel<false, double, uint16_t>;
+                    else if (v == 2) fn = backward_q_kernel<true, float, uint16_t>;
+                    else fn = backward_q_kernel<true, double, uint16_t>;
+                } else {
+                    if (v == 0) fn = backward_q_kernel<false, float, uint8_t>;
+                    else if (v == 1) fn = backward_q_kernel<false, double, uint8_t>;
+                    else if (v == 2) fn = backward_q_kernel<true, float, uint8_t>;
+                    else fn = backward_q_kernel<true, double, uint8_t>;
+                }
+            }
+        }
+    } else {
         const bool lv16 = key >= 100;
         const int k = key % 100;
         switch (k) {
@@ -1435,8 +2026,9 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
             GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
-            const unsigned long long maxcap = (unsigned long long)ng_ * g_->n * 32ULL + (1ULL << 16);
-            const unsigned long long hmax = (unsigned long long)ng_ * n_hubs_ * 32ULL + (1ULL << 12);
+            // a (vertex, group) task recurs at most once per lane of its group
+            const unsigned long long maxcap = (unsigned long long)lanes_ * g_->n + (1ULL << 16);
+            const unsigned long long hmax = (unsigned long long)lanes_ * n_hubs_ + (1ULL << 12);
             const unsigned long long want = std::min(maxcap, std::max(fcap_ * 2, (unsigned long long)h->tail + (1ULL << 20)));
             const unsigned long long hwant = std::min(hmax, std::max(hcap_ * 2, (unsigned long long)h->htail + (1ULL << 12)));
             if (want <= fcap_ && hwant <= hcap_) { set_error("frontier queue cannot grow"); return GBC_ERR_LIMIT; }
@@ -1471,10 +2063,10 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         }
         if (mode == 1) {
             for (int i = 0; i < 32; i++) res.ovf_bits[i] = 0;
-            GBC_CUDA(cudaMemcpyAsync(res.ovf_bits, ovf_, ng_ * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+            GBC_CUDA(cudaMemcpyAsync(res.ovf_bits, ovf_, (lanes_ / 32) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
             int cnt = 0;
-            for (int i = 0; i < ng_; i++) cnt += __builtin_popcount(res.ovf_bits[i]);
+            for (int i = 0; i < lanes_ / 32; i++) cnt += __builtin_popcount(res.ovf_bits[i]);
             res.overflow_count += cnt;
             if (cnt && rq.abort_on_overflow) {
                 cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
@@ -1484,10 +2076,10 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             }
         } else if (mode == 2) {
             uint32_t bits[32] = {};
-            GBC_CUDA(cudaMemcpyAsync(bits, ovf_, ng_ * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
+            GBC_CUDA(cudaMemcpyAsync(bits, ovf_, (lanes_ / 32) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
             int cnt = 0;
-            for (int i = 0; i < ng_; i++) cnt += __builtin_popcount(bits[i]);
+            for (int i = 0; i < lanes_ / 32; i++) cnt += __builtin_popcount(bits[i]);
             if (cnt) {
                 cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
                 GBC_CUDA(cudaGetLastError());

@@ -77,7 +77,9 @@ typedef struct {
                                  lane group (results do not depend on it); 1: lanes in the order given */
     int32_t light_steps;      /* a frontier task with (active lanes x degree) <= this is expanded by a
                                  single thread, 32 tasks per warp; 0 = never; -1 = autotune */
-    int32_t reserved[7];
+    int32_t group_lanes;      /* sources per lane group: 32 (one per warp thread) or 128 (four per
+                                 thread; lanes must then be a multiple of 128); 0 = automatic */
+    int32_t reserved[6];
 } gbc_options;
 
 typedef struct {

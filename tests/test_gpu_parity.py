@@ -234,3 +234,54 @@ def test_edge_cases(gpu, orc):
         ref, _ = orc.bc(og, np.arange(n))
         assert relerr(G.bc(), ref) < TOL_F64
         assert np.array_equal(G.cc(), orc.cc(og, np.arange(n)))
+
+
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "grid24", "er2k", "karate", "rmat14", "star+grid"])
+def test_group128_parity(gpu, orc, graphs, name):
+    """128-lane groups (four lanes per thread): distances and path counts
+    bit-exact, closeness exact, BC within tolerance in both semantics and
+    both sweep precisions, also with the edge-parallel mode forced."""
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = sources_of(csr, 300, seed=21)
+    ref0, _ = orc.bc(og, src, semantics=0)
+    ref1, _ = orc.bc(og, src, semantics=1)
+    with gpu.Graph(csr) as G:
+        for lanes in (128, 256):
+            assert relerr(G.bc(src, group_lanes=128, lanes=lanes), ref0) < TOL_F64
+            assert relerr(G.bc(src, group_lanes=128, lanes=lanes, semantics=1), ref1) < TOL_F64
+            assert relerr(G.bc(src, group_lanes=128, lanes=lanes, delta_precision=gpu.DELTA_F32), ref0) < TOL_F32
+        assert relerr(G.bc(src, group_lanes=128, lanes=128, sparse_lanes=128), ref0) < TOL_F64
+        assert np.array_equal(G.cc(src, group_lanes=128, lanes=256), orc.cc(og, src))
+        assert np.array_equal(G.cc(src, group_lanes=128, lanes=128, sparse_lanes=0), orc.cc(og, src))
+        dist, sig, ovf = G.sssp(src[:130], group_lanes=128)
+        for i, s in enumerate(src[:130]):
+            d0, s0, o0, _ = orc.sssp(og, int(s))
+            assert np.array_equal(dist[i], d0)
+            if not o0.any():
+                assert np.array_equal(sig[i], s0)
+
+
+def test_group128_deep_and_wide(gpu, orc):
+    """128-lane groups on a graph deeper than 8-bit levels and on a grid whose
+    path counts overflow uint64 (wide form)."""
+    n = 700
+    row = np.concatenate([[0], np.cumsum([1] + [2] * (n - 2) + [1])]).astype(np.int64)
+    col = []
+    for v in range(n):
+        col += ([v - 1] if v > 0 else []) + ([v + 1] if v < n - 1 else [])
+    path = gpu.CSR(row, np.array(col, np.int32))
+    og = to_orc(orc, path)
+    src = np.array([0, 5, 350, 699], np.int32)
+    with gpu.Graph(path) as G:
+        assert relerr(G.bc(src, group_lanes=128), orc.bc(og, src)[0]) < TOL_F64
+        assert np.array_equal(G.cc(src, group_lanes=128), orc.cc(og, src))
+    grid = gpu.gen_grid(80, 80, 0.0, seed=1)
+    og = to_orc(orc, grid)
+    src = np.array([0, 79, 3200, 6399], dtype=np.int32)
+    ref, novf = orc.bc(og, src, scaled=True)
+    assert novf > 0
+    with gpu.Graph(grid) as G:
+        got = G.bc(src, group_lanes=128)
+        assert G.stats()["sigma_mode_used"] == gpu.SIGMA_WIDE
+        assert relerr(got, ref) < TOL_F64
