@@ -326,6 +326,7 @@ static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t
     s.fwd_kernels = r.fwd_kernels;
     s.bwd_kernels = r.bwd_kernels;
     s.edges_traversed = -1;   // filled in lazily by gbc_graph_last_stats
+    s.group_lanes = lanes == 1 ? 1 : (G->eng ? G->eng->group_lanes() : 32);
     G->last_src = hsrc;
 }
 

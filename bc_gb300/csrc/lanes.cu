@@ -73,7 +73,7 @@ struct KArgs {
     uint32_t* fq;          // regular frontier entries, all levels
     unsigned long long fcap;
     unsigned long long* foff;
-    uint32_t* hq;          // hub frontier entries (vertex degree > HUB_DEG), all levels
+    uint32_t* hq;          // hub frontier entries (vertex degree > hub_deg), all levels
     unsigned long long hcap;
     unsigned long long* hoff;
     Ctl* ctl;
@@ -85,9 +85,11 @@ struct KArgs {
     int light;             // entries with (active lanes x degree) <= light expand one per thread
     int semantics;
     int gs;                // lanes per group = 1 << gs (5: 32 lanes, one per thread; 7: 128, four per thread)
+    int hub_deg;           // entries of vertices with a higher degree go to the hub queue (CTA per entry)
 };
 
-constexpr int HUB_DEG = 1024;   // entries of higher-degree vertices are expanded by a whole CTA
+constexpr int HUB_DEG = 1024;   // 32-lane groups: entries of higher-degree vertices are expanded by a whole CTA
+constexpr int HUB_DEG_Q = 1024; // the same for 128-lane groups
 constexpr int FETCH = 32;       // regular entries a warp takes per fetch, one per thread
 constexpr int STG = 128;        // regular-queue entries a warp stages in shared memory per append
 constexpr int WARPS = BLOCK / 32;
@@ -105,7 +107,7 @@ __device__ __forceinline__ size_t sidx(int g, int n, int v, int t, int gs) {
     return ((((size_t)g * (size_t)n) + (size_t)v) << gs) + (size_t)t;
 }
 
-__device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > HUB_DEG; }
+__device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > A.hub_deg; }
 
 // ---- wide-exponent path counts ---------------------------------------------
 // Path counts past uint64 are held as (1 + f/2^44) * 2^(e - WBIAS) in one
@@ -1733,6 +1735,7 @@ struct LaneAccess {
         A.hq = e.hq_; A.hcap = e.hcap_; A.hoff = e.hoff_;
         A.cc = e.ccbuf_; A.bcg = e.bcg_; A.sparse = e.sparse_; A.light = e.light_; A.semantics = semantics;
         A.gs = e.gs_;
+        A.hub_deg = e.gs_ == 7 ? HUB_DEG_Q : HUB_DEG;
         A.srcw = e.srcw_;
         return A;
     }
@@ -1858,7 +1861,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
         std::vector<int64_t> hrow(n + 1);
         GBC_CUDA(cudaMemcpy(hrow.data(), g->row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
         n_hubs_ = 0;
-        for (size_t v = 0; v < n; v++) n_hubs_ += (hrow[v + 1] - hrow[v]) > HUB_DEG;
+        for (size_t v = 0; v < n; v++) n_hubs_ += (hrow[v + 1] - hrow[v]) > (gs_ == 7 ? HUB_DEG_Q : HUB_DEG);
     }
     GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));

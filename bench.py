@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--plain-sources", type=int, default=16)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-tune", action="store_true", help="skip gbc_autotune; use the default expansion settings")
+    p.add_argument("--group-lanes", type=int, default=0, choices=(0, 32, 128),
+                   help="sources per lane group (0: the library's choice)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
@@ -329,7 +331,7 @@ def main():
         return sample[idx]
 
     opt = dict(semantics=G.BC_BRANDES, delta_precision=G.DELTA_F64 if args.delta == "f64" else G.DELTA_F32,
-               sigma_mode=G.SIGMA_AUTO, lanes=B)
+               sigma_mode=G.SIGMA_AUTO, lanes=B, group_lanes=args.group_lanes)
     o = G.options(**opt)
     graph = G.Graph(csr)
     stream = torch.cuda.current_stream(dev)
@@ -364,8 +366,10 @@ def main():
     fwd_ms = bwd_ms = 0.0
     fwd_k = bwd_k = launches = 0
     edges = 0
+    group = 32
     for i in range(args.warmup, args.warmup + args.steps):
         st = run_step(i)
+        group = st.group_lanes
         fwd_ms += st.fwd_ms
         bwd_ms += st.bwd_ms
         fwd_k += st.fwd_kernels
@@ -393,8 +397,10 @@ def main():
     adj = 4 * M + 4 * (n + 1)
     fwd_bytes = (adj + 16 * B * n) * args.steps
     bwd_bytes = (adj + 16 * B * n + 16 * n) * args.steps
-    dom = "expand_kernel" if fwd_ms >= bwd_ms else "backward_kernel"
-    dom_ms, dom_bytes, dom_k = (fwd_ms, fwd_bytes, fwd_k) if dom == "expand_kernel" else (bwd_ms, bwd_bytes, bwd_k)
+    fwd_dom = fwd_ms >= bwd_ms
+    q = "_q" if group == 128 else ""   # the 128-lane-group kernels
+    dom = ("expand" if fwd_dom else "backward") + q + "_kernel"
+    dom_ms, dom_bytes, dom_k = (fwd_ms, fwd_bytes, fwd_k) if fwd_dom else (bwd_ms, bwd_bytes, bwd_k)
     hbm, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     tr = load_traffic()
@@ -478,7 +484,7 @@ def main():
                "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",
                "data": "synthetic (seeded R-MAT generator)",
                "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": args.edge_factor,
-                          "n": n, "m_directed": M, "lanes_per_step": B, "sources": args.k,
+                          "n": n, "m_directed": M, "lanes_per_step": B, "lanes_per_group": int(group), "sources": args.k,
                           "parallelism": f"sources sharded over {ws} GPU(s)",
                           "l2": "inputs larger than L2 (lane state ~16*B*n bytes per sweep)",
                           "tuning": tuning},

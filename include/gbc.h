@@ -99,6 +99,8 @@ typedef struct {
     double  bwd_ms;           /* device time of the dependency-sweep level kernels */
     int64_t fwd_kernels;      /* forward level kernels launched (incl. no-op tail launches) */
     int64_t bwd_kernels;      /* dependency-sweep level kernels launched */
+    int32_t group_lanes;      /* lanes per group of the engine that ran (32 or 128; 1 = plain engine) */
+    int32_t reserved_stats;
 } gbc_run_stats;
 
 typedef struct gbc_graph_s* gbc_graph;
