@@ -1085,6 +1085,7 @@ template <> struct Quad<uint16_t> {
 };
 
 constexpr int Q_ITER = 8;   // neighbours whose level quads are loaded before any is used
+constexpr int FETCH_Q = 8;  // regular tasks a warp takes per fetch in 128-lane groups (8: 3% faster than 32 on R-MAT s22)
 
 // Forward scan of one (v, g) task over neighbour chunks r0 + 32*sub, step
 // 32*nsub: thread t pulls sigma for its active lanes (act4) and discovers
@@ -1326,13 +1327,14 @@ __global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
         const unsigned long long e = A.foff[d + 1];
         for (;;) {
             unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH_Q);
             base = __shfl_sync(FULL, base, 0);
             if (base >= e) break;
             const unsigned long long my = base + t;
-            const uint32_t ment = my < e ? A.fq[my] : 0u;
-            const long long m0 = my < e ? A.row[ment >> 5] : 0, m1 = my < e ? A.row[(ment >> 5) + 1] : 0;
-            const int cntE = (int)min((unsigned long long)FETCH, e - base);
+            const bool mine = t < FETCH_Q && my < e;
+            const uint32_t ment = mine ? A.fq[my] : 0u;
+            const long long m0 = mine ? A.row[ment >> 5] : 0, m1 = mine ? A.row[(ment >> 5) + 1] : 0;
+            const int cntE = (int)min((unsigned long long)FETCH_Q, e - base);
             for (int k = 0; k < cntE; k++) {
                 const uint32_t ent = __shfl_sync(FULL, ment, k);
                 const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
@@ -1562,13 +1564,14 @@ __global__ void __launch_bounds__(BLOCK, 4) backward_q_kernel(KArgs A) {
         const unsigned long long e = A.foff[d + 1];
         for (;;) {
             unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH_Q);
             base = __shfl_sync(FULL, base, 0);
             if (base >= e) break;
             const unsigned long long my = base + t;
-            const uint32_t ment = my < e ? A.fq[my] : 0u;
-            const long long m0 = my < e ? A.row[ment >> 5] : 0, m1 = my < e ? A.row[(ment >> 5) + 1] : 0;
-            const int cntE = (int)min((unsigned long long)FETCH, e - base);
+            const bool mine = t < FETCH_Q && my < e;
+            const uint32_t ment = mine ? A.fq[my] : 0u;
+            const long long m0 = mine ? A.row[ment >> 5] : 0, m1 = mine ? A.row[(ment >> 5) + 1] : 0;
+            const int cntE = (int)min((unsigned long long)FETCH_Q, e - base);
             for (int k = 0; k < cntE; k++) {
                 const uint32_t ent = __shfl_sync(FULL, ment, k);
                 const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
