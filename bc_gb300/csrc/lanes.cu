@@ -1742,6 +1742,19 @@ struct LaneAccess {
         A.srcw = e.srcw_;
         return A;
     }
+    // Reset the lane state a batch touched: per task when few were touched,
+    // else one memset of the level and claim arrays (a 128-lane task rewrites a
+    // 128-byte row; on a full R-MAT scale 22 batch the per-task reset wrote
+    // 10 GB in 12.5 ms, the memsets write 4.4 GB).
+    static void reset(LaneEngine& e, const KArgs& A, unsigned long long entries, unsigned long long hentries) {
+        const size_t cells = (size_t)e.lanes_ * e.g_->n;
+        if (((entries + hentries) << e.gs_) * 4 < cells) {
+            cleanup_kernel<<<e.sm_count_ * 4, 256, 0, e.stream_>>>(A, entries, hentries, e.lvl_bytes_);
+        } else {
+            cudaMemsetAsync(e.lvl_, 0xFF, cells * e.lvl_bytes_, e.stream_);
+            cudaMemsetAsync(e.vmark_, 0xFF, (size_t)e.ng_ * e.g_->n * sizeof(int32_t), e.stream_);
+        }
+    }
 };
 
 size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc) {
@@ -2051,7 +2064,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
                 GBC_CUDA(cudaStreamSynchronize(stream_));
                 continue;
             }
-            cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
+            LaneAccess::reset(*this, A, entries, hentries);
             set_error("BFS deeper than %d levels", MAX_LEVEL);
             return GBC_ERR_LIMIT;
         }
@@ -2075,7 +2088,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             for (int i = 0; i < lanes_ / 32; i++) cnt += __builtin_popcount(res.ovf_bits[i]);
             res.overflow_count += cnt;
             if (cnt && rq.abort_on_overflow) {
-                cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
+                LaneAccess::reset(*this, A, entries, hentries);
                 GBC_CUDA(cudaGetLastError());
                 set_error("exact path counts overflowed uint64 in %d lanes", cnt);
                 return GBC_ERR_OVERFLOW;
@@ -2087,7 +2100,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             int cnt = 0;
             for (int i = 0; i < lanes_ / 32; i++) cnt += __builtin_popcount(bits[i]);
             if (cnt) {
-                cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
+                LaneAccess::reset(*this, A, entries, hentries);
                 GBC_CUDA(cudaGetLastError());
                 set_error("path counts exceed 2^524287 in %d lanes", cnt);
                 return GBC_ERR_OVERFLOW;
@@ -2120,7 +2133,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         if (mode == 0 && rq.d_cc) {
             GBC_CUDA(cudaMemcpyAsync(rq.d_cc, ccbuf_, rq.kb * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream_));
         }
-        cleanup_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(A, entries, hentries, lvl_bytes_);
+        LaneAccess::reset(*this, A, entries, hentries);
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches++;
         return GBC_OK;
