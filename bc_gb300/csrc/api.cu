@@ -43,14 +43,18 @@ struct gbc_graph_s {
     } tuned;
     ~gbc_graph_s() {
         eng.reset();
-        cudaFree(g.row);
-        cudaFree(g.col);
+        if (stream) cudaStreamSynchronize(stream);
+        // the CSR and id maps go back to the lane-state cache (graphs created in a loop reuse them)
+        dev_release(g.row, sizeof(int64_t) * ((size_t)g.n + 1));
+        dev_release(g.col, sizeof(int32_t) * std::max<int64_t>(g.m, 1));
+        g.row = nullptr;
+        g.col = nullptr;
         cudaFree(d_src);
         cudaFree(d_ccb);
         cudaFree(d_bc);
         cudaFree(d_pos);
-        cudaFree(d_order);
-        cudaFree(d_inv);
+        dev_release(d_order, sizeof(int32_t) * (size_t)g.n);
+        dev_release(d_inv, sizeof(int32_t) * (size_t)g.n);
         cudaFree(d_bc_out);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -85,8 +89,8 @@ gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_g
     GBC_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
     GBC_CUDA(cudaEventCreate(&G->ev0));
     GBC_CUDA(cudaEventCreate(&G->ev1));
-    if (cudaMalloc(&g.row, sizeof(int64_t) * (n + 1)) != cudaSuccess ||
-        cudaMalloc(&g.col, sizeof(int32_t) * std::max<int64_t>(g.m, 1)) != cudaSuccess) {
+    if (dev_alloc((void**)&g.row, sizeof(int64_t) * ((size_t)n + 1)) != cudaSuccess ||
+        dev_alloc((void**)&g.col, sizeof(int32_t) * std::max<int64_t>(g.m, 1)) != cudaSuccess) {
         cudaGetLastError();
         set_error("device allocation for the CSR failed");
         return GBC_ERR_NOMEM;

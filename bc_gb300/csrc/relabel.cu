@@ -88,24 +88,32 @@ gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order_out,
     int64_t* nrow = nullptr;
     uint64_t *key = nullptr, *skey = nullptr;
     void* tmp = nullptr;
+    // all buffers through the lane-state cache: graphs created in a loop reuse them
+    const size_t sn = sizeof(int32_t) * (size_t)n, sm8 = sizeof(uint64_t) * (size_t)n,
+                 srow = sizeof(int64_t) * ((size_t)n + 1), scol = sizeof(int32_t) * std::max<int64_t>(M, 1);
+    size_t stmp = 0;
     auto cleanup = [&](bool keep) {
-        cudaFree(deg); cudaFree(ids); cudaFree(skeys); cudaFree(ndeg); cudaFree(off32); cudaFree(tmp);
-        cudaFree(key); cudaFree(skey);
-        if (!keep) { cudaFree(order); cudaFree(inv); cudaFree(nrow); cudaFree(ncol); cudaFree(ncol2); }
+        cudaStreamSynchronize(s);   // nothing in flight may still use a buffer handed back
+        dev_release(deg, sn); dev_release(ids, sn); dev_release(skeys, sn); dev_release(ndeg, sn);
+        dev_release(off32, sn); dev_release(tmp, stmp); dev_release(key, sm8); dev_release(skey, sm8);
+        if (!keep) {
+            dev_release(order, sn); dev_release(inv, sn); dev_release(nrow, srow);
+            dev_release(ncol, scol); dev_release(ncol2, scol);
+        }
     };
     bool ok = true;
-    ok &= cudaMalloc(&deg, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&ids, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&skeys, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&order, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&inv, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&ndeg, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&off32, sizeof(int32_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&nrow, sizeof(int64_t) * ((size_t)n + 1)) == cudaSuccess;
-    ok &= cudaMalloc(&ncol, sizeof(int32_t) * std::max<int64_t>(M, 1)) == cudaSuccess;
-    ok &= cudaMalloc(&ncol2, sizeof(int32_t) * std::max<int64_t>(M, 1)) == cudaSuccess;
-    ok &= cudaMalloc(&key, sizeof(uint64_t) * n) == cudaSuccess;
-    ok &= cudaMalloc(&skey, sizeof(uint64_t) * n) == cudaSuccess;
+    ok &= dev_alloc((void**)&deg, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&ids, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&skeys, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&order, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&inv, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&ndeg, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&off32, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&nrow, srow) == cudaSuccess;
+    ok &= dev_alloc((void**)&ncol, scol) == cudaSuccess;
+    ok &= dev_alloc((void**)&ncol2, scol) == cudaSuccess;
+    ok &= dev_alloc((void**)&key, sm8) == cudaSuccess;
+    ok &= dev_alloc((void**)&skey, sm8) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         cleanup(false);
@@ -121,7 +129,8 @@ gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order_out,
     if (e == cudaSuccess)
         e = cub::DeviceSegmentedSort::SortKeys(nullptr, tb3, ncol, ncol2, M, n, nrow, nrow + 1, s);
     if (e == cudaSuccess) e = cub::DeviceRadixSort::SortPairs(nullptr, tb4, key, skey, ids, order, n, 0, 64, s);
-    if (e == cudaSuccess) e = cudaMalloc(&tmp, std::max(std::max(tb1, tb4), std::max(tb2, tb3)) + 16);
+    stmp = std::max(std::max(tb1, tb4), std::max(tb2, tb3)) + 16;
+    if (e == cudaSuccess) e = dev_alloc(&tmp, stmp);
     if (e != cudaSuccess) {
         cudaGetLastError();
         cleanup(false);
@@ -154,9 +163,9 @@ gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order_out,
         set_error("relabel failed: %s", cudaGetErrorString(e));
         return GBC_ERR_CUDA;
     }
-    cudaFree(g.row);
-    cudaFree(g.col);
-    cudaFree(ncol);
+    dev_release(g.row, srow);
+    dev_release(g.col, scol);
+    dev_release(ncol, scol);
     ncol = nullptr;
     g.row = nrow;
     g.col = ncol2;
