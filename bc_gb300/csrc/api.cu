@@ -25,9 +25,8 @@ struct gbc_graph_s {
     double* d_bc = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<int32_t> last_src;
-    // lane assignment: per-vertex level-profile key and degree (computed once)
+    // lane assignment: per-vertex level-profile key (computed once)
     std::vector<uint32_t> key;
-    std::vector<int32_t> deg;
     int32_t key_depth = 0;        // levels of that BFS (0: not run)
     int32_t* d_pos = nullptr;
     int64_t pos_cap = 0;
@@ -82,10 +81,10 @@ static void host_components(const int64_t* row, const int32_t* col, int32_t n, D
     g.max_degree = md;
 }
 
-gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_graph_s* G) {
+static gbc_status graph_alloc(int32_t n, int64_t m, gbc_graph_s* G) {
     DevGraph& g = G->g;
     g.n = n;
-    g.m = row[n];
+    g.m = m;
     GBC_CUDA(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
     GBC_CUDA(cudaEventCreate(&G->ev0));
     GBC_CUDA(cudaEventCreate(&G->ev1));
@@ -95,9 +94,68 @@ gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_g
         set_error("device allocation for the CSR failed");
         return GBC_ERR_NOMEM;
     }
+    return GBC_OK;
+}
+
+// Host CSR to the device, on the graph's stream (not waited for).
+static gbc_status graph_upload(const int64_t* row, const int32_t* col, int32_t n, gbc_graph_s* G) {
+    GBC_TRY(graph_alloc(n, row[n], G));
+    DevGraph& g = G->g;
     GBC_CUDA(cudaMemcpyAsync(g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, G->stream));
     if (g.m) GBC_CUDA(cudaMemcpyAsync(g.col, col, sizeof(int32_t) * g.m, cudaMemcpyHostToDevice, G->stream));
+    return GBC_OK;
+}
+
+// bad[0] = smallest v with row[v+1] < row[v], bad[1] = smallest e with col[e]
+// outside [0, n); both stay 0xFFFFFFFF when there is none (indices < 2^31).
+// Whole blocks step together so that every lane takes part in the warp minimum.
+__global__ void csr_check_kernel(const int64_t* __restrict__ row, const int32_t* __restrict__ col, int32_t n,
+                                 int64_t m, unsigned* __restrict__ bad) {
+    const int64_t len = (int64_t)n > m ? (int64_t)n : m;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < len; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        unsigned br = ~0u, bc = ~0u;
+        if (i < n && row[i + 1] < row[i]) br = (unsigned)i;
+        if (i < m && (uint32_t)col[i] >= (uint32_t)n) bc = (unsigned)i;
+        br = __reduce_min_sync(0xFFFFFFFFu, br);
+        bc = __reduce_min_sync(0xFFFFFFFFu, bc);
+        if ((threadIdx.x & 31) == 0) {
+            if (br != ~0u) atomicMin(&bad[0], br);
+            if (bc != ~0u) atomicMin(&bad[1], bc);
+        }
+    }
+}
+
+// The per-entry checks of validate_csr on the device copy (0.6 GB of CSR
+// takes well under a millisecond here against ~10 ms for 16 host threads),
+// with the same messages and the same first offending index.  host_col, when
+// given, supplies the offending value for the message.  Waits for the upload.
+static gbc_status validate_device(gbc_graph_s* G, const int32_t* host_col) {
+    const DevGraph& g = G->g;
+    unsigned* d_bad = nullptr;
+    if (dev_alloc((void**)&d_bad, 2 * sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("validation flag");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<unsigned, void (*)(unsigned*)> keep(d_bad, [](unsigned* p) { dev_release(p, 2 * sizeof(unsigned)); });
+    int dev = 0, sm = 0;
+    GBC_CUDA(cudaGetDevice(&dev));
+    GBC_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
+    GBC_CUDA(cudaMemsetAsync(d_bad, 0xFF, 2 * sizeof(unsigned), G->stream));
+    csr_check_kernel<<<sm * 8, 256, 0, G->stream>>>(g.row, g.col, g.n, g.m, d_bad);
+    GBC_CUDA(cudaGetLastError());
+    unsigned bad[2] = {~0u, ~0u};
+    GBC_CUDA(cudaMemcpyAsync(bad, d_bad, sizeof bad, cudaMemcpyDeviceToHost, G->stream));
     GBC_CUDA(cudaStreamSynchronize(G->stream));
+    if (bad[0] != ~0u) { set_error("row offsets decrease at %lld", (long long)bad[0]); return GBC_ERR_ARG; }
+    if (bad[1] != ~0u) {
+        int32_t val = 0;
+        if (host_col) val = host_col[bad[1]];
+        else GBC_CUDA(cudaMemcpy(&val, g.col + bad[1], sizeof val, cudaMemcpyDeviceToHost));
+        set_error("col[%lld]=%d out of range", (long long)bad[1], val);
+        return GBC_ERR_ARG;
+    }
     return GBC_OK;
 }
 
@@ -201,25 +259,25 @@ static gbc_status ensure_order_key(gbc_graph_s* G) {
     // its own narrow engine: the main engine's group width depends on the depth found here
     LaneEngine E;
     GBC_TRY(E.init(&g, 32, false, -1, 0, G->stream, 32));
-    std::vector<int64_t> row(g.n + 1);
-    GBC_CUDA(cudaMemcpy(row.data(), g.row, sizeof(int64_t) * (g.n + 1), cudaMemcpyDeviceToHost));
-    G->deg.resize(g.n);
-    for (int32_t v = 0; v < g.n; v++) G->deg[v] = (int32_t)(row[v + 1] - row[v]);
-    std::vector<int32_t> idx(g.n);
-    for (int32_t v = 0; v < g.n; v++) idx[v] = v;
+    // every graph handle is relabelled by descending degree (finish_graph), so
+    // the kb highest-degree vertices are ids 0..kb-1
     const int32_t kb = std::min<int32_t>(32, g.n);
-    std::partial_sort(idx.begin(), idx.begin() + kb, idx.end(),
-                      [&](int32_t a, int32_t b) { return G->deg[a] != G->deg[b] ? G->deg[a] > G->deg[b] : a < b; });
+    std::vector<int32_t> idx(kb);
+    for (int32_t v = 0; v < kb; v++) idx[v] = v;
     int32_t* d_hub = nullptr;
     uint32_t* d_key = nullptr;
-    if (cudaMalloc(&d_hub, sizeof(int32_t) * 32) != cudaSuccess || cudaMalloc(&d_key, sizeof(uint32_t) * g.n) != cudaSuccess) {
+    const size_t skey = sizeof(uint32_t) * (size_t)g.n;
+    if (dev_alloc((void**)&d_hub, sizeof(int32_t) * 32) != cudaSuccess || dev_alloc((void**)&d_key, skey) != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(d_hub);
+        dev_release(d_hub, sizeof(int32_t) * 32);
         set_error("order key buffers");
         return GBC_ERR_NOMEM;
     }
-    std::unique_ptr<void, void (*)(void*)> f1(d_hub, [](void* p) { cudaFree(p); });
-    std::unique_ptr<void, void (*)(void*)> f2(d_key, [](void* p) { cudaFree(p); });
+    // handed back once the stream is idle
+    struct Bufs {
+        cudaStream_t s; int32_t* hub; uint32_t* key; size_t skey;
+        ~Bufs() { cudaStreamSynchronize(s); dev_release(hub, sizeof(int32_t) * 32); dev_release(key, skey); }
+    } bufs{G->stream, d_hub, d_key, skey};
     GBC_CUDA(cudaMemcpyAsync(d_hub, idx.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, G->stream));
     LaneRequest rq;
     rq.job = LaneJob::CC;
@@ -246,11 +304,11 @@ static gbc_status order_sources(gbc_graph_s* G, const gbc_options& o, bool bc, s
     if (o.engine == GBC_ENGINE_PLAIN || o.source_order != 0 || k <= 32) return GBC_OK;
     GBC_TRY(ensure_order_key(G));
     const std::vector<uint32_t>& key = G->key;
-    const std::vector<int32_t>& deg = G->deg;
+    // ties: lower id first, which is higher degree first (ids are in descending degree order)
     std::stable_sort(pos.begin(), pos.end(), [&](int32_t a, int32_t b) {
         const int32_t x = hsrc[a], y = hsrc[b];
         if (key[x] != key[y]) return key[x] < key[y];
-        return deg[x] > deg[y];
+        return x < y;
     });
     std::vector<int32_t> ordered(k);
     for (int64_t i = 0; i < k; i++) ordered[i] = hsrc[pos[i]];
@@ -446,10 +504,15 @@ void gbc_options_default(gbc_options* o) {
 gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, gbc_graph* out) {
     if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
     *out = nullptr;
-    GBC_TRY(validate_csr(row, col, n));
-    GBC_TRY(ensure_device());
+    GBC_TRY(validate_csr_header(row, col, n));
+    if (ensure_device() != GBC_OK) {
+        // no device to check on: the host check, so that a bad CSR is still reported as such
+        GBC_TRY(validate_csr(row, col, n));
+        return ensure_device();
+    }
     auto G = std::make_unique<gbc_graph_s>();
     GBC_TRY(graph_upload(row, col, n, G.get()));
+    GBC_TRY(validate_device(G.get(), col));
     GBC_TRY(finish_graph(G.get()));
     *out = G.release();
     return GBC_OK;
@@ -528,14 +591,17 @@ gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, i
     if (!out || !d_row || (m > 0 && !d_col) || n <= 0 || m < 0) { set_error("bad arguments"); return GBC_ERR_ARG; }
     *out = nullptr;
     GBC_TRY(ensure_device());
-    std::vector<int64_t> row(n + 1);
-    std::vector<int32_t> col(std::max<int64_t>(m, 1));
-    GBC_CUDA(cudaMemcpy(row.data(), d_row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
-    if (m) GBC_CUDA(cudaMemcpy(col.data(), d_col, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
-    if (row[n] != m) { set_error("row[n] != m"); return GBC_ERR_ARG; }
-    GBC_TRY(validate_csr(row.data(), col.data(), n));
+    int64_t r0 = 0, rn = 0;
+    GBC_CUDA(cudaMemcpy(&r0, d_row, sizeof r0, cudaMemcpyDeviceToHost));
+    GBC_CUDA(cudaMemcpy(&rn, d_row + n, sizeof rn, cudaMemcpyDeviceToHost));
+    if (rn != m) { set_error("row[n] != m"); return GBC_ERR_ARG; }
+    if (r0 != 0) { set_error("row[0] must be 0"); return GBC_ERR_ARG; }
+    if (m >= ((int64_t)1 << 31)) { set_error("more than 2^31-1 directed edges (%lld)", (long long)m); return GBC_ERR_ARG; }
     auto G = std::make_unique<gbc_graph_s>();
-    GBC_TRY(graph_upload(row.data(), col.data(), n, G.get()));
+    GBC_TRY(graph_alloc(n, m, G.get()));
+    GBC_CUDA(cudaMemcpyAsync(G->g.row, d_row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToDevice, G->stream));
+    if (m) GBC_CUDA(cudaMemcpyAsync(G->g.col, d_col, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, G->stream));
+    GBC_TRY(validate_device(G.get(), nullptr));
     GBC_TRY(finish_graph(G.get()));
     *out = G.release();
     return GBC_OK;

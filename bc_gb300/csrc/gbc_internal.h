@@ -24,6 +24,11 @@ struct HostCSR {
 // Validate a caller-provided CSR (offsets monotone, ids in range).
 gbc_status validate_csr(const int64_t* row, const int32_t* col, int32_t n);
 
+// The O(1) part of validate_csr: arguments, row[0] == 0 and 0 <= row[n] < 2^31
+// (for a row[n] outside that range it runs the full check, so the message is
+// the one validate_csr gives).  The per-entry checks then run on the device.
+gbc_status validate_csr_header(const int64_t* row, const int32_t* col, int32_t n);
+
 // Build a symmetric, deduplicated CSR without self-loops from an edge list
 // (u[i], v[i]) over n vertices; rows sorted by neighbour id. Multi-threaded.
 void csr_from_edges(int32_t n, const std::vector<int32_t>& u, const std::vector<int32_t>& v, HostCSR& out);

@@ -94,6 +94,13 @@ static int64_t first_bad(int64_t count, F bad) {
     return best.load();
 }
 
+gbc_status validate_csr_header(const int64_t* row, const int32_t* col, int32_t n) {
+    if (n <= 0 || !row || (row[n] > 0 && !col)) { set_error("invalid CSR arguments (n=%d)", n); return GBC_ERR_ARG; }
+    if (row[0] != 0) { set_error("row[0] must be 0"); return GBC_ERR_ARG; }
+    if (row[n] < 0 || row[n] >= ((int64_t)1 << 31)) return validate_csr(row, col, n);
+    return GBC_OK;
+}
+
 gbc_status validate_csr(const int64_t* row, const int32_t* col, int32_t n) {
     if (n <= 0 || !row || (row[n] > 0 && !col)) { set_error("invalid CSR arguments (n=%d)", n); return GBC_ERR_ARG; }
     if (row[0] != 0) { set_error("row[0] must be 0"); return GBC_ERR_ARG; }

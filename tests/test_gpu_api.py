@@ -247,3 +247,36 @@ def test_device_ingest_matches_host_csr(gpu, orc, datasets, case):
                 assert np.array_equal(G.cc(src_s), orc.cc(og, src_s))
     with pytest.raises(gpu.GbcError):
         gpu.Graph.from_edges(np.array([0, 5], np.int32), np.array([1, 12], np.int32), 10)
+
+
+def test_device_side_csr_validation(gpu):
+    """With a device present, the per-entry CSR checks run on the device copy:
+    the same messages and first offending index as the host check, for the
+    host-buffer and the device-pointer entry points, and offsets reported
+    before neighbour ids."""
+    torch = pytest.importorskip("torch")
+    L = gpu.lib()
+    n, m = 5000, 2_000_000
+    row = np.linspace(0, m, n + 1).astype(np.int64)
+    col = (np.arange(m) % n).astype(np.int32)
+    h = C.c_void_p()
+    gpu.check(L.gbc_graph_create(row, col, n, C.byref(h)))
+    L.gbc_graph_destroy(h)
+    bad = col.copy()
+    bad[1_500_001] = n + 5
+    bad[1_900_000] = -1
+    assert L.gbc_graph_create(row, bad, n, C.byref(h)) == 1
+    assert b"col[1500001]=5005 out of range" in L.gbc_last_error()
+    rowbad = row.copy()
+    rowbad[700] = rowbad[702] + 1
+    assert L.gbc_graph_create(rowbad, bad, n, C.byref(h)) == 1
+    assert b"decrease at 700" in L.gbc_last_error()
+    for r, c, msg in ((row, bad, b"col[1500001]=5005 out of range"), (rowbad, col, b"decrease at 700")):
+        d_row, d_col = torch.from_numpy(r).cuda(), torch.from_numpy(c).cuda()
+        assert L.gbc_graph_create_device(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), n, m,
+                                         C.byref(h)) == 1
+        assert msg in L.gbc_last_error()
+    d_row, d_col = torch.from_numpy(row).cuda(), torch.from_numpy(col).cuda()
+    assert L.gbc_graph_create_device(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), n, m - 1,
+                                     C.byref(h)) == 1
+    assert b"row[n] != m" in L.gbc_last_error()
