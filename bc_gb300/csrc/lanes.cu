@@ -1702,6 +1702,16 @@ __global__ void profile_key_kernel(KArgs A, int lvl_bytes, uint32_t* __restrict_
     }
 }
 
+// *out += number of vertices with more than thr neighbours; whole blocks step
+// together so that every lane takes part in the warp sum.
+__global__ void count_hubs_kernel(const int64_t* __restrict__ row, int32_t n, int64_t thr, uint32_t* __restrict__ out) {
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = base + threadIdx.x;
+        const unsigned c = __reduce_add_sync(0xFFFFFFFFu, (v < n && row[v + 1] - row[v] > thr) ? 1u : 0u);
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+    }
+}
+
 // bc[v] = sum over lane groups of the per-group partials (fixed order).
 __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, double* __restrict__ bc) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -1874,10 +1884,13 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     }
     // hub entries: at most 32 levels' worth per (hub vertex, group) to start with
     {
-        std::vector<int64_t> hrow(n + 1);
-        GBC_CUDA(cudaMemcpy(hrow.data(), g->row, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
-        n_hubs_ = 0;
-        for (size_t v = 0; v < n; v++) n_hubs_ += (hrow[v + 1] - hrow[v]) > (gs_ == 7 ? HUB_DEG_Q : HUB_DEG);
+        uint32_t nh = 0;
+        GBC_CUDA(cudaMemsetAsync(ovf_, 0, sizeof(uint32_t), stream_));
+        count_hubs_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(g->row, g->n, gs_ == 7 ? HUB_DEG_Q : HUB_DEG, ovf_);
+        GBC_CUDA(cudaGetLastError());
+        GBC_CUDA(cudaMemcpyAsync(&nh, ovf_, sizeof nh, cudaMemcpyDeviceToHost, stream_));
+        GBC_CUDA(cudaStreamSynchronize(stream_));
+        n_hubs_ = nh;
     }
     GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));

@@ -285,3 +285,37 @@ def test_group128_deep_and_wide(gpu, orc):
         got = G.bc(src, group_lanes=128)
         assert G.stats()["sigma_mode_used"] == gpu.SIGMA_WIDE
         assert relerr(got, ref) < TOL_F64
+
+
+def test_group128_hub_with_wide_sigma(gpu, orc):
+    """A hub (1280 neighbours, above the CTA-wide threshold) whose path counts
+    overflow uint64: an 80x80 grid with the hub joined to the 39 vertices of
+    the anti-diagonal i+j=120 (path counts up to ~1e35 from the corner) and
+    to 1241 leaves.  The hub's sigma and delta are merged across the CTA's
+    warps in the wide form; BC against the oracle's scaled FP64 Brandes."""
+    side = 80
+    grid = gpu.gen_grid(side, side, 0.0, seed=1)
+    n0 = grid.n
+    adj = [list(grid.col[grid.row[v]:grid.row[v + 1]]) for v in range(n0)]
+    hub = n0
+    diag = [i * side + (120 - i) for i in range(120 - (side - 1), side)]
+    leaves = list(range(n0 + 1, n0 + 1 + 1280 - len(diag)))
+    adj.append(sorted(diag + leaves))
+    for v in diag:
+        adj[v].append(hub)
+    for v in leaves:
+        adj.append([hub])
+    row = np.concatenate([[0], np.cumsum([len(a) for a in adj])]).astype(np.int64)
+    col = np.concatenate([np.sort(np.array(a, np.int32)) for a in adj]).astype(np.int32)
+    csr = gpu.CSR(row, col)
+    assert row[hub + 1] - row[hub] == 1280
+    og = to_orc(orc, csr)
+    src = np.array([0, 1, side, side + 1, 79, 6399, leaves[0]], np.int32)
+    ref, novf = orc.bc(og, src, scaled=True)
+    assert novf > 0
+    with gpu.Graph(csr) as G:
+        for dp in (gpu.DELTA_F64, gpu.DELTA_F32):
+            got = G.bc(src, group_lanes=128, delta_precision=dp)
+            assert G.stats()["sigma_mode_used"] == gpu.SIGMA_WIDE
+            assert relerr(got, ref) < (TOL_F64 if dp == gpu.DELTA_F64 else TOL_F32)
+        assert np.array_equal(G.cc(src, group_lanes=128), orc.cc(og, src))
