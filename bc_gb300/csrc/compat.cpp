@@ -98,6 +98,49 @@ struct vVector* new_vec(int cap) {
     return v;
 }
 
+// Reference-semantics betweenness of the sources in `src`, added into BCs.
+void betweenness_into(struct CSR* c, const std::vector<int32_t>& src, float* BCs) {
+    std::vector<int64_t> row;
+    std::vector<int32_t> col;
+    to_native(c, false, row, col);
+    gbc_graph g = nullptr;
+    ok(gbc_graph_create(row.data(), col.data(), c->csrVSize - 1, &g), "gbc_graph_create");
+    std::vector<double> bc(c->csrVSize - 1, 0.0);
+    gbc_options o;
+    gbc_options_default(&o);
+    o.semantics = GBC_BC_REFERENCE;
+    o.delta_precision = GBC_DELTA_F64;
+    if (!src.empty()) ok(gbc_bc(g, src.data(), (int32_t)src.size(), &o, bc.data()), "gbc_bc");
+    gbc_graph_destroy(g);
+    for (int v = 0; v < c->csrVSize - 1; v++) BCs[v] += (float)bc[v];
+}
+
+// The source schedule of Seq_Brandes/Brandes.c:417-475 (computeBC_shareBased):
+// sources in id order, each not-yet-done source s followed by its first
+// not-done neighbour of degree != 1 in csrE[csrV[s] .. csrV[s+1]), which the
+// reference derives from s's traversal.  Every vertex of the range appears
+// once, so the sums equal computeBC's.
+std::vector<int32_t> shared_pair_order(const struct CSR* c) {
+    std::vector<int32_t> order;
+    std::vector<char> done(c->csrVSize, 0);
+    for (int s = c->startNodeID; s <= c->endNodeID; s++) {
+        if (done[s]) continue;
+        done[s] = 1;
+        order.push_back(s);
+        for (int e = c->csrV[s]; e < c->csrV[s + 1]; e++) {
+            const int t = c->csrE[e];
+            if (t < c->startNodeID || t > c->endNodeID || done[t]) continue;
+            const int deg = c->csrNodesDegree ? c->csrNodesDegree[t] : c->csrV[t + 1] - c->csrV[t];
+            if (deg != 1) {
+                done[t] = 1;
+                order.push_back(t);
+                break;
+            }
+        }
+    }
+    return order;
+}
+
 }  // namespace
 
 extern "C" {
@@ -207,22 +250,9 @@ struct CSR* createCSR(struct Graph* g) {
     return c;
 }
 
-void computeBC(struct CSR* c, float* BCs) {
-    std::vector<int64_t> row;
-    std::vector<int32_t> col;
-    to_native(c, false, row, col);
-    gbc_graph g = nullptr;
-    ok(gbc_graph_create(row.data(), col.data(), c->csrVSize - 1, &g), "gbc_graph_create");
-    std::vector<int32_t> src = source_range(c);
-    std::vector<double> bc(c->csrVSize - 1, 0.0);
-    gbc_options o;
-    gbc_options_default(&o);
-    o.semantics = GBC_BC_REFERENCE;
-    o.delta_precision = GBC_DELTA_F64;
-    if (!src.empty()) ok(gbc_bc(g, src.data(), (int32_t)src.size(), &o, bc.data()), "gbc_bc");
-    gbc_graph_destroy(g);
-    for (int v = 0; v < c->csrVSize - 1; v++) BCs[v] += (float)bc[v];
-}
+void computeBC(struct CSR* c, float* BCs) { betweenness_into(c, source_range(c), BCs); }
+
+void computeBC_shareBased(struct CSR* c, float* BCs) { betweenness_into(c, shared_pair_order(c), BCs); }
 
 int* computeCC(struct CSR* c, int* CCs) {
     closeness_into(c, true, GBC_ENGINE_LANES, CCs, true);

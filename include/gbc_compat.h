@@ -147,6 +147,14 @@ struct CSR* createCSR(struct Graph* adjlist);
  * is csrE[csrV[v] .. csrV[v+1]) as in the reference. */
 void computeBC(struct CSR* csr, float* BCs);
 
+/* Shared-traversal betweenness (Seq_Brandes/Brandes.c:374
+ * computeBC_shareBased): same sums as computeBC.  The sources are scheduled
+ * as the reference pairs them (each source followed by its first not-done
+ * neighbour of degree != 1), and the device's lane batches, which run many
+ * sources over one traversal of each row, stand in for its two-source
+ * derivation. */
+void computeBC_shareBased(struct CSR* csr, float* BCs);
+
 /* Closeness distance sums of every source in [startNodeID, endNodeID]
  * (Seq_CC/CC.cpp:37): CCs[s] += sum of distances.  Adjacency of v is
  * csrE[csrV[v] .. oriCsrV[v+1]) as in the reference. Returns CCs. */

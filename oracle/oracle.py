@@ -194,6 +194,7 @@ def _ref(name):
         L = C.CDLL(os.path.join(HERE, "_ref", name))
         if name == "libref_bc.so":
             L.ref_bc_file.argtypes = [C.c_char_p, C.c_int, C.c_int, _f32p, C.c_int, C.POINTER(C.c_int)]
+            L.ref_bc_shared_file.argtypes = [C.c_char_p, _f32p, C.c_int, C.POINTER(C.c_int)]
         else:
             L.ref_cc_file.argtypes = [C.c_char_p, _i32p, C.c_int, C.POINTER(C.c_int)]
             L.ref_d1ap_cc_file.argtypes = [C.c_char_p, _i32p, C.c_int, C.POINTER(C.c_int), _i32p]
@@ -206,6 +207,15 @@ def ref_bc_file(path: str, s_begin=-1, s_end=-1, cap=1 << 24):
     vs = C.c_int()
     rc = _ref("libref_bc.so").ref_bc_file(path.encode(), s_begin, s_end, out, cap, C.byref(vs))
     if rc != 0:
+        raise ValueError("capacity")
+    return out[: vs.value - 1].copy()
+
+
+def ref_bc_shared_file(path: str, cap=1 << 24):
+    """The reference's computeBC_shareBased (Seq_Brandes/Brandes.c:374), FP32."""
+    out = np.zeros(cap, np.float32)
+    vs = C.c_int()
+    if _ref("libref_bc.so").ref_bc_shared_file(path.encode(), out, cap, C.byref(vs)) != 0:
         raise ValueError("capacity")
     return out[: vs.value - 1].copy()
 

@@ -25,3 +25,16 @@ int ref_bc_file(const char* path, int s_begin, int s_end_inclusive, float* out,
     csr->endNodeID = saved_end;
     return 0;
 }
+
+/* The reference's shared-traversal variant (Seq_Brandes/Brandes.c:374
+ * computeBC_shareBased): one forward BFS from a source s also yields the BFS
+ * DAG of s's first not-done, non-leaf neighbour.  It loops from startNodeID
+ * on its own (no nextBFS global). */
+int ref_bc_shared_file(const char* path, float* out, int out_len, int* vsize) {
+    struct Graph* g = buildGraph((char*)path);
+    struct CSR* csr = createCSR(g);
+    *vsize = csr->csrVSize;
+    if (out_len < csr->csrVSize) return -1;
+    computeBC_shareBased(csr, out);
+    return 0;
+}

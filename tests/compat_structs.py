@@ -33,7 +33,7 @@ def bind(L):
     L.buildGraph.argtypes = [C.c_char_p]
     L.createCSR.restype = P(CSR)
     L.createCSR.argtypes = [C.c_void_p]
-    for name in ("computeBC",):
+    for name in ("computeBC", "computeBC_shareBased"):
         getattr(L, name).argtypes = [P(CSR), P(C.c_float)]
         getattr(L, name).restype = None
     L.computeCC.argtypes = [P(CSR), P(I)]

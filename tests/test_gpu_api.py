@@ -54,6 +54,11 @@ def test_dropin_entry_points(gpu, datasets):
         bc = np.frombuffer(bcs, np.float32).astype(np.float64)
         ref = fx["bc_ref_f32"].astype(np.float64)
         assert np.max(np.abs(bc[:-1] - ref) / np.maximum(np.abs(ref), 1.0)) < 5e-5, name
+        shs = (C.c_float * vs)()
+        L.computeBC_shareBased(c, shs)
+        sh = np.frombuffer(shs, np.float32).astype(np.float64)
+        ref = fx["bc_shared_ref_f32"].astype(np.float64)
+        assert np.max(np.abs(sh[:-1] - ref) / np.maximum(np.abs(ref), 1.0)) < 5e-5, name
         ccs = (C.c_int * vs)()
         L.computeCC(c, ccs)
         cc = np.frombuffer(ccs, np.int32)[:-1]

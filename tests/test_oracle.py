@@ -40,6 +40,17 @@ def test_bc_reference_semantics_vs_reference_fp32(orc, datasets, name):
     assert np.max(np.abs(bc[g.start:] - ref[g.start:]) / np.maximum(np.abs(ref[g.start:]), 1.0)) < 5e-5
 
 
+@pytest.mark.parametrize("name", SMALL_BC)
+def test_bc_shared_traversal_reference_vs_oracle(orc, datasets, name):
+    # The reference's computeBC_shareBased (Seq_Brandes/Brandes.c:374) derives a
+    # neighbour's BFS DAG from the source's traversal; its sums are computeBC's
+    # (reference semantics), so the same FP64 restatement pins it.
+    g = orc.load_edgelist(datasets[name])
+    ref = fixture(name)["bc_shared_ref_f32"].astype(np.float64)
+    bc, _ = orc.bc(g, np.arange(g.start, g.N), orc.BC_REFERENCE, nthreads=4)
+    assert np.max(np.abs(bc[g.start:] - ref[g.start:]) / np.maximum(np.abs(ref[g.start:]), 1.0)) < 5e-5
+
+
 def test_brandes_semantics_vs_networkx(orc, datasets):
     nx = pytest.importorskip("networkx")
     for name in ["karate.txt", "dolphins.txt", "testdata1.txt", "testdata2.txt"]:
