@@ -237,7 +237,9 @@ static gbc_status split(const int64_t* row, Reduction& R, const std::vector<int3
         }
     }
     // block graph CSR over slots
+    // a vertex that is not an articulation point has exactly one slot
     auto slot_of = [&](int32_t b, int32_t v) -> int32_t {
+        if (!R.is_ap[v]) return R.vslot[v];
         const auto& V = block_verts[b];
         return (int32_t)(R.bvoff[b] + (std::lower_bound(V.begin(), V.end(), v) - V.begin()));
     };
