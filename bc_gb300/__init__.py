@@ -55,7 +55,8 @@ class ReducedInfo(C.Structure):
     _fields_ = [("n", C.c_int32), ("d1_folded", C.c_int32), ("d1_hubs", C.c_int32), ("alive", C.c_int32),
                 ("articulation_points", C.c_int32), ("blocks", C.c_int32), ("max_block", C.c_int32),
                 ("block_slots", C.c_int32), ("block_edges", C.c_int64), ("components", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("on_device", C.c_int32), ("fold_rounds", C.c_int32), ("forest_levels", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}
@@ -96,6 +97,7 @@ _PROTOS = [
     ("gbc_cc_device", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _vp, _vp]),
     ("gbc_sssp", _st, [_vp, _i32p, C.c_int32, C.POINTER(Options), _vp, _vp, _vp]),
     ("gbc_reduce", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_reduce_host", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
     ("gbc_reduced_info_get", _st, [_vp, C.POINTER(ReducedInfo)]),
     ("gbc_cc_reduced", _st, [_vp, C.POINTER(Options), _i64p]),
     ("gbc_bc_reduced", _st, [_vp, C.POINTER(Options), _f64p]),
@@ -331,12 +333,16 @@ class Graph:
 
 
 class Reduced:
-    """D1-folded, block-split form of a host CSR (gbc_reduced handle)."""
+    """D1-folded, block-split form of a host CSR (gbc_reduced handle).
 
-    def __init__(self, csr: CSR):
+    on_host=False folds and splits on the device (gbc_reduce); on_host=True
+    runs the same reduction on the host (gbc_reduce_host)."""
+
+    def __init__(self, csr: CSR, on_host: bool = False):
         self.csr = csr
         h = _vp()
-        check(lib().gbc_reduce(csr.row, csr.col, csr.n, csr.start, C.byref(h)))
+        fn = lib().gbc_reduce_host if on_host else lib().gbc_reduce
+        check(fn(csr.row, csr.col, csr.n, csr.start, C.byref(h)))
         self.h = h
 
     def info(self) -> dict:

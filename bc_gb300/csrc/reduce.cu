@@ -30,6 +30,7 @@
 #include <mutex>
 
 #include "engine.h"
+#include "reduce.h"
 
 namespace gbc {
 
@@ -68,6 +69,9 @@ struct Reduction {
     std::vector<int32_t> ap_index;    // vertex -> index into ap_child_blocks (-1 if not AP)
     std::vector<int32_t> border;      // blocks in BFS order from the roots
     int32_t max_block = 0;
+    // where the reduction ran, and the device path's round and level counts
+    bool on_device = false;
+    int32_t fold_rounds = 0, forest_levels = 0;
     // device copy of the block graph
     std::unique_ptr<DevGraph> dg;
     int32_t* d_w = nullptr;
@@ -124,6 +128,70 @@ static void fold(const int64_t* row, const int32_t* col, Reduction& R, std::vect
     }
     R.n_hub = 0;
     for (int32_t v = R.start; v < n; v++) R.n_hub += (hub[v] && !R.folded[v]);
+}
+
+// Block-cut tree over the slots (BFS over blocks and articulation points from
+// the first block of each component) and the clone weight w' of every slot.
+static gbc_status block_tree(Reduction& R) {
+    const int32_t n = R.n;
+    R.ap_index.assign(n, -1);
+    int32_t nap = 0;
+    for (int32_t v = 0; v < n; v++) if (R.is_ap[v]) R.ap_index[v] = nap++;
+    std::vector<std::vector<int32_t>> ap_blocks(nap);
+    for (int32_t b = 0; b < R.n_blocks; b++)
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++)
+            if (R.is_ap[R.slot_v[s]]) ap_blocks[R.ap_index[R.slot_v[s]]].push_back(b);
+    R.bparent_ap.assign(R.n_blocks, -2);
+    R.ap_parent_block.assign(n, -1);
+    R.ap_child_blocks.assign(nap, {});
+    R.border.clear();
+    for (int32_t b0 = 0; b0 < R.n_blocks; b0++) {
+        if (R.bparent_ap[b0] != -2) continue;
+        R.bparent_ap[b0] = -1;
+        size_t h = R.border.size();
+        R.border.push_back(b0);
+        while (h < R.border.size()) {
+            const int32_t b = R.border[h++];
+            for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) {
+                const int32_t v = R.slot_v[s];
+                if (!R.is_ap[v] || v == R.bparent_ap[b]) continue;
+                R.ap_parent_block[v] = b;
+                for (int32_t b2 : ap_blocks[R.ap_index[v]]) {
+                    if (b2 == b) continue;
+                    R.bparent_ap[b2] = v;
+                    R.ap_child_blocks[R.ap_index[v]].push_back(b2);
+                    R.border.push_back(b2);
+                }
+            }
+        }
+    }
+    // clone weights: W_sub bottom-up, then w' per slot
+    std::vector<int64_t> wsub(R.n_blocks, 0);
+    for (int64_t h = (int64_t)R.border.size() - 1; h >= 0; h--) {
+        const int32_t b = R.border[h];
+        int64_t sum = 0;
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) {
+            const int32_t v = R.slot_v[s];
+            if (v == R.bparent_ap[b]) continue;
+            sum += R.r[v];
+            if (R.is_ap[v]) for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) sum += wsub[b2];
+        }
+        wsub[b] = sum;
+    }
+    R.slot_w.resize(R.bg.n);
+    for (int32_t b = 0; b < R.n_blocks; b++) {
+        for (int64_t s = R.bvoff[b]; s < R.bvoff[b + 1]; s++) {
+            const int32_t v = R.slot_v[s];
+            int64_t w = R.r[v];
+            if (R.is_ap[v]) {
+                if (v == R.bparent_ap[b]) w = R.comp_w[R.comp[v]] - wsub[b];
+                else for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) w += wsub[b2];
+            }
+            if (w > INT32_MAX) { set_error("clone weight exceeds int32"); return GBC_ERR_ARG; }
+            R.slot_w[s] = (int32_t)w;
+        }
+    }
+    return GBC_OK;
 }
 
 // ----------------------------------------------------- blocks (Tarjan) ----
@@ -257,62 +325,7 @@ static gbc_status split(const int64_t* row, Reduction& R, const std::vector<int3
             R.bg.col[fill[x]++] = y;
             R.bg.col[fill[y]++] = x;
         }
-    // block-cut tree: BFS over blocks / APs from the first block of each component
-    R.ap_index.assign(n, -1);
-    int32_t nap = 0;
-    for (int32_t v = 0; v < n; v++) if (R.is_ap[v]) R.ap_index[v] = nap++;
-    std::vector<std::vector<int32_t>> ap_blocks(nap);
-    for (int32_t b = 0; b < R.n_blocks; b++)
-        for (int32_t v : block_verts[b]) if (R.is_ap[v]) ap_blocks[R.ap_index[v]].push_back(b);
-    R.bparent_ap.assign(R.n_blocks, -2);
-    R.ap_parent_block.assign(n, -1);
-    R.ap_child_blocks.assign(nap, {});
-    R.border.clear();
-    for (int32_t b0 = 0; b0 < R.n_blocks; b0++) {
-        if (R.bparent_ap[b0] != -2) continue;
-        R.bparent_ap[b0] = -1;
-        size_t h = R.border.size();
-        R.border.push_back(b0);
-        while (h < R.border.size()) {
-            const int32_t b = R.border[h++];
-            for (int32_t v : block_verts[b]) {
-                if (!R.is_ap[v] || v == R.bparent_ap[b]) continue;
-                R.ap_parent_block[v] = b;
-                for (int32_t b2 : ap_blocks[R.ap_index[v]]) {
-                    if (b2 == b) continue;
-                    R.bparent_ap[b2] = v;
-                    R.ap_child_blocks[R.ap_index[v]].push_back(b2);
-                    R.border.push_back(b2);
-                }
-            }
-        }
-    }
-    // clone weights: W_sub bottom-up, then w' per slot
-    std::vector<int64_t> wsub(R.n_blocks, 0);
-    for (int64_t h = (int64_t)R.border.size() - 1; h >= 0; h--) {
-        const int32_t b = R.border[h];
-        int64_t s = 0;
-        for (int32_t v : block_verts[b]) {
-            if (v == R.bparent_ap[b]) continue;
-            s += R.r[v];
-            if (R.is_ap[v]) for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) s += wsub[b2];
-        }
-        wsub[b] = s;
-    }
-    R.slot_w.resize(ns);
-    for (int32_t b = 0; b < R.n_blocks; b++) {
-        for (size_t i = 0; i < block_verts[b].size(); i++) {
-            const int32_t v = block_verts[b][i];
-            int64_t w = R.r[v];
-            if (R.is_ap[v]) {
-                if (v == R.bparent_ap[b]) w = R.comp_w[R.comp[v]] - wsub[b];
-                else for (int32_t b2 : R.ap_child_blocks[R.ap_index[v]]) w += wsub[b2];
-            }
-            if (w > INT32_MAX) { set_error("clone weight exceeds int32"); return GBC_ERR_ARG; }
-            R.slot_w[R.bvoff[b] + i] = (int32_t)w;
-        }
-    }
-    return GBC_OK;
+    return block_tree(R);
 }
 
 // Degree relabelling of a weighted device graph: the weights move with their
@@ -568,9 +581,117 @@ struct gbc_reduced_s {
     Reduction R;
 };
 
-extern "C" {
+// The reduction on the host: O(n + m) folding and a Hopcroft-Tarjan DFS, the
+// reference's placement of this step.
+static gbc_status reduce_on_host(const int64_t* row, const int32_t* col, Reduction& R) {
+    const int32_t n = R.n, start = R.start;
+    std::vector<int32_t> lc;
+    std::vector<int64_t> lo;
+    fold(row, col, R, lc, lo);
+    std::vector<int32_t> cid(n, -1);
+    for (int32_t v = start; v < n; v++)
+        if (!R.folded[v]) { cid[v] = (int32_t)R.core_v.size(); R.core_v.push_back(v); }
+    const int32_t nc = (int32_t)R.core_v.size();
+    R.core.n = nc;
+    R.core.row.assign(nc + 1, 0);
+    R.core_w.resize(nc);
+    for (int32_t i = 0; i < nc; i++) {
+        const int32_t v = R.core_v[i];
+        R.core.row[i + 1] = R.core.row[i] + (row[v + 1] - lo[v]);
+        if (R.r[v] > INT32_MAX) { set_error("reach exceeds int32"); return GBC_ERR_ARG; }
+        R.core_w[i] = (int32_t)R.r[v];
+    }
+    R.core.col.resize(R.core.row[nc]);
+    for (int32_t i = 0; i < nc; i++) {
+        const int32_t v = R.core_v[i];
+        int64_t o = R.core.row[i];
+        for (int64_t e = lo[v]; e < row[v + 1]; e++) R.core.col[o++] = cid[lc[e]];
+    }
+    return split(row, R, lc, lo);
+}
 
-gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out) {
+// The reduction on the device (reduce_dev.cu); the host keeps the O(#folded)
+// bookkeeping of the folding order and the O(#slots) block-cut tree.
+static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduction& R) {
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    const int32_t n = R.n;
+    const int64_t M = row[n];
+    if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+    FoldSplit F;
+    {
+        int64_t* d_row = nullptr;
+        int32_t* d_col = nullptr;
+        if (cudaMalloc(&d_row, sizeof(int64_t) * ((size_t)n + 1)) != cudaSuccess ||
+            cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(M, 1)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(d_row);
+            set_error("reduction: graph allocation");
+            return GBC_ERR_NOMEM;
+        }
+        std::unique_ptr<void, void (*)(void*)> f1(d_row, [](void* p) { cudaFree(p); });
+        std::unique_ptr<void, void (*)(void*)> f2(d_col, [](void* p) { cudaFree(p); });
+        GBC_CUDA(cudaMemcpyAsync(d_row, row, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, R.stream));
+        if (M) GBC_CUDA(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * M, cudaMemcpyHostToDevice, R.stream));
+        GBC_TRY(fold_split_device(d_row, d_col, n, M, R.start, R.stream, F));
+    }
+    // folding: order by round, then vertex id; parents' reach before each absorption
+    R.r = std::move(F.r);
+    R.ff = std::move(F.ff);
+    R.parent = std::move(F.parent);
+    R.folded.assign(n, 0);
+    std::vector<int64_t> pos((size_t)F.rounds + 1, 0);
+    for (int32_t v = 0; v < n; v++)
+        if (F.fround[v] >= 0) { R.folded[v] = 1; pos[F.fround[v] + 1]++; }
+    for (int32_t k = 0; k < F.rounds; k++) pos[k + 1] += pos[k];
+    R.fold_order.resize(pos[F.rounds]);
+    for (int32_t v = 0; v < n; v++)
+        if (F.fround[v] >= 0) R.fold_order[pos[F.fround[v]]++] = v;
+    std::vector<int64_t> rc(n, 1);
+    std::vector<uint8_t> hub(n, 0);
+    R.fold_rp.resize(R.fold_order.size());
+    for (size_t i = 0; i < R.fold_order.size(); i++) {
+        const int32_t d1 = R.fold_order[i], p = R.parent[d1];
+        R.fold_rp[i] = rc[p];
+        rc[p] += rc[d1];
+        hub[p] = 1;
+    }
+    R.n_hub = 0;
+    for (int32_t v = R.start; v < n; v++) R.n_hub += (hub[v] && !R.folded[v]);
+    // the folded graph and its components
+    R.core = std::move(F.core);
+    R.core_v = std::move(F.core_v);
+    const int32_t nc = R.core.n;
+    R.core_w.resize(nc);
+    R.comp.assign(n, -1);
+    R.n_comp = F.n_comp;
+    R.comp_w.assign(R.n_comp, 0);
+    R.is_ap.assign(n, 0);
+    R.vslot.assign(n, -1);
+    for (int32_t i = 0; i < nc; i++) {
+        const int32_t v = R.core_v[i];
+        if (R.r[v] > INT32_MAX) { set_error("reach exceeds int32"); return GBC_ERR_ARG; }
+        R.core_w[i] = (int32_t)R.r[v];
+        R.comp[v] = F.core_comp[i];
+        R.comp_w[F.core_comp[i]] += R.r[v];
+        R.is_ap[v] = F.core_ap[i];
+        R.vslot[v] = F.core_vslot[i];
+    }
+    // blocks
+    R.n_blocks = (int32_t)F.bvoff.size() - 1;
+    R.bvoff = std::move(F.bvoff);
+    R.slot_v.resize(F.slot_core.size());
+    for (size_t k = 0; k < F.slot_core.size(); k++) R.slot_v[k] = R.core_v[F.slot_core[k]];
+    R.max_block = 0;
+    for (int32_t b = 0; b < R.n_blocks; b++) R.max_block = std::max<int32_t>(R.max_block, (int32_t)(R.bvoff[b + 1] - R.bvoff[b]));
+    R.bg = std::move(F.bg);
+    R.fold_rounds = F.rounds;
+    R.forest_levels = F.levels;
+    return block_tree(R);
+}
+
+static gbc_status reduce_entry(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out,
+                               bool on_device) {
     if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
     *out = nullptr;
     GBC_TRY(validate_csr(row, col, n));
@@ -583,31 +704,8 @@ gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t
     Reduction& R = H->R;
     R.n = n;
     R.start = start;
-    std::vector<int32_t> lc;
-    std::vector<int64_t> lo;
-    fold(row, col, R, lc, lo);
-    {
-        std::vector<int32_t> cid(n, -1);
-        for (int32_t v = start; v < n; v++)
-            if (!R.folded[v]) { cid[v] = (int32_t)R.core_v.size(); R.core_v.push_back(v); }
-        const int32_t nc = (int32_t)R.core_v.size();
-        R.core.n = nc;
-        R.core.row.assign(nc + 1, 0);
-        R.core_w.resize(nc);
-        for (int32_t i = 0; i < nc; i++) {
-            const int32_t v = R.core_v[i];
-            R.core.row[i + 1] = R.core.row[i] + (row[v + 1] - lo[v]);
-            if (R.r[v] > INT32_MAX) { set_error("reach exceeds int32"); return GBC_ERR_ARG; }
-            R.core_w[i] = (int32_t)R.r[v];
-        }
-        R.core.col.resize(R.core.row[nc]);
-        for (int32_t i = 0; i < nc; i++) {
-            const int32_t v = R.core_v[i];
-            int64_t o = R.core.row[i];
-            for (int64_t e = lo[v]; e < row[v + 1]; e++) R.core.col[o++] = cid[lc[e]];
-        }
-    }
-    GBC_TRY(split(row, R, lc, lo));
+    R.on_device = on_device;
+    GBC_TRY(on_device ? reduce_on_device(row, col, R) : reduce_on_host(row, col, R));
     // components of folded vertices follow their root
     for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
         const int32_t d1 = R.fold_order[i];
@@ -615,6 +713,16 @@ gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t
     }
     *out = H.release();
     return GBC_OK;
+}
+
+extern "C" {
+
+gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out) {
+    return reduce_entry(row, col, n, start, out, true);
+}
+
+gbc_status gbc_reduce_host(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out) {
+    return reduce_entry(row, col, n, start, out, false);
 }
 
 gbc_status gbc_reduced_info_get(gbc_reduced h, gbc_reduced_info* info) {
@@ -633,6 +741,9 @@ gbc_status gbc_reduced_info_get(gbc_reduced h, gbc_reduced_info* info) {
     info->block_slots = R.bg.n;
     info->block_edges = R.bg.m();
     info->components = R.n_comp;
+    info->on_device = R.on_device;
+    info->fold_rounds = R.fold_rounds;
+    info->forest_levels = R.forest_levels;
     return GBC_OK;
 }
 

@@ -200,12 +200,23 @@ typedef struct {
     int32_t block_slots;       /* vertex slots of the block graph (APs counted once per block) */
     int64_t block_edges;       /* directed CSR entries of the block graph */
     int32_t components;        /* connected components of the input (isolated slots included) */
-    int32_t reserved[7];
+    int32_t on_device;         /* 1: folded and split on the device (gbc_reduce) */
+    int32_t fold_rounds;       /* device path: peeling rounds of the folding */
+    int32_t forest_levels;     /* device path: levels of the BFS spanning forest of the folded graph */
+    int32_t reserved[4];
 } gbc_reduced_info;
 
 /* Fold and split a host CSR (vertex slots [start, n) are real vertices;
- * start = 1 marks the reference's phantom slot 0 of 1-based inputs). */
+ * start = 1 marks the reference's phantom slot 0 of 1-based inputs).
+ * Replaces D1Folding + AP_detection + AP_Copy_And_Split + rebuildGraph
+ * (Lib/D1Process/D1Process.c:5, Lib/AP_Process/AP_Process.c:6,468,1141).
+ * gbc_reduce runs the folding (peeling rounds) and the block split
+ * (Tarjan-Vishkin over a BFS spanning forest) on the device;
+ * gbc_reduce_host runs the same reduction on the host (O(n + m) folding and a
+ * Hopcroft-Tarjan DFS), where the reference runs it.  Both give the same
+ * folded vertices, articulation points, blocks and results. */
 gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out);
+gbc_status gbc_reduce_host(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out);
 gbc_status gbc_reduced_info_get(gbc_reduced r, gbc_reduced_info* info);
 /* Closeness of every vertex slot through the reduction: cc[n] (host).
  * Equal to gbc_cc over all vertices of the unreduced graph. */

@@ -102,7 +102,7 @@ def test_reader_matches_oracle_reader(gbc, orc, datasets):
 def _reduced_cc_host(gbc, orc, csr):
     """Block graph from the library, its weighted sums from the oracle, the
     library's host assembly: the whole reduction except the device BFS."""
-    R = gbc.Reduced(csr)
+    R = gbc.Reduced(csr, on_host=True)
     bg, w = R.block_graph()
     ob = orc.Graph(bg.row, bg.col)
     D = orc.cc(ob, np.arange(bg.n), w=w.astype(np.int64), ff=np.zeros(bg.n, np.int64), nthreads=4)
@@ -212,7 +212,7 @@ def test_reduced_bc_host_logic(gbc, orc, datasets, case):
         csr = gbc.add_pendants(base, 30, 3, 4)
     og = orc.Graph(csr.row, csr.col, csr.start)
     ref, _ = orc.bc(og, np.arange(csr.start, csr.n), semantics=orc.BC_BRANDES)
-    R = gbc.Reduced(csr)
+    R = gbc.Reduced(csr, on_host=True)
     core, w, vert = R.core_graph()
     info = R.info()
     assert len(vert) == info["alive"] and int(w.sum()) == csr.n - csr.start   # reach covers every vertex once

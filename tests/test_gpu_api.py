@@ -136,6 +136,87 @@ def test_reduced_bc_matches_plain_brandes(gpu, orc, datasets, case):
         R.bc(semantics=gpu.BC_REFERENCE)
 
 
+def _csr_from_edges(gpu, edges, n):
+    e = np.asarray(edges, np.int64).reshape(-1, 2)
+    u = np.concatenate([e[:, 0], e[:, 1]])
+    v = np.concatenate([e[:, 1], e[:, 0]])
+    o = np.lexsort((v, u))
+    u, v = u[o], v[o]
+    row = np.zeros(n + 1, np.int64)
+    np.add.at(row, u + 1, 1)
+    return gpu.CSR(np.cumsum(row), v.astype(np.int32))
+
+
+def _chain_of_blocks(gpu):
+    """Cycles of 3 to 7 vertices chained by shared vertices and bridges, with
+    pendant paths and a separate triangle: many articulation points."""
+    rng = np.random.default_rng(9)
+    edges, nxt, join = [], 1, 0
+    for k in range(60):
+        size = int(rng.integers(3, 8))
+        cyc = [join] + list(range(nxt, nxt + size - 1))
+        nxt += size - 1
+        edges += [(cyc[i], cyc[(i + 1) % size]) for i in range(size)]
+        join = cyc[int(rng.integers(0, size))]
+        if k % 7 == 3:                       # a bridge to the next cycle
+            edges.append((join, nxt))
+            join, nxt = nxt, nxt + 1
+        if k % 5 == 1:                       # a pendant path
+            edges += [(cyc[1], nxt), (nxt, nxt + 1)]
+            nxt += 2
+    edges += [(nxt, nxt + 1), (nxt + 1, nxt + 2), (nxt + 2, nxt)]
+    return _csr_from_edges(gpu, edges, nxt + 4)   # and one isolated vertex
+
+
+@pytest.mark.parametrize("case", ["karate", "ca-HepPh", "caida", "tech-WHOIS", "ia-email-EU", "testdata1",
+                                  "chain-of-blocks", "rmat14+pendants", "er+pendants", "grid-holes", "ba-tree",
+                                  "path-701", "star-2000"])
+def test_device_reduction_equals_host(gpu, datasets, case):
+    """gbc_reduce (folding rounds + Tarjan-Vishkin blocks on the device) and
+    gbc_reduce_host (sequential folding + DFS) give the same folded vertices,
+    articulation points, blocks, block graph and clone weights, and the same
+    closeness (exact) and betweenness."""
+    named = {"karate": "karate.txt", "ca-HepPh": "ca-HepPh.mtx", "caida": "caida.mtx", "tech-WHOIS": "tech-WHOIS.mtx",
+             "ia-email-EU": "ia-email-EU.mtx", "testdata1": "testdata1.txt"}
+    if case in named:
+        csr = gpu.read_edgelist(datasets[named[case]])
+    elif case == "chain-of-blocks":
+        csr = _chain_of_blocks(gpu)
+    elif case == "rmat14+pendants":
+        csr = gpu.add_pendants(gpu.gen_rmat(14, 4, seed=5), 3000, 3, 9)
+    elif case == "er+pendants":
+        csr = gpu.add_pendants(gpu.gen_er(4000, 1.5, seed=5), 600, 3, 9)
+    elif case == "grid-holes":
+        csr = gpu.gen_grid(60, 60, 0.3, seed=2, largest_only=False)
+    elif case == "ba-tree":
+        csr = gpu.gen_ba(3000, 1, 3)
+    elif case == "path-701":
+        csr = _csr_from_edges(gpu, [(i, i + 1) for i in range(700)], 701)
+    else:
+        csr = _csr_from_edges(gpu, [(0, i) for i in range(1, 2001)], 2001)
+    Rd, Rh = gpu.Reduced(csr), gpu.Reduced(csr, on_host=True)
+    di, hi = Rd.info(), Rh.info()
+    assert di["on_device"] == 1 and hi["on_device"] == 0
+    for k in ("n", "d1_folded", "d1_hubs", "alive", "articulation_points", "blocks", "max_block", "block_slots",
+              "block_edges", "components"):
+        assert di[k] == hi[k], (case, k, di[k], hi[k])
+    # vertices with live edges are the same; a tree component keeps one root,
+    # which may be either end of its last edge
+    cd, wd, vd = Rd.core_graph()
+    ch, wh, vh = Rh.core_graph()
+    kd, kh = np.diff(cd.row) > 0, np.diff(ch.row) > 0
+    assert np.array_equal(vd[kd], vh[kh]) and np.array_equal(wd[kd], wh[kh])
+    assert np.array_equal(np.sort(wd[~kd]), np.sort(wh[~kh]))
+    for i, j in zip(np.nonzero(kd)[0], np.nonzero(kh)[0]):
+        a, b = vd[cd.col[cd.row[i]:cd.row[i + 1]]], vh[ch.col[ch.row[j]:ch.row[j + 1]]]
+        assert np.array_equal(np.sort(a), np.sort(b))
+    (bd, bwd), (bh, bwh) = Rd.block_graph(), Rh.block_graph()
+    assert bd.n == bh.n and np.array_equal(np.sort(bwd), np.sort(bwh))
+    assert np.array_equal(Rd.cc(), Rh.cc())
+    bcd, bch = Rd.bc(), Rh.bc()
+    assert np.max(np.abs(bcd - bch) / np.maximum(np.abs(bch), 1.0)) < 1e-12
+
+
 def test_c2_config_reduction_full_size(gpu, orc):
     """The D1-folding + AP-splitting configuration at full size: R-MAT scale
     18, edge factor 4 (a=.57, b=.19, c=.19) with 60K pendant paths of depth
