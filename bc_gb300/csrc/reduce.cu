@@ -633,6 +633,8 @@ static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduc
         std::unique_ptr<void, void (*)(void*)> f2(d_col, [](void* p) { cudaFree(p); });
         GBC_CUDA(cudaMemcpyAsync(d_row, row, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, R.stream));
         if (M) GBC_CUDA(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * M, cudaMemcpyHostToDevice, R.stream));
+        GBC_TRY(check_csr_device(d_row, d_col, n, M, col, R.stream));
+        if (R.start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
         GBC_TRY(fold_split_device(d_row, d_col, n, M, R.start, R.stream, F));
     }
     // folding: order by round, then vertex id; parents' reach before each absorption
@@ -694,12 +696,15 @@ static gbc_status reduce_entry(const int64_t* row, const int32_t* col, int32_t n
                                bool on_device) {
     if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
     *out = nullptr;
-    GBC_TRY(validate_csr(row, col, n));
+    // the device path checks the entries on its device copy
+    GBC_TRY(on_device ? validate_csr_header(row, col, n) : validate_csr(row, col, n));
     if (start < 0 || start > 1 || start >= n) { set_error("start must be 0 or 1"); return GBC_ERR_ARG; }
-    if (start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
-    for (int32_t v = 0; v < n; v++)
-        for (int64_t e = row[v]; e < row[v + 1]; e++)
-            if (col[e] == v) { set_error("self-loop at vertex %d", v); return GBC_ERR_ARG; }
+    if (!on_device) {
+        if (start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
+        for (int32_t v = 0; v < n; v++)
+            for (int64_t e = row[v]; e < row[v + 1]; e++)
+                if (col[e] == v) { set_error("self-loop at vertex %d", v); return GBC_ERR_ARG; }
+    }
     auto H = std::make_unique<gbc_reduced_s>();
     Reduction& R = H->R;
     R.n = n;

@@ -29,6 +29,12 @@ struct FoldSplit {
     int32_t rounds = 0, levels = 0;   // peeling rounds, spanning-forest depth + 1
 };
 
+// The per-entry checks of the reduction's input on the device copy: row
+// offsets monotone, ids in [0, n), no self-loops (same messages as the host
+// checks).  host_col, when given, supplies the offending value for a message.
+gbc_status check_csr_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t M, const int32_t* host_col,
+                            cudaStream_t s);
+
 // Fold and split a device CSR (vertex slots [start, n) are real vertices).
 // Everything proportional to n or to the edge count runs on the device; the
 // result is copied to `out`.

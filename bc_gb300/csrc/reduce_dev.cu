@@ -103,6 +103,39 @@ __device__ __forceinline__ void uf_union(int32_t* uf, int32_t a, int32_t b, int*
     atomicExch(err, 1);
 }
 
+// ------------------------------------------------------------- CSR checks --
+// bad[0] = smallest v with row[v+1] < row[v], bad[1] = smallest e with col[e]
+// outside [0, n) (0xFFFFFFFF: none).  Whole blocks step together so that every
+// lane takes part in the warp minimum.
+__global__ void csr_entries_check_kernel(const int64_t* __restrict__ row, const int32_t* __restrict__ col, int32_t n,
+                                         int64_t m, unsigned* __restrict__ bad) {
+    const int64_t len = (int64_t)n > m ? (int64_t)n : m;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < len; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        unsigned br = ~0u, bc = ~0u;
+        if (i < n && row[i + 1] < row[i]) br = (unsigned)i;
+        if (i < m && (uint32_t)col[i] >= (uint32_t)n) bc = (unsigned)i;
+        br = __reduce_min_sync(FULLM, br);
+        bc = __reduce_min_sync(FULLM, bc);
+        if ((threadIdx.x & 31) == 0) {
+            if (br != ~0u) atomicMin(&bad[0], br);
+            if (bc != ~0u) atomicMin(&bad[1], bc);
+        }
+    }
+}
+
+// bad[2] = smallest v that lists itself (rows already known to be monotone)
+__global__ void self_loop_check_kernel(const int64_t* __restrict__ row, const int32_t* __restrict__ col, int32_t n,
+                                       unsigned* __restrict__ bad) {
+    const int t = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+        bool loop = false;
+        for (int64_t j = row[v] + t; j < row[v + 1]; j += 32) loop |= col[j] == v;
+        if (__any_sync(FULLM, loop) && t == 0) atomicMin(&bad[2], (unsigned)v);
+    }
+}
+
 // ---------------------------------------------------------------- folding --
 __global__ void fold_init_kernel(const int64_t* __restrict__ row, int32_t n, int32_t start, int32_t* __restrict__ deg,
                                  uint8_t* __restrict__ alive, int32_t* __restrict__ fround, int32_t* __restrict__ parent,
@@ -537,6 +570,30 @@ gbc_status read_u32(const unsigned* d, unsigned* h, cudaStream_t s) {
 }
 
 }  // namespace
+
+gbc_status check_csr_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t M, const int32_t* host_col,
+                            cudaStream_t s) {
+    DBuf<unsigned> bad;
+    RD_ALLOC(bad, 3);
+    GBC_CUDA(cudaMemsetAsync(bad.p, 0xFF, 3 * sizeof(unsigned), s));
+    csr_entries_check_kernel<<<grid_threads(std::max<int64_t>(n, M)), RB, 0, s>>>(d_row, d_col, n, M, bad.p);
+    unsigned h[3];
+    GBC_CUDA(cudaMemcpyAsync(h, bad.p, sizeof h, cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    if (h[0] != ~0u) { set_error("row offsets decrease at %lld", (long long)h[0]); return GBC_ERR_ARG; }
+    if (h[1] != ~0u) {
+        int32_t val = 0;
+        if (host_col) val = host_col[h[1]];
+        else GBC_CUDA(cudaMemcpy(&val, d_col + h[1], sizeof val, cudaMemcpyDeviceToHost));
+        set_error("col[%lld]=%d out of range", (long long)h[1], val);
+        return GBC_ERR_ARG;
+    }
+    self_loop_check_kernel<<<grid_warps(n), RB, 0, s>>>(d_row, d_col, n, bad.p);
+    GBC_CUDA(cudaMemcpyAsync(h, bad.p, sizeof h, cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    if (h[2] != ~0u) { set_error("self-loop at vertex %d", (int)h[2]); return GBC_ERR_ARG; }
+    return GBC_OK;
+}
 
 gbc_status fold_split_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t M, int32_t start,
                              cudaStream_t s, FoldSplit& out) {

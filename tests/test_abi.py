@@ -157,9 +157,14 @@ def test_reduce_rejects_bad_input(gbc):
     h = C.c_void_p()
     row = np.array([0, 1, 2], np.int64)
     loop = np.array([0, 1], np.int32)   # self-loop at 0
-    assert L.gbc_reduce(row, loop, 2, 0, C.byref(h)) == 1
+    assert L.gbc_reduce_host(row, loop, 2, 0, C.byref(h)) == 1
+    assert b"self-loop at vertex 0" in L.gbc_last_error()
     ok = np.array([1, 0], np.int32)
-    assert L.gbc_reduce(row, ok, 2, 1, C.byref(h)) == 1   # phantom slot with edges
+    assert L.gbc_reduce_host(row, ok, 2, 1, C.byref(h)) == 1   # phantom slot with edges
+    if gbc.device_count() == 0:
+        # the device reduction checks its argument header, then needs a device
+        assert L.gbc_reduce(row, np.array([1, 5], np.int32), 2, 0, C.byref(h)) == 9
+        assert L.gbc_reduce(row, ok, 2, 7, C.byref(h)) == 1
 
 
 def _weighted_brandes(csr, w):

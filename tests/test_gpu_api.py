@@ -217,6 +217,23 @@ def test_device_reduction_equals_host(gpu, datasets, case):
     assert np.max(np.abs(bcd - bch) / np.maximum(np.abs(bch), 1.0)) < 1e-12
 
 
+def test_device_reduction_rejects_bad_input(gpu):
+    """gbc_reduce checks the entries on its device copy before any kernel
+    indexes by them, with the host path's messages."""
+    L = gpu.lib()
+    h = C.c_void_p()
+    row = np.array([0, 1, 2], np.int64)
+    cases = [(row, np.array([0, 1], np.int32), 0, b"self-loop at vertex 0"),
+             (row, np.array([1, 0], np.int32), 1, b"phantom slot 0 must have no edges"),
+             (row, np.array([1, 2], np.int32), 0, b"col[1]=2 out of range"),
+             (np.array([0, 2, 1, 2], np.int64), np.array([1, 0], np.int32), 0, b"row offsets decrease at 1")]
+    for r, c, start, msg in cases:
+        n = len(r) - 1
+        for fn in (L.gbc_reduce, L.gbc_reduce_host):
+            assert fn(r, c, n, start, C.byref(h)) == 1, msg
+            assert msg in L.gbc_last_error(), (msg, L.gbc_last_error())
+
+
 def test_c2_config_reduction_full_size(gpu, orc):
     """The D1-folding + AP-splitting configuration at full size: R-MAT scale
     18, edge factor 4 (a=.57, b=.19, c=.19) with 60K pendant paths of depth
