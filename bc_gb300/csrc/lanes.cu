@@ -1086,6 +1086,22 @@ template <> struct Quad<uint16_t> {
 
 constexpr int Q_ITER = 8;   // neighbours whose level quads are loaded before any is used
 constexpr int FETCH_Q = 8;  // regular tasks a warp takes per fetch in 128-lane groups (8: 3% faster than 32 on R-MAT s22)
+constexpr unsigned long long TAIL_Q = 16384;   // fewer regular tasks left than this: take one per fetch
+
+// Next regular tasks of the level for this warp: FETCH_Q per atomic while
+// many remain, then one at a time, so that no warp is left holding several
+// heavy tasks while the rest of the GPU has finished the level.
+__device__ __forceinline__ unsigned long long q_fetch(const KArgs& A, unsigned long long e, int& take) {
+    unsigned long long base = 0;
+    int tk = FETCH_Q;
+    if ((threadIdx.x & 31) == 0) {
+        const unsigned long long cur = *(volatile unsigned long long*)&A.ctl->next;
+        tk = cur + TAIL_Q < e ? FETCH_Q : 1;
+        base = atomicAdd(&A.ctl->next, (unsigned long long)tk);
+    }
+    take = __shfl_sync(FULL, tk, 0);
+    return __shfl_sync(FULL, base, 0);
+}
 
 // Forward scan of one (v, g) task over neighbour chunks r0 + 32*sub, step
 // 32*nsub: thread t pulls sigma for its active lanes (act4) and discovers
@@ -1326,15 +1342,14 @@ __global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
         // regular entries: a warp takes FETCH at a time and expands them in turn
         const unsigned long long e = A.foff[d + 1];
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH_Q);
-            base = __shfl_sync(FULL, base, 0);
+            int take;
+            const unsigned long long base = q_fetch(A, e, take);
             if (base >= e) break;
             const unsigned long long my = base + t;
-            const bool mine = t < FETCH_Q && my < e;
+            const bool mine = t < take && my < e;
             const uint32_t ment = mine ? A.fq[my] : 0u;
             const long long m0 = mine ? A.row[ment >> 5] : 0, m1 = mine ? A.row[(ment >> 5) + 1] : 0;
-            const int cntE = (int)min((unsigned long long)FETCH_Q, e - base);
+            const int cntE = (int)min((unsigned long long)take, e - base);
             for (int k = 0; k < cntE; k++) {
                 const uint32_t ent = __shfl_sync(FULL, ment, k);
                 const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
@@ -1563,15 +1578,14 @@ __global__ void __launch_bounds__(BLOCK, 4) backward_q_kernel(KArgs A) {
         }
         const unsigned long long e = A.foff[d + 1];
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH_Q);
-            base = __shfl_sync(FULL, base, 0);
+            int take;
+            const unsigned long long base = q_fetch(A, e, take);
             if (base >= e) break;
             const unsigned long long my = base + t;
-            const bool mine = t < FETCH_Q && my < e;
+            const bool mine = t < take && my < e;
             const uint32_t ment = mine ? A.fq[my] : 0u;
             const long long m0 = mine ? A.row[ment >> 5] : 0, m1 = mine ? A.row[(ment >> 5) + 1] : 0;
-            const int cntE = (int)min((unsigned long long)FETCH_Q, e - base);
+            const int cntE = (int)min((unsigned long long)take, e - base);
             for (int k = 0; k < cntE; k++) {
                 const uint32_t ent = __shfl_sync(FULL, ment, k);
                 const long long r0 = __shfl_sync(FULL, m0, k), r1 = __shfl_sync(FULL, m1, k);
