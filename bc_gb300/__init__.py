@@ -36,7 +36,7 @@ class Options(C.Structure):
     _fields_ = [("semantics", C.c_int32), ("delta_precision", C.c_int32), ("sigma_mode", C.c_int32),
                 ("engine", C.c_int32), ("lanes", C.c_int32), ("sparse_lanes", C.c_int32),
                 ("levels_per_graph", C.c_int32), ("source_order", C.c_int32), ("light_steps", C.c_int32),
-                ("group_lanes", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("group_lanes", C.c_int32), ("direction", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class RunStats(C.Structure):
@@ -45,7 +45,7 @@ class RunStats(C.Structure):
                 ("frontier_entries", C.c_int64), ("sigma_overflow_lanes", C.c_int64), ("kernel_ms", C.c_double),
                 ("total_ms", C.c_double), ("lanes", C.c_int32), ("sigma_mode_used", C.c_int32),
                 ("fwd_ms", C.c_double), ("bwd_ms", C.c_double), ("fwd_kernels", C.c_int64),
-                ("bwd_kernels", C.c_int64), ("group_lanes", C.c_int32), ("reserved_stats", C.c_int32)]
+                ("bwd_kernels", C.c_int64), ("group_lanes", C.c_int32), ("bottom_up_levels", C.c_int32)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}

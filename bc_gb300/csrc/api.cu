@@ -194,6 +194,7 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("lanes must be 0 or a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
     if (o.group_lanes != 0 && o.group_lanes != 32 && o.group_lanes != 128) { set_error("group_lanes must be 0, 32 or 128"); return GBC_ERR_ARG; }
     if (o.group_lanes == 128 && o.lanes % 128) { set_error("group_lanes 128 needs lanes = 0 or a multiple of 128"); return GBC_ERR_ARG; }
+    if (o.direction != 0 && o.direction != 1) { set_error("direction must be 0 or 1"); return GBC_ERR_ARG; }
     return GBC_OK;
 }
 
@@ -389,6 +390,7 @@ static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t
     s.bwd_kernels = r.bwd_kernels;
     s.edges_traversed = -1;   // filled in lazily by gbc_graph_last_stats
     s.group_lanes = lanes == 1 ? 1 : (G->eng ? G->eng->group_lanes() : 32);
+    s.bottom_up_levels = (int32_t)r.bottom_up_levels;
     G->last_src = hsrc;
 }
 
@@ -464,6 +466,7 @@ static gbc_status cc_core(gbc_graph_s* G, const int32_t* d_src, const int32_t* h
         rq.d_src = d_src + b0;
         rq.kb = std::min(lanes, k - b0);
         rq.d_cc = d_cc + b0;
+        rq.top_down_only = o.direction == 1;
         GBC_TRY(E->run(rq, res));
         batches++;
     }

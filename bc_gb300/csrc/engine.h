@@ -40,6 +40,10 @@ size_t dev_free_bytes();
 gbc_status csr_from_edges_device(const int32_t* d_u, const int32_t* d_v, int64_t m, int32_t n, cudaStream_t s,
                                  int64_t** d_row, int32_t** d_col, int64_t* M);
 
+// Connected-component label of every vertex of a device CSR (the smallest
+// vertex id of its component), by union-find on the device (reduce_dev.cu).
+gbc_status component_labels(const int64_t* d_row, const int32_t* d_col, int32_t n, cudaStream_t s, int32_t* d_lab);
+
 struct DevGraph;
 // Reassign vertex ids by descending degree and rewrite the rows (relabel.cu).
 // g.row / g.col are replaced; *d_order[new] = old, *d_inv[old] = new.
@@ -80,6 +84,7 @@ struct LaneRequest {
     uint64_t* d_sigma = nullptr;         // [kb][n] (SSSP) nullable
     bool abort_on_overflow = false;      // exact sigma: stop before the backward sweep if a lane overflowed
     uint32_t* d_profile_key = nullptr;   // [n] (CC job): level of lane 0 << 16 | min level of lanes 1..31
+    bool top_down_only = false;          // CC job, 128-lane groups: no bottom-up levels
 };
 
 struct LaneResult {
@@ -91,6 +96,7 @@ struct LaneResult {
     int64_t graph_launches = 0;
     double fwd_ms = 0, bwd_ms = 0;      // device time inside the level-loop graphs
     int64_t fwd_kernels = 0, bwd_kernels = 0;
+    int64_t bottom_up_levels = 0;       // closeness levels discovered bottom-up
 };
 
 class LaneEngine {
@@ -159,6 +165,11 @@ private:
     double* bcg_ = nullptr;
     unsigned long long* ccbuf_ = nullptr;
     int32_t* srcw_ = nullptr;             // per-lane source weights of the running batch
+    // bottom-up closeness levels (128-lane groups), set up on the first closeness batch
+    int32_t* vcomp_ = nullptr;            // component label of every vertex
+    int32_t* lcomp_ = nullptr;            // component label of every lane's source
+    uint32_t* done_ = nullptr;            // [ng][ceil(n/32)] bits: (vertex, group) has nothing left to reach
+    size_t done_sz_ = 0;
     struct Captured { int key = -1; cudaGraphExec_t exec = nullptr; };
     std::vector<Captured> graphs_;
     int sm_count_ = 0;

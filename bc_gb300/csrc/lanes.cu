@@ -57,6 +57,14 @@ struct Ctl {
     unsigned long long htail;   // append position, hub queue
     unsigned long long next;    // fetch position of the running level, regular queue
     unsigned long long hnext;   // fetch position of the running level, hub queue
+    // direction switching (closeness, 128-lane groups)
+    int bu;                     // the running level discovers bottom-up
+    int td_only;                // this batch stays top-down
+    int bu_levels;              // bottom-up levels of this batch
+    unsigned long long fdeg;    // degree sum of the entries appended for the next level
+    unsigned long long fprev;   // the same for the running level
+    unsigned long long mu;      // bottom-up level: degree sum of (vertex, group) pairs still unreached in some lane
+    unsigned long long bnext;   // bottom-up level: fetch position over the done-bitmap words
 };
 
 struct KArgs {
@@ -86,6 +94,12 @@ struct KArgs {
     int semantics;
     int gs;                // lanes per group = 1 << gs (5: 32 lanes, one per thread; 7: 128, four per thread)
     int hub_deg;           // entries of vertices with a higher degree go to the hub queue (CTA per entry)
+    // direction switching (closeness, 128-lane groups); dir = 0 disables it
+    int dir;
+    const int32_t* vcomp;  // component label of every vertex
+    int32_t* lcomp;        // component label of every lane's source (-1: empty lane)
+    uint32_t* done;        // [ng][ceil(n/32)] bits: (vertex, group) has no reachable unreached lane
+    unsigned long long mtot;   // directed entries x lane groups
 };
 
 constexpr int HUB_DEG = 1024;   // 32-lane groups: entries of higher-degree vertices are expanded by a whole CTA
@@ -219,7 +233,8 @@ struct Sum {
 // discovers one or two vertices.
 struct Stage {
     uint32_t* buf;
-    int cnt;   // uniform across the warp
+    int cnt;                   // uniform across the warp
+    unsigned long long fdeg;   // this thread's degree sum of appended entries (direction switching)
 };
 
 __device__ __forceinline__ void stage_flush(const KArgs& A, Stage& S) {
@@ -267,8 +282,18 @@ __device__ __forceinline__ bool claim(const KArgs& A, size_t gbase, int x, int l
     return atomicExch(p, lev) != lev;
 }
 
+// Direction of the next closeness level (128-lane groups).  Top-down until
+// the frontier has passed its peak (the next frontier's edges no more than
+// the running one's) while still holding over 1/16 of all edges (x lane
+// groups): before the peak the lanes of a group sit at several distances from
+// most vertices, so a bottom-up scan of a row rarely stops early.  After a
+// bottom-up level, which measured the edges still unreached (mu), stay
+// bottom-up while the frontier's edges exceed half of those.
+constexpr unsigned long long BU_ALPHA = 2;
+constexpr unsigned long long BU_MIN_SHARE = 16;
+
 // Last CTA of a forward launch publishes the next level's frontier bounds.
-__device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, int maxd) {
+__device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, int maxd, bool dir = false) {
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -291,6 +316,17 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, 
                     if (tail == A.foff[d + 1] && htail == A.hoff[d + 1]) { A.ctl->done = 1; A.ctl->maxlevel = d; }
                     else if (d + 1 >= maxd) { A.ctl->err |= 2; A.ctl->done = 1; A.ctl->maxlevel = d; }
                     else A.ctl->level = d + 1;
+                    if (dir && !A.ctl->td_only) {
+                        const unsigned long long mf = atomicAdd(&A.ctl->fdeg, 0ULL);
+                        const unsigned long long mu = atomicAdd(&A.ctl->mu, 0ULL);
+                        A.ctl->bu = A.ctl->bu ? (mf * BU_ALPHA > mu)
+                                              : (mf <= A.ctl->fprev && mf * BU_MIN_SHARE > A.mtot);
+                        A.ctl->fprev = mf;
+                        A.ctl->bu_levels += A.ctl->bu;
+                        A.ctl->fdeg = 0;
+                        A.ctl->mu = 0;
+                        A.ctl->bnext = 0;
+                    }
                 }
             }
         }
@@ -304,12 +340,14 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, 
 template <typename LT> struct Simd;
 template <> struct Simd<uint8_t> {
     static constexpr int LPW = 4;
+    __device__ static __forceinline__ bool any_inf(unsigned w) { return __vcmpeq4(w, 0xFFFFFFFFu) != 0u; }
     __device__ static __forceinline__ unsigned bc(int d) { return ((unsigned)d & 0xFFu) * 0x01010101u; }
     __device__ static __forceinline__ unsigned eq(unsigned a, unsigned b) { return __vcmpeq4(a, b); }
     __device__ static __forceinline__ unsigned gt(unsigned a, unsigned b) { return __vcmpgtu4(a, b); }
     __device__ static __forceinline__ bool has(unsigned m, int j) { return (m >> (8 * j)) & 1u; }
 };
 template <> struct Simd<uint16_t> {
+    __device__ static __forceinline__ bool any_inf(unsigned w) { return __vcmpeq2(w, 0xFFFFFFFFu) != 0u; }
     static constexpr int LPW = 2;
     __device__ static __forceinline__ unsigned bc(int d) { return ((unsigned)d & 0xFFFFu) * 0x00010001u; }
     __device__ static __forceinline__ unsigned eq(unsigned a, unsigned b) { return __vcmpeq2(a, b); }
@@ -1165,7 +1203,9 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
             }
             const int xi = __shfl_sync(FULL, xm, (k0 + (t & (Q_ITER - 1))) & 31);
             const bool has = (t < Q_ITER) && ((want >> t) & 1u) && claim(A, gbase, xi, d + 1);
-            warp_append(A, S, has, has && is_hub(A, xi), ((uint32_t)xi << 5) | (uint32_t)g);
+            const long long dx = has ? A.row[xi + 1] - A.row[xi] : 0;
+            if (MODE == 0) S.fdeg += (unsigned long long)dx;
+            warp_append(A, S, has, dx > A.hub_deg, ((uint32_t)xi << 5) | (uint32_t)g);
         }
     }
 }
@@ -1233,7 +1273,9 @@ __device__ __forceinline__ void q_fwd_edges(const KArgs& A, Stage& S, int d, int
                         has = claim(A, gbase, x, d + 1);
                     }
                 }
-                warp_append(A, S, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
+                const long long dx = has ? A.row[x + 1] - A.row[x] : 0;
+                if (MODE == 0) S.fdeg += (unsigned long long)dx;
+                warp_append(A, S, has, dx > A.hub_deg, ((uint32_t)x << 5) | (uint32_t)g);
             }
             if (MODE == 1) {
 #pragma unroll
@@ -1271,6 +1313,129 @@ __device__ __forceinline__ void q_cc_add(const KArgs& A, unsigned long long* cc_
         if ((act4 >> j) & 1u) atomicAdd(&cc_sh[(g << 7) + 4 * t + j], (unsigned long long)c);
 }
 
+// ---- bottom-up closeness levels (128-lane groups) ---------------------------
+constexpr int BU_WORDS = 4;   // done-bitmap words (32 vertices of one group each) a warp takes per fetch
+
+// One (x, g) of a bottom-up level: the lanes of x still unreached, among those
+// whose source lies in x's component, look for a level-d neighbour; the scan
+// stops as soon as every one of them has found one.  Returns true when no
+// such lane is left (x is done in group g).
+template <typename LT>
+__device__ __forceinline__ bool q_bu_vertex(const KArgs& A, Stage& S, int d, int g, int x, unsigned long long& mu) {
+    const int t = threadIdx.x & 31;
+    LT* lv = reinterpret_cast<LT*>(A.lvl) + (((size_t)g * (size_t)A.n) << 7);
+    LT* own = lv + ((size_t)x << 7);
+    unsigned um = Quad<LT>::load(own, t).unreached();
+    if (!__any_sync(FULL, um != 0u)) return true;
+    {
+        const int cx = A.vcomp[x];
+        const int4 c4 = *reinterpret_cast<const int4*>(A.lcomp + (g << 7) + 4 * t);
+        um &= (unsigned)(c4.x == cx) | ((unsigned)(c4.y == cx) << 1) | ((unsigned)(c4.z == cx) << 2) |
+              ((unsigned)(c4.w == cx) << 3);
+    }
+    if (!__any_sync(FULL, um != 0u)) return true;
+    const long long r0 = A.row[x], r1 = A.row[x + 1];
+    unsigned found = 0;
+    bool open = true;   // uniform: some lane is still looking
+    for (long long jb = r0; jb < r1 && open; jb += 32) {
+        const int cnt = (int)min(32LL, r1 - jb);
+        const int ym = (t < cnt) ? A.col[jb + t] : 0;
+        for (int k0 = 0; k0 < cnt && open; k0 += Q_ITER) {
+            Quad<LT> q[Q_ITER];
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                const int y = __shfl_sync(FULL, ym, (k0 + i) & 31);
+                q[i] = (k0 + i < cnt) ? Quad<LT>::load(lv + ((size_t)y << 7), t) : Quad<LT>::none();
+            }
+#pragma unroll
+            for (int i = 0; i < Q_ITER; i++) {
+                const unsigned f = q[i].eq(d) & um;
+                found |= f;
+                um &= ~f;
+            }
+            open = __any_sync(FULL, um != 0u);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if ((found >> j) & 1u) own[4 * t + j] = (LT)(d + 1);
+    const long long dx = r1 - r0;
+    if (__any_sync(FULL, found != 0u)) {
+        if (t == 0) {
+            A.vmark[(size_t)g * A.n + x] = d + 1;
+            S.fdeg += (unsigned long long)dx;
+        }
+        warp_append(A, S, t == 0, dx > A.hub_deg, ((uint32_t)x << 5) | (uint32_t)g);
+    }
+    if (open && t == 0) mu += (unsigned long long)dx;
+    return !open;
+}
+
+// A bottom-up closeness level d: the closeness terms of the level-d entries
+// (which a top-down level adds while expanding them), then discovery of level
+// d+1 from the unreached side over every (vertex, group) not yet done.
+template <typename LT>
+__device__ __forceinline__ void q_bottom_up(const KArgs& A, Stage& S, unsigned long long* cc_sh, int d,
+                                            unsigned long long& mu) {
+    const int t = threadIdx.x & 31;
+    for (int pass = 0; pass < 2; pass++) {
+        unsigned long long* ctr = pass == 0 ? &A.ctl->hnext : &A.ctl->next;
+        const uint32_t* q = pass == 0 ? A.hq : A.fq;
+        const unsigned long long e = pass == 0 ? A.hoff[d + 1] : A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(ctr, 32ULL);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const uint32_t ment = base + t < e ? q[base + t] : 0u;
+            const int cnt = (int)min(32ULL, e - base);
+            for (int k = 0; k < cnt; k++) {
+                const uint32_t ent = __shfl_sync(FULL, ment, k);
+                const int v = (int)(ent >> 5), g = (int)(ent & 31u);
+                const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (((size_t)g * (size_t)A.n) << 7);
+                q_cc_add<0, LT>(A, cc_sh, d, g, v, Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d));
+            }
+        }
+    }
+    const unsigned long long nwords = (unsigned long long)((A.n + 31) >> 5);
+    const unsigned long long total = (unsigned long long)A.ng * nwords;
+    for (;;) {
+        unsigned long long wbase = 0;
+        if (t == 0) wbase = atomicAdd(&A.ctl->bnext, (unsigned long long)BU_WORDS);
+        wbase = __shfl_sync(FULL, wbase, 0);
+        if (wbase >= total) break;
+        const int nw = (int)min((unsigned long long)BU_WORDS, total - wbase);
+        for (int k = 0; k < nw; k++) {
+            const unsigned long long wi = wbase + k;
+            const int g = (int)(wi / nwords);
+            const int x0 = (int)(wi - (unsigned long long)g * nwords) << 5;
+            const uint32_t dw = A.done[wi];
+            uint32_t cand = ~dw;
+            if (x0 + 32 > A.n) cand &= (1u << (A.n - x0)) - 1u;
+            // thread t reads the whole row of vertex x0 + t: rows with no unreached lane are done
+            bool un = false;
+            if ((cand >> t) & 1u) {
+                const uint4* r = reinterpret_cast<const uint4*>(reinterpret_cast<const LT*>(A.lvl) +
+                                                                ((((size_t)g * (size_t)A.n) + (size_t)(x0 + t)) << 7));
+#pragma unroll
+                for (int i = 0; i < (int)(sizeof(LT) * 8); i++) {
+                    const uint4 w = r[i];
+                    un |= Simd<LT>::any_inf(w.x) | Simd<LT>::any_inf(w.y) | Simd<LT>::any_inf(w.z) | Simd<LT>::any_inf(w.w);
+                }
+            }
+            const uint32_t um32 = __ballot_sync(FULL, un);
+            uint32_t nd = cand & ~um32;
+            cand &= um32;
+            while (cand) {
+                const int b = __ffs(cand) - 1;
+                cand &= cand - 1u;
+                if (q_bu_vertex<LT>(A, S, d, g, x0 + b, mu)) nd |= 1u << b;
+            }
+            if (nd && t == 0) A.done[wi] = dw | nd;
+        }
+    }
+}
+
 // Forward level kernel, 128-lane groups.
 template <int MODE, typename LT>
 __global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
@@ -1288,7 +1453,11 @@ __global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
     const int d = *(volatile int*)&A.ctl->level;
     const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
     Stage S{stg[wib], 0};
-    if (!done) {
+    const bool bu = MODE == 0 && A.dir && *(volatile int*)&A.ctl->bu;
+    unsigned long long mu = 0;
+    if (!done && bu) {
+        q_bottom_up<LT>(A, S, cc_sh, d, mu);
+    } else if (!done) {
         // hub entries: one CTA per entry, warps split the neighbours
         const unsigned long long he = A.hoff[d + 1];
         for (;;) {
@@ -1372,11 +1541,21 @@ __global__ void __launch_bounds__(BLOCK, 4) expand_q_kernel(KArgs A) {
     }
     stage_flush(A, S);
     if (MODE == 0) {
+        if (A.dir) {   // the next level's frontier edges, and the edges left unreached by a bottom-up level
+            unsigned long long f = S.fdeg, m = mu;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                f += __shfl_xor_sync(FULL, f, o);
+                m += __shfl_xor_sync(FULL, m, o);
+            }
+            if (t == 0 && f) atomicAdd(&A.ctl->fdeg, f);
+            if (t == 0 && m) atomicAdd(&A.ctl->mu, m);
+        }
         __syncthreads();
         for (int i = threadIdx.x; i < (A.ng << 7); i += blockDim.x)
             if (cc_sh[i]) atomicAdd(&A.cc[i], cc_sh[i]);
     }
-    fwd_last_block(A, d, done, Lv<LT>::MAXD);
+    fwd_last_block(A, d, done, Lv<LT>::MAXD, MODE == 0 && A.dir != 0);
 }
 
 // Dependency-sweep scan of one (v, g) task: per active lane of thread t, the
@@ -1623,8 +1802,12 @@ __global__ void __launch_bounds__(BLOCK, 4) backward_q_kernel(KArgs A) {
 }
 
 // One CTA: place each lane's source at level 0 and build F_0.
-__global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, int mode, int lvl_bytes) {
+__global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, int mode, int lvl_bytes, int td_only) {
     const int l = threadIdx.x;
+    if (A.lcomp && l < (A.ng << A.gs)) {
+        const int s = l < kb ? src[l] : -1;
+        A.lcomp[l] = (s >= 0 && s < A.n) ? A.vcomp[s] : -1;
+    }
     if (l < kb) {
         const int g = l >> A.gs, t = l & ((1 << A.gs) - 1);
         const int s = src[l];
@@ -1657,6 +1840,13 @@ __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, in
         A.ctl->done = (tail == 0 && htail == 0);
         A.ctl->err = 0;
         A.ctl->blocks = 0;
+        A.ctl->bu = 0;
+        A.ctl->td_only = td_only;
+        A.ctl->bu_levels = 0;
+        A.ctl->fdeg = 0;
+        A.ctl->fprev = 0;
+        A.ctl->mu = 0;
+        A.ctl->bnext = 0;
     }
 }
 
@@ -1764,6 +1954,11 @@ struct LaneAccess {
         A.gs = e.gs_;
         A.hub_deg = e.gs_ == 7 ? HUB_DEG_Q : HUB_DEG;
         A.srcw = e.srcw_;
+        A.dir = (e.gs_ == 7 && e.vcomp_) ? 1 : 0;
+        A.vcomp = e.vcomp_;
+        A.lcomp = e.lcomp_;
+        A.done = e.done_;
+        A.mtot = (unsigned long long)e.g_->m * (unsigned long long)e.ng_;
         return A;
     }
     // Reset the lane state a batch touched: per task when few were touched,
@@ -1810,6 +2005,12 @@ void LaneEngine::release() {
     dev_release(ccbuf_, 1024 * sizeof(unsigned long long));
     dev_release(srcw_, 1024 * sizeof(int32_t));
     srcw_ = nullptr;
+    cudaFree(vcomp_);
+    cudaFree(lcomp_);
+    cudaFree(done_);
+    vcomp_ = lcomp_ = nullptr;
+    done_ = nullptr;
+    done_sz_ = 0;
     lvl_ = nullptr; sig_ = nullptr; rho_ = nullptr; vmark_ = nullptr; fq_ = nullptr; foff_ = nullptr;
     ctl_ = nullptr; ovf_ = nullptr; ctl_host_ = nullptr; bcg_ = nullptr; ccbuf_ = nullptr;
 }
@@ -2033,12 +2234,30 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
     const bool bc = rq.job != LaneJob::CC;
     if (bc && !need_bc_) { set_error("engine was initialised without BC state"); return GBC_ERR_ARG; }
     const int mode = rq.job == LaneJob::CC ? 0 : (rq.sigma_wide ? 2 : 1);
+    if (mode == 0 && gs_ == 7 && !vcomp_) {
+        // first closeness batch on 128-lane groups: component labels for the bottom-up levels
+        const size_t n = (size_t)g_->n;
+        done_sz_ = (size_t)ng_ * ((n + 31) / 32) * sizeof(uint32_t);
+        if (cudaMalloc(&vcomp_, sizeof(int32_t) * std::max<size_t>(n, 1)) != cudaSuccess ||
+            cudaMalloc(&lcomp_, sizeof(int32_t) * 1024) != cudaSuccess || cudaMalloc(&done_, std::max<size_t>(done_sz_, 4)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(vcomp_); cudaFree(lcomp_); cudaFree(done_);
+            vcomp_ = lcomp_ = nullptr;
+            done_ = nullptr;
+            set_error("bottom-up state allocation");
+            return GBC_ERR_NOMEM;
+        }
+        GBC_TRY(component_labels(g_->row, g_->col, g_->n, stream_, vcomp_));
+        for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
+        graphs_.clear();   // captured level loops hold the arguments without these buffers
+    }
     for (int attempt = 0; attempt < 4; attempt++) {
         KArgs A = LaneAccess::args(*this, rq.semantics);
         GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
         if (mode == 0) GBC_CUDA(cudaMemsetAsync(ccbuf_, 0, lanes_ * sizeof(unsigned long long), stream_));
         if (mode != 0) GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
-        seed_kernel<<<1, 1024, 0, stream_>>>(A, rq.d_src, rq.kb, mode, lvl_bytes_);
+        if (mode == 0 && done_) GBC_CUDA(cudaMemsetAsync(done_, 0, done_sz_, stream_));
+        seed_kernel<<<1, 1024, 0, stream_>>>(A, rq.d_src, rq.kb, mode, lvl_bytes_, rq.top_down_only ? 1 : 0);
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches += 1;
         cudaGraphExec_t fwd;
@@ -2096,6 +2315,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             return GBC_ERR_LIMIT;
         }
         res.levels += maxlevel + 1;
+        res.bottom_up_levels += h->bu_levels;
         res.frontier_entries += (int64_t)(entries + hentries);
         if (rq.d_profile_key) {
             profile_key_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, lvl_bytes_, rq.d_profile_key);

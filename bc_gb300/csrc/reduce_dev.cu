@@ -571,6 +571,20 @@ gbc_status read_u32(const unsigned* d, unsigned* h, cudaStream_t s) {
 
 }  // namespace
 
+gbc_status component_labels(const int64_t* d_row, const int32_t* d_col, int32_t n, cudaStream_t s, int32_t* d_lab) {
+    if (n <= 0) return GBC_OK;
+    DBuf<int32_t> uf;
+    DBuf<int> err;
+    RD_ALLOC(uf, n);
+    RD_ALLOC(err, 1);
+    GBC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+    iota_kernel<<<grid_threads(n), RB, 0, s>>>(uf.p, n);
+    cc_union_kernel<<<grid_warps(n), RB, 0, s>>>(d_row, d_col, n, uf.p, err.p);
+    uf_flatten_kernel<<<grid_threads(n), RB, 0, s>>>(uf.p, n, d_lab, nullptr);
+    GBC_CUDA(cudaGetLastError());
+    return check_err(err.p, s);   // synchronises: uf is freed on return
+}
+
 gbc_status check_csr_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int64_t M, const int32_t* host_col,
                             cudaStream_t s) {
     DBuf<unsigned> bad;

@@ -430,13 +430,18 @@ def main():
                 "note": "rel err = max|a-b|/max(|b|,1) as in the tests; the FP64-delta path is checked against the "
                         "FP64 oracle to 1e-9 in tests"}
         # closeness on the same graph: batched lanes vs the plain engine
-        graph.cc(s0, lanes=B)
+        # (direction switching: bottom-up levels on large frontiers; the top-down-only figure beside it)
+        graph.cc(s0, lanes=B, direction=1)
+        stt = graph.stats()
+        cc_td = float(ce[s0].sum()) / (stt["kernel_ms"] * 1e-3) / 1e9
+        cc_ref = graph.cc(s0, lanes=B)
         stc = graph.stats()
         cc_gteps = float(ce[s0].sum()) / (stc["kernel_ms"] * 1e-3) / 1e9
         graph.cc(s0[:args.plain_sources], engine=G.ENGINE_PLAIN)
         stp = graph.stats()
         cc_plain = float(ce[s0[:args.plain_sources]].sum()) / (stp["kernel_ms"] * 1e-3) / 1e9
         closeness = {"value": round(cc_gteps, 3), "unit": "GTEPS", "sources": int(B),
+                     "bottom_up_levels": int(stc["bottom_up_levels"]), "top_down_only": round(cc_td, 3),
                      "plain": round(cc_plain, 3), "speedup_batched_vs_plain": round(cc_gteps / cc_plain, 2)}
         plain_gteps = None
         if not args.no_plain:

@@ -79,7 +79,9 @@ typedef struct {
                                  single thread, 32 tasks per warp; 0 = never; -1 = autotune */
     int32_t group_lanes;      /* sources per lane group: 32 (one per warp thread) or 128 (four per
                                  thread; lanes must then be a multiple of 128); 0 = automatic */
-    int32_t reserved[6];
+    int32_t direction;        /* closeness with 128-lane groups: 0 = switch between top-down and
+                                 bottom-up levels by frontier size (default); 1 = top-down only */
+    int32_t reserved[5];
 } gbc_options;
 
 typedef struct {
@@ -100,7 +102,7 @@ typedef struct {
     int64_t fwd_kernels;      /* forward level kernels launched (incl. no-op tail launches) */
     int64_t bwd_kernels;      /* dependency-sweep level kernels launched */
     int32_t group_lanes;      /* lanes per group of the engine that ran (32 or 128; 1 = plain engine) */
-    int32_t reserved_stats;
+    int32_t bottom_up_levels; /* closeness levels discovered bottom-up, summed over batches */
 } gbc_run_stats;
 
 typedef struct gbc_graph_s* gbc_graph;

@@ -85,6 +85,26 @@ def test_cc_bit_exact(gpu, orc, graphs, name):
         assert np.array_equal(got_plain, ref[:50])
 
 
+@pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "rmat14", "star+grid", "grid24"])
+def test_cc_direction_switching(gpu, orc, graphs, name):
+    """Closeness on 128-lane groups with bottom-up levels on the large
+    frontiers equals the oracle and the top-down-only run bit for bit, also
+    on graphs with many components (lanes whose source lies elsewhere are
+    masked out of the early exit)."""
+    csr = graphs[name]
+    src = sources_of(csr, 512)
+    with gpu.Graph(csr) as G:
+        a = G.cc(src, lanes=256, group_lanes=128)
+        st = G.stats()
+        b = G.cc(src, lanes=256, group_lanes=128, direction=1)
+        stb = G.stats()
+    ref = orc.cc(to_orc(orc, csr), src, nthreads=8)
+    assert np.array_equal(a, ref) and np.array_equal(b, ref)
+    assert stb["bottom_up_levels"] == 0
+    if name in ("ba4096", "rmat12", "rmat14"):
+        assert st["bottom_up_levels"] > 0
+
+
 @pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "rmat14", "star+grid"])
 @pytest.mark.parametrize("sem", [0, 1])
 def test_bc_fp64(gpu, orc, graphs, name, sem):
