@@ -15,7 +15,14 @@ component / time.
           the sources are copied from pinned host memory (gbc_graph_create +
           gbc_bc) and the BC vector is read back.
   plain : the one-source-at-a-time engine on a sample of the same sources.
-  roofline / cpu_baseline / clocks as documented in DESIGN.md.
+  roofline : the dominant level kernel's algorithmic bytes per launch (adjacency
+          once + 16 B per lane and vertex of lane state per sweep, + 16 B per
+          vertex of BC accumulation in the sweep) over its CUDA-event duration,
+          against the measured HBM copy bandwidth; traffic from the committed
+          ncu summary.
+  cpu_baseline : the oracle's FP64 Brandes with all host threads on a
+          bounded sample of the same sources.
+  clocks : SM clocks and throttle reasons sampled during the timed region.
 
 --impl reference times the CPU restatement of the reference's sequential
 Brandes (oracle/, the reference's own code is not buildable on the GPU host)
