@@ -2251,7 +2251,8 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         for (auto& c : graphs_) if (c.exec) cudaGraphExecDestroy(c.exec);
         graphs_.clear();   // captured level loops hold the arguments without these buffers
     }
-    for (int attempt = 0; attempt < 4; attempt++) {
+    // retries: a queue overflow (grown up to its bound, below), a level-width switch, a sigma re-run
+    for (int attempt = 0; attempt < 8; attempt++) {
         KArgs A = LaneAccess::args(*this, rq.semantics);
         GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
         if (mode == 0) GBC_CUDA(cudaMemsetAsync(ccbuf_, 0, lanes_ * sizeof(unsigned long long), stream_));
@@ -2291,11 +2292,13 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
             GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
-            // a (vertex, group) task recurs at most once per lane of its group
+            // a (vertex, group) task recurs at most once per lane of its group.  Grow 4x: on
+            // deep graphs with 128-lane groups a task recurs at up to 128 levels, and the
+            // forward pass stops at the overflowing level, so its tail understates the need
             const unsigned long long maxcap = (unsigned long long)lanes_ * g_->n + (1ULL << 16);
             const unsigned long long hmax = (unsigned long long)lanes_ * n_hubs_ + (1ULL << 12);
-            const unsigned long long want = std::min(maxcap, std::max(fcap_ * 2, (unsigned long long)h->tail + (1ULL << 20)));
-            const unsigned long long hwant = std::min(hmax, std::max(hcap_ * 2, (unsigned long long)h->htail + (1ULL << 12)));
+            const unsigned long long want = std::min(maxcap, std::max(fcap_ * 4, (unsigned long long)h->tail + (1ULL << 20)));
+            const unsigned long long hwant = std::min(hmax, std::max(hcap_ * 4, (unsigned long long)h->htail + (1ULL << 12)));
             if (want <= fcap_ && hwant <= hcap_) { set_error("frontier queue cannot grow"); return GBC_ERR_LIMIT; }
             GBC_TRY(alloc_queue(std::max(want, fcap_), std::max(hwant, hcap_)));
             continue;

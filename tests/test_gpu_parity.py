@@ -307,6 +307,25 @@ def test_group128_deep_and_wide(gpu, orc):
         assert relerr(got, ref) < TOL_F64
 
 
+def test_group128_grid_queue_growth(gpu, orc):
+    """128-lane groups of random sources on a grid: a (vertex, group) task
+    recurs at up to 128 levels, far beyond the first frontier queue, which
+    has to grow several times within one batch.  Betweenness (wide path
+    counts) and closeness against the oracle."""
+    grid = gpu.gen_grid(200, 200, 0.05, seed=3)
+    og = to_orc(orc, grid)
+    src = np.random.default_rng(7).choice(grid.n, 512, replace=False).astype(np.int32)
+    ref, _ = orc.bc(og, src, scaled=True, nthreads=8)
+    with gpu.Graph(grid) as G:
+        got = G.bc(src, lanes=512, group_lanes=128)
+        st = G.stats()
+        cc = G.cc(src, lanes=512, group_lanes=128)
+    assert st["group_lanes"] == 128 and st["sigma_mode_used"] == gpu.SIGMA_WIDE
+    assert st["frontier_entries"] > 8 * 4 * grid.n    # beyond the initial queue of 8 entries per (vertex, group)
+    assert relerr(got, ref) < TOL_F64
+    assert np.array_equal(cc, orc.cc(og, src, nthreads=8))
+
+
 def test_group128_hub_with_wide_sigma(gpu, orc):
     """A hub (1280 neighbours, above the CTA-wide threshold) whose path counts
     overflow uint64: an 80x80 grid with the hub joined to the 39 vertices of
