@@ -209,7 +209,7 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
 static int32_t group_of(const gbc_graph_s* G, const gbc_options& o) {
     if (o.group_lanes) return o.group_lanes;
     if (G->tuned.done && G->tuned.group) return G->tuned.group;
-    return (G->key_depth > 0 && G->key_depth <= 32) ? 128 : 32;
+    return (G->key_depth > 0 && G->key_depth <= SMALL_WORLD_DEPTH) ? 128 : 32;
 }
 
 static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested, int32_t group) {
@@ -254,14 +254,13 @@ static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_o
 
 // Level-profile key of every vertex: one forward batch from the 32 highest-
 // degree vertices; key = (level from the top vertex, nearest of the others).
-static gbc_status ensure_order_key(gbc_graph_s* G) {
-    if (!G->key.empty()) return GBC_OK;
-    const DevGraph& g = G->g;
+// The graph's ids must be in descending degree order (every device graph of
+// this library is relabelled so), so the 32 highest-degree vertices are ids
+// 0..31.  depth = levels of that batch.
+gbc_status level_profile_key(const DevGraph& g, cudaStream_t stream, std::vector<uint32_t>& key, int32_t& depth) {
     // its own narrow engine: the main engine's group width depends on the depth found here
     LaneEngine E;
-    GBC_TRY(E.init(&g, 32, false, -1, 0, G->stream, 32));
-    // every graph handle is relabelled by descending degree (finish_graph), so
-    // the kb highest-degree vertices are ids 0..kb-1
+    GBC_TRY(E.init(&g, 32, false, -1, 0, stream, 32));
     const int32_t kb = std::min<int32_t>(32, g.n);
     std::vector<int32_t> idx(kb);
     for (int32_t v = 0; v < kb; v++) idx[v] = v;
@@ -278,8 +277,8 @@ static gbc_status ensure_order_key(gbc_graph_s* G) {
     struct Bufs {
         cudaStream_t s; int32_t* hub; uint32_t* key; size_t skey;
         ~Bufs() { cudaStreamSynchronize(s); dev_release(hub, sizeof(int32_t) * 32); dev_release(key, skey); }
-    } bufs{G->stream, d_hub, d_key, skey};
-    GBC_CUDA(cudaMemcpyAsync(d_hub, idx.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, G->stream));
+    } bufs{stream, d_hub, d_key, skey};
+    GBC_CUDA(cudaMemcpyAsync(d_hub, idx.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream));
     LaneRequest rq;
     rq.job = LaneJob::CC;
     rq.d_src = d_hub;
@@ -287,11 +286,16 @@ static gbc_status ensure_order_key(gbc_graph_s* G) {
     rq.d_profile_key = d_key;
     LaneResult res;
     GBC_TRY(E.run(rq, res));
-    G->key_depth = (int32_t)res.levels;
-    G->key.resize(g.n);
-    GBC_CUDA(cudaMemcpyAsync(G->key.data(), d_key, sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, G->stream));
-    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    depth = (int32_t)res.levels;
+    key.resize(g.n);
+    GBC_CUDA(cudaMemcpyAsync(key.data(), d_key, sizeof(uint32_t) * g.n, cudaMemcpyDeviceToHost, stream));
+    GBC_CUDA(cudaStreamSynchronize(stream));
     return GBC_OK;
+}
+
+static gbc_status ensure_order_key(gbc_graph_s* G) {
+    if (!G->key.empty()) return GBC_OK;
+    return level_profile_key(G->g, G->stream, G->key, G->key_depth);
 }
 
 // Reorder sources so that each 32-lane group holds sources with similar BFS

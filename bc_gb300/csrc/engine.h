@@ -176,6 +176,15 @@ private:
     std::vector<cudaEvent_t> ev_;       // timing events, two per graph launch
 };
 
+// Level-profile key of every vertex of a degree-relabelled device graph: one
+// 32-lane closeness batch from its 32 highest-degree vertices; key = (level
+// from the top vertex) << 16 | (nearest of the others); depth = that batch's
+// levels (api.cu).  Sources sorted by key share lane groups with sources
+// whose BFS levels move together; graphs whose depth stays within
+// SMALL_WORLD_DEPTH run on 128-lane groups.
+gbc_status level_profile_key(const DevGraph& g, cudaStream_t stream, std::vector<uint32_t>& key, int32_t& depth);
+constexpr int32_t SMALL_WORLD_DEPTH = 32;
+
 // Plain engine: one source at a time, int32 distances, uint64 sigma, the
 // level loop driven from the host with one device->host read per level.
 gbc_status plain_bc(const DevGraph* g, const int32_t* h_src, int32_t k, int semantics, int delta_f64,

@@ -78,6 +78,10 @@ struct Reduction {
     std::vector<int32_t> b_inv;       // slot -> internal id of the degree-relabelled device block graph
     cudaStream_t stream = nullptr;
     std::unique_ptr<LaneEngine> eng;
+    // lane grouping of the two device graphs: level-profile order of their
+    // vertices (internal ids) and the group width it implies
+    std::vector<int32_t> b_order, c_order;
+    int32_t b_group = 0, c_group = 0;
     std::mutex mu;
     ~Reduction() {
         eng.reset();
@@ -368,18 +372,35 @@ static gbc_status upload(Reduction& R) {
     return GBC_OK;
 }
 
+// Internal ids of a degree-relabelled device graph in level-profile order
+// (ties: lower id first) and the lane-group width for it, as the graph
+// handles of the API choose them.
+static gbc_status profile_order(const DevGraph& g, cudaStream_t s, std::vector<int32_t>& order, int32_t& group) {
+    std::vector<uint32_t> key;
+    int32_t depth = 0;
+    GBC_TRY(level_profile_key(g, s, key, depth));
+    order.resize(g.n);
+    for (int32_t i = 0; i < g.n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+    group = (depth > 0 && depth <= SMALL_WORLD_DEPTH) ? 128 : 32;
+    return GBC_OK;
+}
+
 // D_B(slot) for every slot, by the lane engine over the block graph.
 static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<int64_t>& D) {
     GBC_TRY(upload(R));
     const int32_t ns = R.bg.n;
     D.assign(ns, 0);
     if (ns == 0) return GBC_OK;
-    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + 31) / 32) * 32);
+    if (R.b_order.empty()) GBC_TRY(profile_order(*R.dg, R.stream, R.b_order, R.b_group));
+    int32_t group = o.group_lanes ? o.group_lanes : R.b_group;
+    if (o.lanes % group) group = 32;
+    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + group - 1) / group) * group);
     const size_t fr = dev_free_bytes();
-    while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(ns, lanes, false) > fr / 2) lanes -= 32;
-    if (!R.eng || R.eng->lanes() != lanes) {
+    while (!o.lanes && lanes > group && LaneEngine::bytes_needed(ns, lanes, false) > fr / 2) lanes -= group;
+    if (!R.eng || R.eng->lanes() != lanes || R.eng->group_lanes() != group) {
         R.eng = std::make_unique<LaneEngine>();
-        GBC_TRY(R.eng->init(R.dg.get(), lanes, false, o.sparse_lanes, o.levels_per_graph, R.stream));
+        GBC_TRY(R.eng->init(R.dg.get(), lanes, false, o.sparse_lanes, o.levels_per_graph, R.stream, group));
     }
     R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
     int32_t* d_src = nullptr;
@@ -392,9 +413,10 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
     }
     std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
     std::unique_ptr<void, void (*)(void*)> f2(d_cc, [](void* p) { cudaFree(p); });
-    std::vector<int32_t> src(ns);
-    for (int32_t i = 0; i < ns; i++) src[i] = R.b_inv[i];   // lane i holds slot i
-    GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, R.stream));
+    // lane i holds the i-th internal id in level-profile order; slot_of_id maps it back
+    std::vector<int32_t> slot_of_id(ns);
+    for (int32_t sl = 0; sl < ns; sl++) slot_of_id[R.b_inv[sl]] = sl;
+    GBC_CUDA(cudaMemcpyAsync(d_src, R.b_order.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, R.stream));
     LaneResult res;
     for (int32_t b0 = 0; b0 < ns; b0 += lanes) {
         LaneRequest rq;
@@ -402,10 +424,13 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
         rq.d_src = d_src + b0;
         rq.kb = std::min(lanes, ns - b0);
         rq.d_cc = d_cc + b0;
+        rq.top_down_only = o.direction == 1;
         GBC_TRY(R.eng->run(rq, res));
     }
-    GBC_CUDA(cudaMemcpyAsync(D.data(), d_cc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, R.stream));
+    std::vector<int64_t> Dl(ns);
+    GBC_CUDA(cudaMemcpyAsync(Dl.data(), d_cc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, R.stream));
     GBC_CUDA(cudaStreamSynchronize(R.stream));
+    for (int32_t i = 0; i < ns; i++) D[slot_of_id[R.b_order[i]]] = Dl[i];
     return GBC_OK;
 }
 
@@ -520,12 +545,15 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
     const int32_t nc = R.core.n;
     out.assign(nc, 0.0);
     if (nc == 0) return GBC_OK;
-    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((nc + 31) / 32) * 32);
+    if (R.c_order.empty()) GBC_TRY(profile_order(*R.cdg, R.stream, R.c_order, R.c_group));
+    int32_t group = o.group_lanes ? o.group_lanes : R.c_group;
+    if (o.lanes % group) group = 32;
+    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((nc + group - 1) / group) * group);
     const size_t fr = dev_free_bytes();
-    while (!o.lanes && lanes > 32 && LaneEngine::bytes_needed(nc, lanes, true) > fr / 2) lanes -= 32;
-    if (!R.ceng || R.ceng->lanes() != lanes) {
+    while (!o.lanes && lanes > group && LaneEngine::bytes_needed(nc, lanes, true) > fr / 2) lanes -= group;
+    if (!R.ceng || R.ceng->lanes() != lanes || R.ceng->group_lanes() != group) {
         R.ceng = std::make_unique<LaneEngine>();
-        GBC_TRY(R.ceng->init(R.cdg.get(), lanes, true, o.sparse_lanes, o.levels_per_graph, R.stream));
+        GBC_TRY(R.ceng->init(R.cdg.get(), lanes, true, o.sparse_lanes, o.levels_per_graph, R.stream, group));
     }
     R.ceng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
     int32_t* d_src = nullptr;
@@ -538,9 +566,8 @@ static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double
     }
     std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
     std::unique_ptr<void, void (*)(void*)> f2(d_bc, [](void* p) { cudaFree(p); });
-    std::vector<int32_t> src(nc);
-    for (int32_t i = 0; i < nc; i++) src[i] = i;
-    GBC_CUDA(cudaMemcpyAsync(d_src, src.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, R.stream));
+    // every core vertex once, in level-profile order (internal ids)
+    GBC_CUDA(cudaMemcpyAsync(d_src, R.c_order.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, R.stream));
     GBC_TRY(R.ceng->bc_begin());
     LaneResult res;
     bool wide = o.sigma_mode == GBC_SIGMA_WIDE;   // AUTO: later batches start wide after an overflow
