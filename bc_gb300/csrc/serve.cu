@@ -47,6 +47,9 @@ struct SGraph {
     int32_t* d_order = nullptr;
     int32_t* d_inv = nullptr;
     std::vector<int32_t> h_inv;
+    // level-profile key of every internal id: a request's sources are sorted by
+    // it, so that each 32-lane group holds sources whose BFS levels move together
+    std::vector<uint32_t> key;
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
@@ -387,6 +390,8 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     GBC_TRY(relabel_by_degree(G->g, G->stream, &G->d_order, &G->d_inv));
     G->h_inv.resize(n);
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    int32_t depth = 0;
+    GBC_TRY(level_profile_key(G->g, G->stream, G->key, depth));
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
@@ -408,10 +413,12 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
     if (kind < GBC_Q_CC || kind > GBC_Q_BC_SAMPLED) { set_error("bad query kind"); return GBC_ERR_ARG; }
     auto r = std::make_unique<Req>();
     int32_t n = 0;
+    const SGraph* SG = nullptr;   // graphs are never removed while the server lives
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (gid < 0 || gid >= (int32_t)s->graphs.size()) { set_error("unknown graph %d", gid); return GBC_ERR_NOT_FOUND; }
-        n = s->graphs[gid]->g.n;
+        SG = s->graphs[gid].get();
+        n = SG->g.n;
     }
     gbc_options_default(&r->opt);
     if (opt) r->opt = *opt;
@@ -427,6 +434,9 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
         r->src.resize(n);
         for (int32_t i = 0; i < n; i++) r->src[i] = i;
     }
+    // sources in level-profile order (results are per vertex, so the order is free)
+    std::stable_sort(r->src.begin(), r->src.end(),
+                     [&](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
     if (r->bc()) {
         if (cudaMalloc(&r->d_bc, sizeof(double) * n) != cudaSuccess || cudaMemset(r->d_bc, 0, sizeof(double) * n) != cudaSuccess) {
             cudaGetLastError();

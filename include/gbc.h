@@ -309,8 +309,9 @@ gbc_status gbc_server_wait(gbc_server s, int64_t req_id, double timeout_ms, int3
 gbc_status gbc_server_fetch(gbc_server s, int64_t req_id, double* bc, int64_t* cc, double* latency_ms);
 gbc_status gbc_server_cancel(gbc_server s, int64_t req_id);
 /* The source vertices of a request (the drawn sample for GBC_Q_BC_SAMPLED):
- * *k = count; out (may be NULL) receives them if cap >= count.  Valid until
- * the request is fetched. */
+ * *k = count; out (may be NULL) receives them if cap >= count, in the order
+ * the server runs them (grouped by BFS level profile, not the draw order).
+ * Valid until the request is fetched. */
 gbc_status gbc_server_sources(gbc_server s, int64_t req_id, int32_t* out, int32_t cap, int32_t* k);
 /* Aggregate counters: completed requests, lane batches, shared batches
  * (batches that carried sources of more than one request), edges traversed. */
