@@ -97,6 +97,7 @@ _PROTOS = [
     ("gbc_cc_device", _st, [_vp, _vp, C.c_int32, C.POINTER(Options), _vp, _vp]),
     ("gbc_sssp", _st, [_vp, _i32p, C.c_int32, C.POINTER(Options), _vp, _vp, _vp]),
     ("gbc_reduce", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_set_device", _st, [C.c_int]),
     ("gbc_reduce_host", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
     ("gbc_reduced_info_get", _st, [_vp, C.POINTER(ReducedInfo)]),
     ("gbc_cc_reduced", _st, [_vp, C.POINTER(Options), _i64p]),

@@ -493,6 +493,14 @@ int gbc_device_count(void) {
     return n;
 }
 
+gbc_status gbc_set_device(int device) {
+    const int n = gbc_device_count();
+    if (n == 0) { set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    if (device < 0 || device >= n) { set_error("device %d out of range [0,%d)", device, n); return GBC_ERR_ARG; }
+    GBC_CUDA(cudaSetDevice(device));
+    return GBC_OK;
+}
+
 void gbc_options_default(gbc_options* o) {
     if (!o) return;
     std::memset(o, 0, sizeof *o);

@@ -352,7 +352,13 @@ gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out) {
     S->nworkers = S->cfg.workers ? S->cfg.workers : 4;
     S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : dev_free_bytes() / 2;
     gbc_server_s* raw = S.get();
-    for (int32_t w = 0; w < S->nworkers; w++) S->workers.emplace_back([raw] { raw->run(); });
+    int dev = 0;
+    GBC_CUDA(cudaGetDevice(&dev));   // the workers run on the creating thread's device
+    for (int32_t w = 0; w < S->nworkers; w++)
+        S->workers.emplace_back([raw, dev] {
+            cudaSetDevice(dev);
+            raw->run();
+        });
     *out = S.release();
     return GBC_OK;
 }

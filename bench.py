@@ -327,6 +327,7 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
+    G.check(G.lib().gbc_set_device(dev.index))   # the library's own (static) CUDA runtime
 
     csr, sample = make_graph(args)
     ce = comp_edges(csr)

@@ -112,6 +112,12 @@ const char* gbc_last_error(void);
 const char* gbc_version(void);
 /* Number of CUDA devices visible (0 when none; never fails). */
 int gbc_device_count(void);
+/* Make `device` the calling thread's device for the library's own CUDA
+ * runtime (it is linked statically, so a device chosen through another
+ * runtime, e.g. a framework's, need not reach it).  Graphs, engines and
+ * servers live on the device that was current when they were created; a
+ * server's worker threads use its device. */
+gbc_status gbc_set_device(int device);
 
 /* ---- device-resident graphs ------------------------------------------- */
 /* Upload an undirected CSR (both directions of every edge present):

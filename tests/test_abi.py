@@ -261,3 +261,9 @@ def test_score_file_matches_reference_layout(gbc, orc, datasets, tmp_path):
         assert abs(float(a) - float(b)) <= 2e-6 * max(1.0, float(b))
     gbc.write_scores(str(out), bc, csr.start, csr.start, append=True)
     assert out.read_text().splitlines()[-2:] == ["1 1", got[1]]
+
+
+def test_set_device_without_gpu(gbc):
+    if gbc.device_count() > 0:
+        pytest.skip("a device is visible")
+    assert gbc.lib().gbc_set_device(0) == 9    # GBC_ERR_NO_DEVICE

@@ -383,3 +383,11 @@ def test_device_side_csr_validation(gpu):
     assert L.gbc_graph_create_device(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), n, m - 1,
                                      C.byref(h)) == 1
     assert b"row[n] != m" in L.gbc_last_error()
+
+
+def test_set_device(gpu):
+    L = gpu.lib()
+    n = gpu.device_count()
+    assert L.gbc_set_device(0) == 0
+    assert L.gbc_set_device(n) == 1 and b"out of range" in L.gbc_last_error()
+    assert L.gbc_set_device(-1) == 1
