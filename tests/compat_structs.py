@@ -1,6 +1,7 @@
 """ctypes mirrors of the reference structs declared in include/gbc_compat.h
 (field order and types of Lib/CSR/CSR.h:34-95 and Lib/AdjList/AdjList.h)."""
 import ctypes as C
+import os
 
 P = C.POINTER
 I = C.c_int
@@ -52,3 +53,18 @@ def bind(L):
 def load(L, path):
     g = L.buildGraph(path.encode())
     return g, L.createCSR(g)
+
+
+def build_dropin_driver(gbc, out_dir):
+    """Compile tests/dropin_driver.c with gcc against include/gbc_compat.h and
+    link it with -lgbc, as a reference driver would be; returns the binary."""
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    libdir = os.path.dirname(gbc.build.LIB)
+    exe = os.path.join(str(out_dir), "dropin_driver")
+    cmd = ["gcc", "-O2", "-Wall", "-I", os.path.join(root, "include"), os.path.join(here, "dropin_driver.c"),
+           "-L", libdir, "-lgbc", "-Wl,-rpath," + libdir, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe

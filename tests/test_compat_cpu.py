@@ -7,7 +7,7 @@ import os
 
 import numpy as np
 
-from compat_structs import bind, load
+from compat_structs import bind, build_dropin_driver, load
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -42,3 +42,12 @@ def test_struct_reductions_match_reference_counts(gbc, datasets):
         assert (cc.foldedDegreeOneCount, cc.hubNodeCount, cc.ordinaryNodeCount) == (st["d1"], st["hub"], st["ordinary"])
         L.AP_detection(c)
         assert c.contents.ap_count == st["ap"], name
+
+
+def test_dropin_driver_compiles_and_links(gbc, tmp_path):
+    """A C driver written against include/gbc_compat.h builds with gcc and links
+    with -lgbc alone: every symbol of the struct-CSR sequence it calls
+    (buildGraph, createCSR, computeBC, computeCC, the D1+AP closeness) is
+    exported with a C signature."""
+    exe = build_dropin_driver(gbc, tmp_path)
+    assert os.path.exists(exe)

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from compat_structs import bind, load
+from compat_structs import bind, build_dropin_driver, load
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -391,3 +391,23 @@ def test_set_device(gpu):
     assert L.gbc_set_device(0) == 0
     assert L.gbc_set_device(n) == 1 and b"out of range" in L.gbc_last_error()
     assert L.gbc_set_device(-1) == 1
+
+
+def test_dropin_driver_on_karate(gpu, datasets, tmp_path):
+    """The C driver built against include/gbc_compat.h reproduces the
+    reference's golden BC file for karate and its closeness outputs."""
+    import subprocess
+    exe = build_dropin_driver(gpu, tmp_path)
+    prefix = str(tmp_path / "karate")
+    r = subprocess.run([exe, datasets["karate.txt"], prefix], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    gold = np.loadtxt(os.path.join(GOLDEN, "karate_BC_Score.txt"), skiprows=1)
+    with open(prefix + "_bc.txt") as f:
+        assert f.readline().split() == ["1", "34"]
+    got = np.loadtxt(prefix + "_bc.txt", skiprows=1)
+    assert np.max(np.abs(got - gold) / np.maximum(gold, 1.0)) < 2e-6
+    fx = fixture("karate.txt")
+    assert np.array_equal(np.loadtxt(prefix + "_cc.txt", dtype=np.int64), fx["cc_ref"][1:])
+    assert np.array_equal(np.loadtxt(prefix + "_d1ap.txt", dtype=np.int64), fx["d1ap_cc_ref"][1:])
+    st = STRUCT["karate.txt"]
+    assert r.stdout.split()[:6] == ["folded", str(st["d1"]), "hubs", str(st["hub"]), "aps", str(st["ap"])]
