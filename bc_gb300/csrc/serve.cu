@@ -8,9 +8,10 @@
 // launches.  Each registered graph keeps its CSR in HBM and, while it has
 // work, one lane engine sized to its pending sources.  A lane batch is filled
 // from every admitted request on one graph that wants the same kind of sweep
-// (closeness or betweenness), oldest first; a request takes whole 32-lane groups, so its betweenness
-// partials stay separate and are added into its own FP64 result vector after
-// each batch.  Requests that arrive while a batch runs join the next batch.
+// (closeness or betweenness), oldest first; a request takes whole lane groups
+// (128 lanes on small-world graphs, else 32, as graph handles choose them), so
+// its betweenness partials stay separate and are added into its own FP64
+// result vector after each batch.  Its sources run in level-profile order.  Requests that arrive while a batch runs join the next batch.
 // Engines are created under an HBM budget and idle ones are released when a
 // new graph needs room.
 #include <cuda_runtime.h>
@@ -50,6 +51,7 @@ struct SGraph {
     // level-profile key of every internal id: a request's sources are sorted by
     // it, so that each 32-lane group holds sources whose BFS levels move together
     std::vector<uint32_t> key;
+    int32_t group = 32;          // lanes per lane group: 128 on small-world graphs, as on graph handles
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
@@ -126,8 +128,10 @@ namespace {
 // replaced when more sources wait than it holds; its buffers go to the cache.
 gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy, int64_t pending) {
     SGraph& G = *S->graphs[gi];
-    const int32_t want = (int32_t)std::min<int64_t>(S->max_lanes, std::max<int64_t>(32, (pending + 31) / 32 * 32));
-    if (G.eng && (G.eng->lanes() >= want || G.eng->lanes() >= S->max_lanes)) return GBC_OK;
+    const int32_t gr = G.group;
+    const int32_t cap = S->max_lanes / gr * gr;
+    const int32_t want = (int32_t)std::min<int64_t>(cap, std::max<int64_t>(gr, (pending + gr - 1) / gr * gr));
+    if (G.eng && (G.eng->lanes() >= want || G.eng->lanes() >= cap)) return GBC_OK;
     G.eng.reset();
     int32_t lanes = want;
     for (;;) {
@@ -141,11 +145,11 @@ gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& g
             }
         }
         if (used + need <= S->budget) break;
-        if (lanes <= 32) { set_error("graph does not fit the HBM budget"); return GBC_ERR_BUSY; }
-        lanes = std::max(32, lanes / 2);
+        if (lanes <= gr) { set_error("graph does not fit the HBM budget"); return GBC_ERR_BUSY; }
+        lanes = std::max(gr, lanes / 2 / gr * gr);
     }
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream));
+    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream, gr));
     if (G.lanes != lanes) {
         cudaFree(G.d_src);
         cudaFree(G.d_dst);
@@ -230,6 +234,7 @@ void gbc_server_s::run() {
                     continue;
                 }
                 lanes = graphs[gi]->lanes;
+                const int32_t grp = graphs[gi]->group;
                 // fill the batch: oldest request's kind, whole lane groups per request
                 kind = -1;
                 int32_t used = 0;
@@ -241,12 +246,12 @@ void gbc_server_s::run() {
                     if (kind < 0) kind = rk;
                     if (rk != kind) continue;
                     const int32_t room = lanes - used;
-                    if (room < 32) break;
+                    if (room < grp) break;
                     const int32_t take = (int32_t)std::min<size_t>(room, r->src.size() - r->next);
                     slots.push_back({r, r->next, take, used});
                     r->next += take;
                     r->inflight++;
-                    used += ((take + 31) / 32) * 32;
+                    used += ((take + grp - 1) / grp) * grp;
                 }
                 Gp = graphs[gi].get();
                 Gp->running = true;
@@ -257,15 +262,16 @@ void gbc_server_s::run() {
         // device work outside the lock
         SGraph& G = *Gp;
         cudaStream_t stream = G.stream;
-        const int32_t ng = lanes / 32;
+        const int32_t grp = G.group;
+        const int32_t ng = lanes / grp;
         hsrc.assign(lanes, -1);
         hdst.assign(ng, nullptr);
         int32_t kb = 0;
         const bool bc_batch = kind > 0;
         for (auto& sl : slots) {
             for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = G.h_inv[sl.r->src[sl.first + i]];
-            for (int32_t gg = sl.lane0 / 32; gg < (sl.lane0 + sl.count + 31) / 32; gg++) hdst[gg] = sl.r->d_bc;
-            kb = std::max(kb, ((sl.lane0 + sl.count + 31) / 32) * 32);
+            for (int32_t gg = sl.lane0 / grp; gg < (sl.lane0 + sl.count + grp - 1) / grp; gg++) hdst[gg] = sl.r->d_bc;
+            kb = std::max(kb, ((sl.lane0 + sl.count + grp - 1) / grp) * grp);
         }
         gbc_status st = GBC_OK;
         if (cudaMemcpyAsync(G.d_src, hsrc.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
@@ -398,6 +404,7 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     int32_t depth = 0;
     GBC_TRY(level_profile_key(G->g, G->stream, G->key, depth));
+    G->group = (depth > 0 && depth <= SMALL_WORLD_DEPTH && s->max_lanes % 128 == 0) ? 128 : 32;
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
