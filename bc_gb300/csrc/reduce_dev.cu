@@ -258,6 +258,20 @@ __global__ void cc_union_kernel(const int64_t* __restrict__ crow, const int32_t*
         }
 }
 
+// Link every vertex with its first two neighbours (one warp per vertex): on a
+// power-law graph this forms most of the giant component with little
+// contention, so that the full pass below mostly finds equal roots at once.
+__global__ void cc_link_sample_kernel(const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol, int32_t nc,
+                                      int32_t* uf, int* err) {
+    for (int32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nc; u += gridDim.x * blockDim.x)
+        for (int64_t j = crow[u]; j < crow[u + 1] && j < crow[u] + 2; j++) uf_union(uf, u, ccol[j], err);
+}
+
+// uf[v] = root of v, in place (no unions run meanwhile, so the roots are fixed)
+__global__ void uf_compress_kernel(int32_t* uf, int32_t nc) {
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nc; v += gridDim.x * blockDim.x) uf[v] = uf_find(uf, v);
+}
+
 // lab[v] = smallest vertex of v's set; roots[v] = 1 for the smallest vertices
 __global__ void uf_flatten_kernel(int32_t* uf, int32_t nc, int32_t* __restrict__ lab, int32_t* __restrict__ isroot) {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nc; v += gridDim.x * blockDim.x) {
@@ -393,11 +407,25 @@ __global__ void lohi_up_kernel(const int32_t* __restrict__ q, unsigned cnt, cons
     }
 }
 
-// the two joining rules over tree edges (named by their child vertex)
-__global__ void tv_union_kernel(const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol,
-                                const int32_t* __restrict__ parent, const int32_t* __restrict__ pre,
-                                const int32_t* __restrict__ nd, const int32_t* __restrict__ lo,
-                                const int32_t* __restrict__ hi, int32_t nc, int32_t* uf, int* err) {
+// The two joining rules over tree edges (named by their child vertex).
+// (b): the edge into u joins the edge into its parent (one per vertex); run
+// first, so that the many cross edges of rule (a) mostly find equal roots.
+__global__ void tv_union_tree_kernel(const int32_t* __restrict__ parent, const int32_t* __restrict__ pre,
+                                     const int32_t* __restrict__ nd, const int32_t* __restrict__ lo,
+                                     const int32_t* __restrict__ hi, int32_t nc, int32_t* uf, int* err) {
+    for (int32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nc; u += gridDim.x * blockDim.x) {
+        const int32_t pu = parent[u];
+        if (pu >= 0 && parent[pu] >= 0) {
+            const int32_t pv = pre[pu];
+            if (lo[u] < pv || hi[u] >= pv + nd[pu]) uf_union(uf, u, pu, err);
+        }
+    }
+}
+
+// (a): a non-tree edge between unrelated endpoints joins the edges into both (one warp per vertex)
+__global__ void tv_union_cross_kernel(const int64_t* __restrict__ crow, const int32_t* __restrict__ ccol,
+                                      const int32_t* __restrict__ parent, const int32_t* __restrict__ pre,
+                                      const int32_t* __restrict__ nd, int32_t nc, int32_t* uf, int* err) {
     const int t = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nc; u += nw) {
@@ -406,11 +434,7 @@ __global__ void tv_union_kernel(const int64_t* __restrict__ crow, const int32_t*
             const int32_t w = ccol[j];
             if (w == pu || parent[w] == u) continue;
             const int32_t pw = pre[w];
-            if (pw > preu && pw >= preu + ndu) uf_union(uf, (int32_t)u, w, err);   // (a) unrelated endpoints
-        }
-        if (t == 0 && pu >= 0 && parent[pu] >= 0) {
-            const int32_t pv = pre[pu];
-            if (lo[u] < pv || hi[u] >= pv + nd[pu]) uf_union(uf, (int32_t)u, pu, err);   // (b)
+            if (pw > preu && pw >= preu + ndu) uf_union(uf, (int32_t)u, w, err);
         }
     }
 }
@@ -579,6 +603,8 @@ gbc_status component_labels(const int64_t* d_row, const int32_t* d_col, int32_t 
     RD_ALLOC(err, 1);
     GBC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
     iota_kernel<<<grid_threads(n), RB, 0, s>>>(uf.p, n);
+    cc_link_sample_kernel<<<grid_threads(n), RB, 0, s>>>(d_row, d_col, n, uf.p, err.p);
+    uf_compress_kernel<<<grid_threads(n), RB, 0, s>>>(uf.p, n);
     cc_union_kernel<<<grid_warps(n), RB, 0, s>>>(d_row, d_col, n, uf.p, err.p);
     uf_flatten_kernel<<<grid_threads(n), RB, 0, s>>>(uf.p, n, d_lab, nullptr);
     GBC_CUDA(cudaGetLastError());
@@ -701,6 +727,8 @@ gbc_status fold_split_device(const int64_t* d_row, const int32_t* d_col, int32_t
     RD_ALLOC(level, nc); RD_ALLOC(par, nc); RD_ALLOC(nd, nc); RD_ALLOC(pre, nc); RD_ALLOC(lo, nc); RD_ALLOC(hi, nc);
     RD_ALLOC(order, nc);
     iota_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc);
+    cc_link_sample_kernel<<<grid_threads(nc), RB, 0, s>>>(crow.p, ccol.p, nc, uf.p, err.p);
+    uf_compress_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc);
     cc_union_kernel<<<grid_warps(nc), RB, 0, s>>>(crow.p, ccol.p, nc, uf.p, err.p);
     uf_flatten_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc, lab.p, isroot.p);
     GBC_TRY(cub_run([&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, isroot.p, cpos.p, nc, s); }, s, "component ids"));
@@ -750,7 +778,9 @@ gbc_status fold_split_device(const int64_t* d_row, const int32_t* d_col, int32_t
     DBuf<uint8_t> ap;
     RD_ALLOC(blab, nc); RD_ALLOC(nkeys, nc); RD_ALLOC(kpos, nc); RD_ALLOC(ap, nc);
     iota_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc);
-    tv_union_kernel<<<grid_warps(nc), RB, 0, s>>>(crow.p, ccol.p, par.p, pre.p, nd.p, lo.p, hi.p, nc, uf.p, err.p);
+    tv_union_tree_kernel<<<grid_threads(nc), RB, 0, s>>>(par.p, pre.p, nd.p, lo.p, hi.p, nc, uf.p, err.p);
+    uf_compress_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc);
+    tv_union_cross_kernel<<<grid_warps(nc), RB, 0, s>>>(crow.p, ccol.p, par.p, pre.p, nd.p, nc, uf.p, err.p);
     uf_flatten_kernel<<<grid_threads(nc), RB, 0, s>>>(uf.p, nc, blab.p, nullptr);
     ap_kernel<<<grid_warps(nc), RB, 0, s>>>(crow.p, ccol.p, par.p, blab.p, nc, ap.p, nkeys.p);
     GBC_TRY(cub_run([&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, nkeys.p, kpos.p, nc, s); }, s, "slot key offsets"));
