@@ -23,6 +23,10 @@ component / time.
   cpu_baseline : the oracle's FP64 Brandes with all host threads on a
           bounded sample of the same sources.
   clocks : SM clocks and throttle reasons sampled during the timed region.
+  reduction / deep_grid : the two other single-GPU configurations in short
+          form -- the D1+AP reduction on R-MAT s18 + 60K pendant trees
+          (device reduction, reduced vs unreduced closeness and betweenness)
+          and the 1024^2 grid (1024 sources, wide path counts).
 
 --impl reference times the CPU restatement of the reference's sequential
 Brandes (oracle/, the reference's own code is not buildable on the GPU host)
@@ -70,6 +74,8 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     p.add_argument("--serve-rates", default="5,10,20", help="query arrival rates per second, comma-separated")
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--no-reduction", action="store_true", help="skip the D1+AP reduction section (R-MAT s18 + pendant trees)")
+    p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 1024 sources)")
     return p.parse_args()
 
 
@@ -276,6 +282,52 @@ def serving(G, seconds, rates, seed=11):
             "directed_entries": int(sum(c.m for _, c in specs)), "workers": 4, "points": points,
             "mix": "uniform over graphs: 15% exact CC (graphs <= 32K vertices), 10% exact BC (<= 16K), "
                    "40% k=64 and 35% k=1024 sampled BC"}
+
+
+def reduction_section(G):
+    """The D1-folding + articulation-point configuration: R-MAT scale 18, edge
+    factor 4, with 60K pendant trees of depth 1-3 (382K vertex slots).  Device
+    reduction, then closeness and betweenness of every vertex through it
+    against the unreduced graph (wall times of the calls, device-resident)."""
+    csr = G.add_pendants(G.gen_rmat(18, 4, seed=18), 60000, 3, 2)
+    G.Reduced(G.add_pendants(G.gen_rmat(10, 4, seed=1), 100, 3, 2))   # first-call setup
+
+    def wall(f):
+        t = time.perf_counter()
+        r = f()
+        return r, (time.perf_counter() - t) * 1e3
+
+    R, t_red = wall(lambda: G.Reduced(csr))
+    info = R.info()
+    cc_r, t_ccr = wall(R.cc)
+    bc_r, t_bcr = wall(R.bc)
+    with G.Graph(csr) as g:
+        cc_p, t_ccp = wall(g.cc)
+        bc_p, t_bcp = wall(g.bc)
+    rel = float(np.max(np.abs(bc_r - bc_p) / np.maximum(np.abs(bc_p), 1.0)))
+    return {"graph": "rmat18_ef4+60k_pendant_trees", "n": int(csr.n), "m": int(csr.m // 2),
+            "reduce_ms": round(t_red, 2), "folded": info["d1_folded"], "fold_rounds": info["fold_rounds"],
+            "articulation_points": info["articulation_points"], "blocks": info["blocks"],
+            "cc_reduced_ms": round(t_ccr, 1), "cc_unreduced_ms": round(t_ccp, 1), "cc_bit_equal": bool(np.array_equal(cc_r, cc_p)),
+            "bc_reduced_ms": round(t_bcr, 1), "bc_unreduced_ms": round(t_bcp, 1), "bc_max_rel_diff": rel}
+
+
+def grid_section(G):
+    """The deep configuration: 1024 x 1024 grid with 5% of the edges removed
+    (seed 3), largest component, 1024 uniformly sampled sources (seed 3):
+    betweenness (FP32 delta; path counts pass 2^64, so wide form) and
+    closeness, GTEPS from the library's own CUDA-event timing."""
+    grid = G.gen_grid(1024, 1024, 0.05, seed=3, largest_only=True)
+    src = np.random.default_rng(3).choice(grid.n, 1024, replace=False).astype(np.int32)
+    with G.Graph(grid) as g:
+        g.bc(src, delta_precision=G.DELTA_F32)
+        st = g.stats()
+        g.cc(src)
+        st2 = g.stats()
+    return {"graph": "grid1024_minus5pct_largest", "n": int(grid.n), "m": int(grid.m // 2), "sources": 1024,
+            "bc_gteps": round(st["edges_traversed"] / st["kernel_ms"] / 1e6, 3), "bc_levels": int(st["levels"]),
+            "sigma_mode": "wide" if st["sigma_mode_used"] == G.SIGMA_WIDE else "exact", "lanes_per_group": int(st["group_lanes"]),
+            "cc_gteps": round(st2["edges_traversed"] / st2["kernel_ms"] / 1e6, 3)}
 
 
 def run_reference(args):
@@ -492,6 +544,8 @@ def main():
         serve = None
         if not args.no_serve:
             serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")])
+        red = None if args.no_reduction else reduction_section(G)
+        deep = None if args.no_grid else grid_section(G)
         out = {"metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",
@@ -505,7 +559,8 @@ def main():
                "plain": None if plain_gteps is None else {
                    "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),
                    "speedup_batched_vs_plain": round(gteps / plain_gteps, 2)},
-               "closeness": closeness, "precision": prec, "serving": serve, "clocks": clocks}
+               "closeness": closeness, "precision": prec, "serving": serve, "reduction": red, "deep_grid": deep,
+               "clocks": clocks}
         print(json.dumps(out), flush=True)
     if ws > 1:
         dist.barrier()
