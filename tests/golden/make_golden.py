@@ -8,9 +8,9 @@ sequential code from its sources into oracle/_ref.  It
     for karate (reference/karate_BC_Score.txt),
   * records, per dataset, the reference's own outputs: plain closeness sums
     (Seq_CC/CC.cpp:37 computeCC), the D1+AP closeness of the release path
-    (Seq_CC/CC.cpp:1728) with its structural counts, and -- for the smaller
-    graphs -- the reference's FP32 betweenness (Seq_Brandes/Brandes.c:224)
-    and its shared-traversal variant (Seq_Brandes/Brandes.c:374).
+    (Seq_CC/CC.cpp:1728) with its structural counts, the reference's FP32
+    betweenness (Seq_Brandes/Brandes.c:224), and -- for the smaller graphs --
+    its shared-traversal variant (Seq_Brandes/Brandes.c:374).
 The GPU machine has no reference tree; the tests read only these fixtures.
 """
 import gzip
@@ -45,8 +45,8 @@ def main():
         cc = O.ref_cc_file(src)
         d1ap, stats = O.ref_d1ap_cc_file(src)
         out = {"cc_ref": cc.astype(np.int64), "d1ap_cc_ref": d1ap.astype(np.int64)}
+        out["bc_ref_f32"] = O.ref_bc_file(src)
         if name in BC_SMALL:
-            out["bc_ref_f32"] = O.ref_bc_file(src)
             out["bc_shared_ref_f32"] = O.ref_bc_shared_file(src)
         np.savez_compressed(os.path.join(HERE, name.split(".")[0] + ".npz"), **out)
         meta[name] = stats
