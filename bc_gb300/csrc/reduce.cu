@@ -69,6 +69,14 @@ struct Reduction {
     std::vector<int32_t> ap_index;    // vertex -> index into ap_child_blocks (-1 if not AP)
     std::vector<int32_t> border;      // blocks in BFS order from the roots
     int32_t max_block = 0;
+    // device path: the folded graph and the block graph as the device built
+    // them; core / bg above then hold only n until an export asks for the rows
+    int64_t* d_core_row = nullptr;
+    int32_t* d_core_col = nullptr;
+    int64_t core_m = 0;
+    int64_t* d_bg_row = nullptr;
+    int32_t* d_bg_col = nullptr;
+    int64_t bg_m = 0;
     // where the reduction ran, and the device path's round and level counts
     bool on_device = false;
     int32_t fold_rounds = 0, forest_levels = 0;
@@ -91,9 +99,39 @@ struct Reduction {
         cudaFree(d_w);
         cudaFree(d_cw);
         cudaFree(d_cinv);
+        cudaFree(d_core_row);
+        cudaFree(d_core_col);
+        cudaFree(d_bg_row);
+        cudaFree(d_bg_col);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+// Directed entries of the two graphs, wherever their rows are.
+static int64_t core_entries(const Reduction& R) { return R.d_core_row ? R.core_m : R.core.m(); }
+static int64_t bg_entries(const Reduction& R) { return R.d_bg_row ? R.bg_m : R.bg.m(); }
+
+// Host rows of a graph that the device path left on the device (for exports).
+static gbc_status host_rows(HostCSR& h, const int64_t* d_row, const int32_t* d_col, int64_t m) {
+    if (!h.row.empty()) return GBC_OK;
+    if (!d_row) {   // an empty graph
+        h.row.assign((size_t)h.n + 1, 0);
+        return GBC_OK;
+    }
+    h.row.resize((size_t)h.n + 1);
+    h.col.resize((size_t)m);
+    GBC_CUDA(cudaMemcpy(h.row.data(), d_row, sizeof(int64_t) * ((size_t)h.n + 1), cudaMemcpyDeviceToHost));
+    if (m) GBC_CUDA(cudaMemcpy(h.col.data(), d_col, sizeof(int32_t) * m, cudaMemcpyDeviceToHost));
+    return GBC_OK;
+}
+
+// A device graph for the lane engine: a copy of the device-built rows, or an upload of the host rows.
+static gbc_status graph_rows(DevGraph& g, const HostCSR& h, const int64_t* d_row, const int32_t* d_col) {
+    const cudaMemcpyKind k = d_row ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    GBC_CUDA(cudaMemcpy(g.row, d_row ? (const void*)d_row : (const void*)h.row.data(), sizeof(int64_t) * (g.n + 1), k));
+    if (g.m) GBC_CUDA(cudaMemcpy(g.col, d_row ? (const void*)d_col : (const void*)h.col.data(), sizeof(int32_t) * g.m, k));
+    return GBC_OK;
+}
 
 // ---------------------------------------------------------------- fold ----
 static void fold(const int64_t* row, const int32_t* col, Reduction& R, std::vector<int32_t>& livecol,
@@ -357,13 +395,12 @@ static gbc_status upload(Reduction& R) {
     GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
     auto g = std::make_unique<DevGraph>();
     g->n = R.bg.n;
-    g->m = R.bg.m();
+    g->m = bg_entries(R);
     bool ok = cudaMalloc(&g->row, sizeof(int64_t) * (g->n + 1)) == cudaSuccess;
     ok &= cudaMalloc(&g->col, sizeof(int32_t) * std::max<int64_t>(g->m, 1)) == cudaSuccess;
     ok &= cudaMalloc(&R.d_w, sizeof(int32_t) * std::max<int32_t>(g->n, 1)) == cudaSuccess;
     if (!ok) { cudaGetLastError(); set_error("block graph allocation"); cudaFree(g->row); cudaFree(g->col); return GBC_ERR_NOMEM; }
-    GBC_CUDA(cudaMemcpy(g->row, R.bg.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
-    if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.bg.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
+    GBC_TRY(graph_rows(*g, R.bg, R.d_bg_row, R.d_bg_col));
     GBC_CUDA(cudaMemcpy(R.d_w, R.slot_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
     GBC_TRY(relabel_weighted(*g, R.stream, &R.d_w, R.b_inv));
     g->w = R.d_w;
@@ -519,13 +556,12 @@ static gbc_status core_upload(Reduction& R) {
     if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
     auto g = std::make_unique<DevGraph>();
     g->n = R.core.n;
-    g->m = R.core.m();
+    g->m = core_entries(R);
     bool ok = cudaMalloc(&g->row, sizeof(int64_t) * (g->n + 1)) == cudaSuccess;
     ok &= cudaMalloc(&g->col, sizeof(int32_t) * std::max<int64_t>(g->m, 1)) == cudaSuccess;
     ok &= cudaMalloc(&R.d_cw, sizeof(int32_t) * std::max<int32_t>(g->n, 1)) == cudaSuccess;
     if (!ok) { cudaGetLastError(); set_error("core graph allocation"); cudaFree(g->row); cudaFree(g->col); return GBC_ERR_NOMEM; }
-    GBC_CUDA(cudaMemcpy(g->row, R.core.row.data(), sizeof(int64_t) * (g->n + 1), cudaMemcpyHostToDevice));
-    if (g->m) GBC_CUDA(cudaMemcpy(g->col, R.core.col.data(), sizeof(int32_t) * g->m, cudaMemcpyHostToDevice));
+    GBC_TRY(graph_rows(*g, R.core, R.d_core_row, R.d_core_col));
     if (g->n) GBC_CUDA(cudaMemcpy(R.d_cw, R.core_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
     std::vector<int32_t> cinv;
     GBC_TRY(relabel_weighted(*g, R.stream, &R.d_cw, cinv));
@@ -664,6 +700,12 @@ static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduc
         if (R.start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
         GBC_TRY(fold_split_device(d_row, d_col, n, M, R.start, R.stream, F));
     }
+    R.d_core_row = F.d_core_row;
+    R.d_core_col = F.d_core_col;
+    R.core_m = F.core_m;
+    R.d_bg_row = F.d_bg_row;
+    R.d_bg_col = F.d_bg_col;
+    R.bg_m = F.bg_m;
     // folding: order by round, then vertex id; parents' reach before each absorption
     R.r = std::move(F.r);
     R.ff = std::move(F.ff);
@@ -771,7 +813,7 @@ gbc_status gbc_reduced_info_get(gbc_reduced h, gbc_reduced_info* info) {
     info->blocks = R.n_blocks;
     info->max_block = R.max_block;
     info->block_slots = R.bg.n;
-    info->block_edges = R.bg.m();
+    info->block_edges = bg_entries(R);
     info->components = R.n_comp;
     info->on_device = R.on_device;
     info->fold_rounds = R.fold_rounds;
@@ -813,7 +855,9 @@ gbc_status gbc_bc_reduced(gbc_reduced h, const gbc_options* opt, double* bc) {
 gbc_status gbc_reduced_core_graph(gbc_reduced h, int64_t** row, int32_t** col, int32_t** weight, int32_t** vertex,
                                   int32_t* n_core) {
     if (!h || !row || !col || !weight || !vertex || !n_core) { set_error("NULL argument"); return GBC_ERR_ARG; }
-    const Reduction& R = h->R;
+    Reduction& R = h->R;
+    std::lock_guard<std::mutex> lk(R.mu);
+    GBC_TRY(host_rows(R.core, R.d_core_row, R.d_core_col, R.core_m));
     GBC_TRY(export_csr(R.core, row, col));
     const size_t nc = std::max<size_t>(R.core.n, 1);
     *weight = (int32_t*)malloc(sizeof(int32_t) * nc);
@@ -838,7 +882,9 @@ gbc_status gbc_reduced_assemble_bc(gbc_reduced h, const double* core_bc, double*
 
 gbc_status gbc_reduced_block_graph(gbc_reduced h, int64_t** row, int32_t** col, int32_t** weight, int32_t* n_slots) {
     if (!h || !row || !col || !weight || !n_slots) { set_error("NULL argument"); return GBC_ERR_ARG; }
-    const Reduction& R = h->R;
+    Reduction& R = h->R;
+    std::lock_guard<std::mutex> lk(R.mu);
+    GBC_TRY(host_rows(R.bg, R.d_bg_row, R.d_bg_col, R.bg_m));
     GBC_TRY(export_csr(R.bg, row, col));
     *weight = (int32_t*)malloc(sizeof(int32_t) * std::max<int32_t>(R.bg.n, 1));
     if (!*weight) { free(*row); free(*col); set_error("host allocation"); return GBC_ERR_NOMEM; }

@@ -27,6 +27,14 @@ struct FoldSplit {
     std::vector<int32_t> core_vslot;  // core id -> its first slot
     HostCSR bg;                       // block graph over slots, rows ascending
     int32_t rounds = 0, levels = 0;   // peeling rounds, spanning-forest depth + 1
+    // the folded graph and the block graph stay on the device (cudaMalloc'd,
+    // owned by the receiver); core and bg above carry only their n
+    int64_t* d_core_row = nullptr;
+    int32_t* d_core_col = nullptr;
+    int64_t core_m = 0;
+    int64_t* d_bg_row = nullptr;
+    int32_t* d_bg_col = nullptr;
+    int64_t bg_m = 0;
 };
 
 // The per-entry checks of the reduction's input on the device copy: row

@@ -709,17 +709,20 @@ gbc_status fold_split_device(const int64_t* d_row, const int32_t* d_col, int32_t
     if (nc > (INT32_MAX >> 1)) { set_error("reduction: %d vertices left after folding, above 2^30", nc); return GBC_ERR_ARG; }
     out.core_v.resize(nc);
     out.core.n = nc;
-    out.core.row.resize((size_t)nc + 1);
-    out.core.col.resize((size_t)Mc);
+    out.core_m = Mc;
     if (nc > 0) GBC_CUDA(cudaMemcpyAsync(out.core_v.data(), core_v.p, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, s));
-    GBC_CUDA(cudaMemcpyAsync(out.core.row.data(), crow.p, sizeof(int64_t) * ((size_t)nc + 1), cudaMemcpyDeviceToHost, s));
-    if (Mc > 0) GBC_CUDA(cudaMemcpyAsync(out.core.col.data(), ccol.p, sizeof(int32_t) * Mc, cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaStreamSynchronize(s));
     // the folding buffers are no longer needed
     deg.alloc(0); fround.alloc(0); parent.alloc(0); cand.alloc(0); alive.alloc(0); r.alloc(0); ff.alloc(0);
     a32.alloc(0); cid.alloc(0); core_v.alloc(0); cdeg.alloc(0);
     out.bvoff.assign(1, 0);
-    if (nc == 0) return GBC_OK;
+    if (nc == 0) {
+        out.d_core_row = crow.p;
+        out.d_core_col = ccol.p;
+        crow.p = nullptr;
+        ccol.p = nullptr;
+        return GBC_OK;
+    }
 
     // ---- components and the BFS forest
     DBuf<int32_t> uf, lab, isroot, cpos, comp, level, par, nd, pre, lo, hi, order;
@@ -857,16 +860,22 @@ gbc_status fold_split_device(const int64_t* d_row, const int32_t* d_col, int32_t
     out.bvoff.resize((size_t)nb + 1);
     out.slot_core.resize(ns);
     out.bg.n = ns;
-    out.bg.row.resize((size_t)ns + 1);
-    out.bg.col.resize((size_t)Mc);
+    out.bg_m = Mc;
     GBC_CUDA(cudaMemcpyAsync(out.core_comp.data(), comp.p, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaMemcpyAsync(out.core_ap.data(), ap.p, nc, cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaMemcpyAsync(out.core_vslot.data(), vslot.p, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaMemcpyAsync(out.bvoff.data(), bvoff.p, sizeof(int64_t) * ((size_t)nb + 1), cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaMemcpyAsync(out.slot_core.data(), slot_core.p, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost, s));
-    GBC_CUDA(cudaMemcpyAsync(out.bg.row.data(), brow.p, sizeof(int64_t) * ((size_t)ns + 1), cudaMemcpyDeviceToHost, s));
-    if (Mc > 0) GBC_CUDA(cudaMemcpyAsync(out.bg.col.data(), bcol.p, sizeof(int32_t) * Mc, cudaMemcpyDeviceToHost, s));
     GBC_CUDA(cudaStreamSynchronize(s));
+    // the two graphs stay on the device, owned by the caller from here
+    out.d_core_row = crow.p;
+    out.d_core_col = ccol.p;
+    out.d_bg_row = brow.p;
+    out.d_bg_col = bcol.p;
+    crow.p = nullptr;
+    ccol.p = nullptr;
+    brow.p = nullptr;
+    bcol.p = nullptr;
     return GBC_OK;
 }
 
