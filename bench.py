@@ -517,7 +517,7 @@ def main():
             bc_p = torch.empty(csr.n, dtype=torch.float64).pin_memory()
             src_p = torch.empty(B, dtype=torch.int32).pin_memory()
             row_np, col_np, bc_np, src_np = row_p.numpy(), col_p.numpy(), bc_p.numpy(), src_p.numpy()
-            e2e_steps = max(1, min(args.steps, 2))
+            e2e_steps = max(1, min(args.steps, 4))
             t0 = time.perf_counter()
             e_edges = 0
             for i in range(e2e_steps):
