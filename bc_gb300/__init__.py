@@ -99,6 +99,7 @@ _PROTOS = [
     ("gbc_reduce", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
     ("gbc_set_device", _st, [C.c_int]),
     ("gbc_reduce_host", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    ("gbc_reduce_device", _st, [_vp, _vp, C.c_int32, C.c_int32, C.POINTER(_vp)]),
     ("gbc_reduced_info_get", _st, [_vp, C.POINTER(ReducedInfo)]),
     ("gbc_cc_reduced", _st, [_vp, C.POINTER(Options), _i64p]),
     ("gbc_bc_reduced", _st, [_vp, C.POINTER(Options), _f64p]),

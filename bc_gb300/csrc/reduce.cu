@@ -675,31 +675,49 @@ static gbc_status reduce_on_host(const int64_t* row, const int32_t* col, Reducti
 
 // The reduction on the device (reduce_dev.cu); the host keeps the O(#folded)
 // bookkeeping of the folding order and the O(#slots) block-cut tree.
-static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduction& R) {
+static gbc_status device_ready(Reduction& R) {
     int nd = 0;
     if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
+    if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
+    return GBC_OK;
+}
+
+static gbc_status reduce_device_csr(const int64_t* d_row, const int32_t* d_col, int64_t M, const int32_t* host_col,
+                                    Reduction& R);
+
+// Host CSR: upload, then the device reduction.
+static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduction& R) {
+    GBC_TRY(device_ready(R));
     const int32_t n = R.n;
     const int64_t M = row[n];
-    if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
-    FoldSplit F;
-    {
-        int64_t* d_row = nullptr;
-        int32_t* d_col = nullptr;
-        if (cudaMalloc(&d_row, sizeof(int64_t) * ((size_t)n + 1)) != cudaSuccess ||
-            cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(M, 1)) != cudaSuccess) {
-            cudaGetLastError();
-            cudaFree(d_row);
-            set_error("reduction: graph allocation");
-            return GBC_ERR_NOMEM;
-        }
-        std::unique_ptr<void, void (*)(void*)> f1(d_row, [](void* p) { cudaFree(p); });
-        std::unique_ptr<void, void (*)(void*)> f2(d_col, [](void* p) { cudaFree(p); });
-        GBC_CUDA(cudaMemcpyAsync(d_row, row, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, R.stream));
-        if (M) GBC_CUDA(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * M, cudaMemcpyHostToDevice, R.stream));
-        GBC_TRY(check_csr_device(d_row, d_col, n, M, col, R.stream));
-        if (R.start == 1 && row[1] != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
-        GBC_TRY(fold_split_device(d_row, d_col, n, M, R.start, R.stream, F));
+    int64_t* d_row = nullptr;
+    int32_t* d_col = nullptr;
+    if (cudaMalloc(&d_row, sizeof(int64_t) * ((size_t)n + 1)) != cudaSuccess ||
+        cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(M, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d_row);
+        set_error("reduction: graph allocation");
+        return GBC_ERR_NOMEM;
     }
+    std::unique_ptr<void, void (*)(void*)> f1(d_row, [](void* p) { cudaFree(p); });
+    std::unique_ptr<void, void (*)(void*)> f2(d_col, [](void* p) { cudaFree(p); });
+    GBC_CUDA(cudaMemcpyAsync(d_row, row, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, R.stream));
+    if (M) GBC_CUDA(cudaMemcpyAsync(d_col, col, sizeof(int32_t) * M, cudaMemcpyHostToDevice, R.stream));
+    return reduce_device_csr(d_row, d_col, M, col, R);
+}
+
+// The reduction of a device CSR, its entries checked on the device first.
+static gbc_status reduce_device_csr(const int64_t* d_row, const int32_t* d_col, int64_t M, const int32_t* host_col,
+                                    Reduction& R) {
+    const int32_t n = R.n;
+    GBC_TRY(check_csr_device(d_row, d_col, n, M, host_col, R.stream));
+    if (R.start == 1) {
+        int64_t r1 = 0;
+        GBC_CUDA(cudaMemcpy(&r1, d_row + 1, sizeof r1, cudaMemcpyDeviceToHost));
+        if (r1 != 0) { set_error("phantom slot 0 must have no edges"); return GBC_ERR_ARG; }
+    }
+    FoldSplit F;
+    GBC_TRY(fold_split_device(d_row, d_col, n, M, R.start, R.stream, F));
     R.d_core_row = F.d_core_row;
     R.d_core_col = F.d_core_col;
     R.core_m = F.core_m;
@@ -761,6 +779,14 @@ static gbc_status reduce_on_device(const int64_t* row, const int32_t* col, Reduc
     return block_tree(R);
 }
 
+// Components of folded vertices follow their root.
+static void folded_components(Reduction& R) {
+    for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
+        const int32_t d1 = R.fold_order[i];
+        R.comp[d1] = R.comp[R.parent[d1]];
+    }
+}
+
 static gbc_status reduce_entry(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out,
                                bool on_device) {
     if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
@@ -780,11 +806,7 @@ static gbc_status reduce_entry(const int64_t* row, const int32_t* col, int32_t n
     R.start = start;
     R.on_device = on_device;
     GBC_TRY(on_device ? reduce_on_device(row, col, R) : reduce_on_host(row, col, R));
-    // components of folded vertices follow their root
-    for (int64_t i = (int64_t)R.fold_order.size() - 1; i >= 0; i--) {
-        const int32_t d1 = R.fold_order[i];
-        R.comp[d1] = R.comp[R.parent[d1]];
-    }
+    folded_components(R);
     *out = H.release();
     return GBC_OK;
 }
@@ -797,6 +819,30 @@ gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t
 
 gbc_status gbc_reduce_host(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out) {
     return reduce_entry(row, col, n, start, out, false);
+}
+
+gbc_status gbc_reduce_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int32_t start, gbc_reduced* out) {
+    if (!out) { set_error("out is NULL"); return GBC_ERR_ARG; }
+    *out = nullptr;
+    if (n <= 0 || !d_row) { set_error("invalid CSR arguments (n=%d)", n); return GBC_ERR_ARG; }
+    if (start < 0 || start > 1 || start >= n) { set_error("start must be 0 or 1"); return GBC_ERR_ARG; }
+    auto H = std::make_unique<gbc_reduced_s>();
+    Reduction& R = H->R;
+    R.n = n;
+    R.start = start;
+    R.on_device = true;
+    GBC_TRY(device_ready(R));
+    // the header checks of the host path, on the two offsets they need
+    int64_t ends[2] = {0, 0};
+    GBC_CUDA(cudaMemcpy(&ends[0], d_row, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    GBC_CUDA(cudaMemcpy(&ends[1], d_row + n, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (ends[0] != 0) { set_error("row[0] must be 0"); return GBC_ERR_ARG; }
+    if (ends[1] < 0 || ends[1] >= ((int64_t)1 << 31)) { set_error("row[n]=%lld out of range", (long long)ends[1]); return GBC_ERR_ARG; }
+    if (ends[1] > 0 && !d_col) { set_error("invalid CSR arguments (n=%d)", n); return GBC_ERR_ARG; }
+    GBC_TRY(reduce_device_csr(d_row, d_col, ends[1], nullptr, R));
+    folded_components(R);
+    *out = H.release();
+    return GBC_OK;
 }
 
 gbc_status gbc_reduced_info_get(gbc_reduced h, gbc_reduced_info* info) {

@@ -225,6 +225,10 @@ typedef struct {
  * folded vertices, articulation points, blocks and results. */
 gbc_status gbc_reduce(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out);
 gbc_status gbc_reduce_host(const int64_t* row, const int32_t* col, int32_t n, int32_t start, gbc_reduced* out);
+/* gbc_reduce on a CSR already in device memory (d_row[n+1], d_col[d_row[n]]
+ * on the current device, complete before the call, not modified); its
+ * entries are checked on the device as gbc_reduce checks them. */
+gbc_status gbc_reduce_device(const int64_t* d_row, const int32_t* d_col, int32_t n, int32_t start, gbc_reduced* out);
 gbc_status gbc_reduced_info_get(gbc_reduced r, gbc_reduced_info* info);
 /* Closeness of every vertex slot through the reduction: cc[n] (host).
  * Equal to gbc_cc over all vertices of the unreduced graph. */

@@ -428,3 +428,33 @@ def test_dropin_driver_on_karate(gpu, datasets, tmp_path):
     assert np.array_equal(np.loadtxt(prefix + "_d1ap.txt", dtype=np.int64), fx["d1ap_cc_ref"][1:])
     st = STRUCT["karate.txt"]
     assert r.stdout.split()[:6] == ["folded", str(st["d1"]), "hubs", str(st["hub"]), "aps", str(st["ap"])]
+
+
+def test_reduce_from_device_arrays(gpu, datasets):
+    """gbc_reduce_device on a CSR already on the device equals gbc_reduce on
+    the same CSR from host memory, and rejects a bad CSR with the same message."""
+    torch = pytest.importorskip("torch")
+    L = gpu.lib()
+    cases = [gpu.add_pendants(gpu.gen_rmat(14, 4, seed=5), 3000, 3, 9), gpu.read_edgelist(datasets["karate.txt"]),
+             _chain_of_blocks(gpu)]
+    for csr in cases:
+        d_row = torch.from_numpy(csr.row).cuda()
+        d_col = torch.from_numpy(csr.col).cuda()
+        torch.cuda.synchronize()
+        h = C.c_void_p()
+        gpu.check(L.gbc_reduce_device(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), csr.n, csr.start,
+                                      C.byref(h)))
+        info = gpu.ReducedInfo()
+        gpu.check(L.gbc_reduced_info_get(h, C.byref(info)))
+        cc = np.zeros(csr.n, np.int64)
+        gpu.check(L.gbc_cc_reduced(h, C.byref(gpu.options()), cc))
+        gpu.check(L.gbc_reduced_destroy(h))
+        R = gpu.Reduced(csr)
+        assert info.as_dict() == R.info()
+        assert np.array_equal(cc, R.cc())
+    row = torch.tensor([0, 1, 2], dtype=torch.int64, device="cuda")
+    col = torch.tensor([0, 1], dtype=torch.int32, device="cuda")   # self-loop at 0
+    torch.cuda.synchronize()
+    h = C.c_void_p()
+    assert L.gbc_reduce_device(C.c_void_p(row.data_ptr()), C.c_void_p(col.data_ptr()), 2, 0, C.byref(h)) == 1
+    assert b"self-loop at vertex 0" in L.gbc_last_error()
