@@ -24,10 +24,17 @@
 // address) and keeps it for later calls; make that first call on a device
 // before any stream capture.
 //
+// Before any BFS indexes the array with the caller's CSR, a check kernel
+// reads the whole CSR on the device: row[0] == 0, rows non-decreasing, every
+// col entry in [0, n). It records the first offending row and the first
+// offending entry in two 64-bit status words of the array's header, and a
+// bad CSR is refused with GBC_ERR_ARG before anything is written past the
+// header.
+//
 // The kernels are launched on the caller's stream. The host reads each new
-// frontier size back with a 64-bit copy into a local variable, and writes
-// each source's sum with a 64-bit copy from a local variable. Nothing is
-// allocated on either side.
+// frontier size and the two status words back with copies into local
+// variables, and writes each source's sum with a 64-bit copy from a local
+// variable. Nothing is allocated on either side.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -40,7 +47,8 @@ constexpr int32_t NOALLOC_MAX_N = 1 << 21;   // GBC_NOALLOC_MAX_VERTICES
 constexpr int32_t HDR = 64;                  // int32 slots before the distance array (counters)
 constexpr unsigned FULL = 0xFFFFFFFFu;
 
-// [0,64): counters (tail at slot 0 as 64 bits), then dist[MAX_N], queue[MAX_N]
+// [0,64): counters (queue tail at slots 0-1, first bad row at 2-3, first bad
+// col entry at 4-5, each 64 bits), then dist[MAX_N], queue[MAX_N]
 static __device__ __align__(256) int32_t g_noalloc_scratch[HDR + 2 * NOALLOC_MAX_N];
 
 // Device address of g_noalloc_scratch, looked up once per device.
@@ -68,6 +76,22 @@ gbc_status scratch_for_current_device(int32_t** out) {
     }
     *out = g_scratch_ptr[dev];
     return GBC_OK;
+}
+
+// CSR entry check: the smallest v with row[v] > row[v+1] and the smallest j
+// with col[j] outside [0, n), into the status words (all ones: none).  The
+// host has checked row[0] == 0 and 0 <= row[n] < 2^31 already.
+__global__ void na_check(const int64_t* __restrict__ row, const int32_t* __restrict__ col, int32_t n, long long m,
+                         int32_t* scratch) {
+    unsigned long long* bad = reinterpret_cast<unsigned long long*>(scratch) + 1;
+    const long long span = m > (long long)n ? m : (long long)n;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < span; i += (long long)gridDim.x * blockDim.x) {
+        if (i < n && row[i] > row[i + 1]) atomicMin(&bad[0], (unsigned long long)i);
+        if (i < m) {
+            const int32_t x = col[i];
+            if (x < 0 || x >= n) atomicMin(&bad[1], (unsigned long long)i);
+        }
+    }
 }
 
 // dist[0..n) = -1 (every call starts from a cleared distance array).
@@ -137,6 +161,33 @@ extern "C" gbc_status gbc_cc_noalloc(const int64_t* d_row, const int32_t* d_col,
     GBC_CUDA(cudaGetDevice(&dev));
     GBC_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
     unsigned long long* d_tail = reinterpret_cast<unsigned long long*>(scratch);
+    // the CSR's two end offsets, then every row and entry on the device
+    int64_t ends[2] = {-1, -1};
+    GBC_CUDA(cudaMemcpyAsync(&ends[0], d_row, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaMemcpyAsync(&ends[1], d_row + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    if (ends[0] != 0) {
+        set_error("gbc_cc_noalloc: row[0] must be 0 (got %lld)", (long long)ends[0]);
+        return GBC_ERR_ARG;
+    }
+    if (ends[1] < 0 || ends[1] >= ((int64_t)1 << 31)) {
+        set_error("gbc_cc_noalloc: row[n]=%lld out of range", (long long)ends[1]);
+        return GBC_ERR_ARG;
+    }
+    unsigned long long bad[2] = {0, 0};
+    GBC_CUDA(cudaMemsetAsync(d_tail + 1, 0xFF, sizeof(bad), s));
+    na_check<<<sm * 4, 256, 0, s>>>(d_row, d_col, n, (long long)ends[1], scratch);
+    GBC_CUDA(cudaGetLastError());
+    GBC_CUDA(cudaMemcpyAsync(bad, d_tail + 1, sizeof(bad), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    if (bad[0] != ~0ULL) {
+        set_error("gbc_cc_noalloc: row offsets decrease at vertex %llu", bad[0]);
+        return GBC_ERR_ARG;
+    }
+    if (bad[1] != ~0ULL) {
+        set_error("gbc_cc_noalloc: col[%llu] is outside [0,%d)", bad[1], n);
+        return GBC_ERR_ARG;
+    }
     for (int32_t i = 0; i < k; i++) {
         int32_t src = -1;
         GBC_CUDA(cudaMemcpyAsync(&src, d_sources + i, sizeof(int32_t), cudaMemcpyDeviceToHost, s));

@@ -45,3 +45,40 @@ def test_cc_noalloc_equals_gbc_cc_on_consecutive_calls(gpu):
     st = fn(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), MAX_VERTICES + 1,
             C.c_void_p(d_src.data_ptr()), 1, C.c_void_p(d_out.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert st == 1 and b"scratch" in gpu.lib().gbc_last_error()
+
+
+def test_cc_noalloc_refuses_a_bad_csr(gpu):
+    """A CSR the caller got wrong (an entry equal to n, or a row offset that
+    decreases) is refused with GBC_ERR_ARG by the device check that runs
+    before the BFS writes anything; a good call right after still equals
+    gbc_cc."""
+    torch = pytest.importorskip("torch")
+    fn = _noalloc(gpu)
+    csr = gpu.gen_er(3000, 4.0, seed=5)
+    stream = torch.cuda.current_stream()
+    src = np.arange(0, csr.n, 97, dtype=np.int32)
+    d_src = torch.from_numpy(src).cuda()
+    d_out = torch.full((len(src),), -1, dtype=torch.int64, device="cuda")
+
+    def call(row, col):
+        d_row = torch.from_numpy(row).cuda()
+        d_col = torch.from_numpy(col).cuda()
+        st = fn(C.c_void_p(d_row.data_ptr()), C.c_void_p(d_col.data_ptr()), csr.n, C.c_void_p(d_src.data_ptr()),
+                len(src), C.c_void_p(d_out.data_ptr()), C.c_void_p(stream.cuda_stream))
+        torch.cuda.synchronize()
+        return st, gpu.lib().gbc_last_error()
+
+    col = csr.col.copy()
+    col[len(col) // 2] = csr.n                     # one entry past the last vertex
+    st, msg = call(csr.row, col)
+    assert st == 1 and b"outside" in msg, msg
+    row = csr.row.copy()
+    v = int(np.argmax(np.diff(row) > 0)) + 1        # a vertex after one with neighbours
+    row[v] = row[v + 1] + 1                         # row[v] > row[v+1]
+    st, msg = call(row, csr.col)
+    assert st == 1 and b"decrease" in msg, msg
+    st, msg = call(csr.row, csr.col)
+    assert st == 0, msg
+    with gpu.Graph(csr) as G:
+        ref = G.cc(src)
+    assert np.array_equal(d_out.cpu().numpy(), ref)
