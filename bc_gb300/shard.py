@@ -39,12 +39,13 @@ def gather_cc(cc_partial: np.ndarray, group=None) -> np.ndarray:
     import torch
     import torch.distributed as dist
     world = dist.get_world_size(group)
-    n = torch.tensor([len(cc_partial)], dtype=torch.int64)
-    sizes = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"   # NCCL gathers device tensors only
+    n = torch.tensor([len(cc_partial)], dtype=torch.int64, device=dev)
+    sizes = [torch.zeros(1, dtype=torch.int64, device=dev) for _ in range(world)]
     dist.all_gather(sizes, n, group=group)
     mx = int(max(x.item() for x in sizes))
-    buf = torch.zeros(mx, dtype=torch.int64)
-    buf[:len(cc_partial)] = torch.from_numpy(np.ascontiguousarray(cc_partial, dtype=np.int64))
-    out = [torch.zeros(mx, dtype=torch.int64) for _ in range(world)]
+    buf = torch.zeros(mx, dtype=torch.int64, device=dev)
+    buf[:len(cc_partial)] = torch.from_numpy(np.ascontiguousarray(cc_partial, dtype=np.int64)).to(dev)
+    out = [torch.zeros(mx, dtype=torch.int64, device=dev) for _ in range(world)]
     dist.all_gather(out, buf, group=group)
-    return np.concatenate([o[:int(s.item())].numpy() for o, s in zip(out, sizes)])
+    return np.concatenate([o[:int(s.item())].cpu().numpy() for o, s in zip(out, sizes)])

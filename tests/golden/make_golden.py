@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures under tests/golden/ from the reference tree.
 
-Run here, where the reference is mounted (path given as argv[1], default
-/root/reference), after `make -C oracle ref` built the reference's own
+Run where the reference is mounted (its path as argv[1], or in the
+environment variable GBC_REFERENCE_TREE), after `make -C oracle ref` built the reference's own
 sequential code from its sources into oracle/_ref.  It
   * copies the shipped edge-list datasets used by the tests (gzip'd; these
     are public graph datasets, not code) and the reference's golden BC file
@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from oracle import oracle as O  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GBC_REFERENCE_TREE", "")
 DATASETS = ["karate.txt", "dolphins.txt", "football.txt", "polbooks.txt", "testdata.txt", "testdata1.txt",
             "testdata2.txt", "ia-fb-messages.mtx", "tech-WHOIS.mtx", "caida.mtx", "ia-email-EU.mtx", "ca-HepPh.mtx"]
 BC_SMALL = {"karate.txt", "dolphins.txt", "football.txt", "polbooks.txt", "testdata.txt", "testdata1.txt",
@@ -33,7 +33,9 @@ BC_SMALL = {"karate.txt", "dolphins.txt", "football.txt", "polbooks.txt", "testd
 
 
 def main():
-    O.build(ref=True)
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py <reference tree> (or set GBC_REFERENCE_TREE)")
+    O.build(ref=True, tree=REF)
     os.makedirs(os.path.join(HERE, "datasets"), exist_ok=True)
     meta = {}
     for name in DATASETS:
