@@ -652,3 +652,180 @@ int32_t orc_ap_cc(int32_t N, const int64_t* row, const int32_t* col, int32_t sta
     free(is_ap); free(part); free(dist); free(q);
     return c;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Seeded R-MAT generator, so the bench's CPU legs build their graph without
+ * the product library.  It restates gbc_gen_rmat of libgbc bit for bit: a
+ * splitmix64-seeded xoshiro256** stream per block of 65,536 edges (stream
+ * 1000 + block), one uniform per level choosing a quadrant (a, b, c, rest),
+ * a Fisher-Yates relabelling (stream 7, Lemire's bounded draw), then the
+ * symmetric CSR without self-loops or repeated edges, rows ascending.
+ * tests/test_oracle.py checks the two generators give identical arrays.     */
+typedef struct { uint64_t s[4]; } orc_rng;
+
+static uint64_t orc_splitmix(uint64_t* x) {
+    uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static void orc_rng_init(orc_rng* r, uint64_t seed, uint64_t stream) {
+    uint64_t x = seed ^ (stream * 0xD1B54A32D192ED03ull + 0x8CB92BA72F3D8DD7ull);
+    for (int i = 0; i < 4; i++) r->s[i] = orc_splitmix(&x);
+}
+static inline uint64_t orc_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+static uint64_t orc_next(orc_rng* r) {
+    uint64_t* s = r->s;
+    const uint64_t out = orc_rotl(s[1] * 5, 7) * 9;
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = orc_rotl(s[3], 45);
+    return out;
+}
+static double orc_uniform(orc_rng* r) { return (double)(orc_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+static uint64_t orc_below(orc_rng* r, uint64_t bound) {
+    if (bound == 0) return 0;
+    unsigned __int128 m = (unsigned __int128)orc_next(r) * bound;
+    uint64_t l = (uint64_t)m;
+    if (l < bound) {
+        const uint64_t t = (0 - bound) % bound;
+        while (l < t) { m = (unsigned __int128)orc_next(r) * bound; l = (uint64_t)m; }
+    }
+    return (uint64_t)(m >> 64);
+}
+
+typedef struct {
+    int32_t scale, nthreads, tid;
+    double a, b, c;
+    uint64_t seed;
+    int64_t E;
+    int32_t *eu, *ev;
+    const int32_t* perm;
+    int64_t* row;
+    int32_t* col;
+    int64_t* fill;
+    int64_t* newdeg;
+    int32_t n;
+    int phase;
+} rmat_job;
+
+static int cmp_i32(const void* x, const void* y) {
+    const int32_t a = *(const int32_t*)x, b = *(const int32_t*)y;
+    return (a > b) - (a < b);
+}
+
+static void* rmat_worker(void* arg) {
+    rmat_job* J = (rmat_job*)arg;
+    const int64_t chunk = 1 << 16;
+    if (J->phase == 0) {   /* edges, block ci on thread ci % nthreads */
+        const int64_t nchunks = (J->E + chunk - 1) / chunk;
+        for (int64_t ci = J->tid; ci < nchunks; ci += J->nthreads) {
+            orc_rng r;
+            orc_rng_init(&r, J->seed, 1000 + (uint64_t)ci);
+            const int64_t hi = J->E < (ci + 1) * chunk ? J->E : (ci + 1) * chunk;
+            for (int64_t i = ci * chunk; i < hi; i++) {
+                uint32_t x = 0, y = 0;
+                for (int32_t l = 0; l < J->scale; l++) {
+                    const double p = orc_uniform(&r);
+                    uint32_t bx = 0, by = 0;
+                    if (p < J->a) {
+                    } else if (p < J->a + J->b) {
+                        by = 1;
+                    } else if (p < J->a + J->b + J->c) {
+                        bx = 1;
+                    } else {
+                        bx = 1;
+                        by = 1;
+                    }
+                    x = (x << 1) | bx;
+                    y = (y << 1) | by;
+                }
+                J->eu[i] = J->perm ? J->perm[x] : (int32_t)x;
+                J->ev[i] = J->perm ? J->perm[y] : (int32_t)y;
+            }
+        }
+    } else {   /* sort + unique the rows of vertices tid, tid + nthreads, ... */
+        for (int32_t x = J->tid; x < J->n; x += J->nthreads) {
+            int32_t* p = J->col + J->row[x];
+            const int64_t len = J->row[x + 1] - J->row[x];
+            qsort(p, (size_t)len, sizeof(int32_t), cmp_i32);
+            int64_t k = 0;
+            for (int64_t i = 0; i < len; i++)
+                if (k == 0 || p[i] != p[k - 1]) p[k++] = p[i];
+            J->newdeg[x] = k;
+        }
+    }
+    return NULL;
+}
+
+int orc_gen_rmat(int32_t scale, int32_t ef, double a, double b, double c, uint64_t seed, int permute, int nthreads,
+                 int32_t* n_out, int64_t** row_out, int32_t** col_out) {
+    if (scale < 1 || scale > 30 || ef < 1 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    const int32_t n = (int32_t)1 << scale;
+    const int64_t E = (int64_t)ef * n;
+    int32_t* eu = (int32_t*)malloc(sizeof(int32_t) * (size_t)E);
+    int32_t* ev = (int32_t*)malloc(sizeof(int32_t) * (size_t)E);
+    int32_t* perm = NULL;
+    if (!eu || !ev) { free(eu); free(ev); return -2; }
+    if (permute) {
+        perm = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+        if (!perm) { free(eu); free(ev); return -2; }
+        for (int32_t i = 0; i < n; i++) perm[i] = i;
+        orc_rng pr;
+        orc_rng_init(&pr, seed, 7);
+        for (int32_t i = n - 1; i > 0; i--) {
+            const int32_t j = (int32_t)orc_below(&pr, (uint64_t)i + 1);
+            const int32_t t = perm[i];
+            perm[i] = perm[j];
+            perm[j] = t;
+        }
+    }
+    rmat_job* jobs = (rmat_job*)calloc((size_t)nthreads, sizeof(rmat_job));
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int t = 0; t < nthreads; t++) {
+        rmat_job J = {scale, nthreads, t, a, b, c, seed, E, eu, ev, perm, NULL, NULL, NULL, NULL, n, 0};
+        jobs[t] = J;
+        pthread_create(&th[t], NULL, rmat_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(perm);
+    /* both directions of every non-loop edge, then sorted unique rows */
+    int64_t* row = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < E; i++)
+        if (eu[i] != ev[i]) { row[eu[i] + 1]++; row[ev[i] + 1]++; }
+    for (int32_t i = 0; i < n; i++) row[i + 1] += row[i];
+    int32_t* col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(row[n] ? row[n] : 1));
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    memcpy(fill, row, sizeof(int64_t) * (size_t)n);
+    for (int64_t i = 0; i < E; i++)
+        if (eu[i] != ev[i]) { col[fill[eu[i]]++] = ev[i]; col[fill[ev[i]]++] = eu[i]; }
+    free(fill);
+    free(eu);
+    free(ev);
+    int64_t* newdeg = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    for (int t = 0; t < nthreads; t++) {
+        jobs[t].phase = 1;
+        jobs[t].row = row;
+        jobs[t].col = col;
+        jobs[t].newdeg = newdeg;
+        pthread_create(&th[t], NULL, rmat_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(jobs);
+    free(th);
+    int64_t* orow = (int64_t*)malloc(sizeof(int64_t) * ((size_t)n + 1));
+    orow[0] = 0;
+    for (int32_t i = 0; i < n; i++) orow[i + 1] = orow[i] + newdeg[i];
+    int32_t* ocol = (int32_t*)malloc(sizeof(int32_t) * (size_t)(orow[n] ? orow[n] : 1));
+    for (int32_t i = 0; i < n; i++) memcpy(ocol + orow[i], col + row[i], sizeof(int32_t) * (size_t)newdeg[i]);
+    free(newdeg);
+    free(row);
+    free(col);
+    *n_out = n;
+    *row_out = orow;
+    *col_out = ocol;
+    return 0;
+}

@@ -102,6 +102,14 @@ int32_t orc_ap_cc(int32_t N, const int64_t* row, const int32_t* col,
 int32_t orc_components(int32_t N, const int64_t* row, const int32_t* col,
                        int32_t* comp, int32_t* size_out);
 
+/* Seeded R-MAT graph (scale, edge factor, quadrant probabilities a, b, c),
+ * symmetrised, without self-loops or repeated edges, rows ascending; with
+ * permute, vertex ids are relabelled by a seeded shuffle.  Gives the same
+ * arrays as libgbc's gbc_gen_rmat for the same arguments.  *row_out /
+ * *col_out are malloc'd (orc_free). */
+int orc_gen_rmat(int32_t scale, int32_t ef, double a, double b, double c, uint64_t seed, int permute, int nthreads,
+                 int32_t* n_out, int64_t** row_out, int32_t** col_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,11 +26,15 @@ _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 
 
-def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and, with ref=True, the reference's code)."""
+def build(ref: bool = False, tree: str = "") -> None:
+    """Compile liboracle.so (and, with ref=True, the reference's code from
+    the tree at `tree`, or GBC_REFERENCE_TREE when `tree` is empty)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        tree = tree or os.environ.get("GBC_REFERENCE_TREE", "")
+        if not tree:
+            raise RuntimeError("the reference tree is needed: pass tree= or set GBC_REFERENCE_TREE")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + tree], check=True)
 
 
 def lib():
@@ -59,6 +63,8 @@ def lib():
         L.orc_ap_cc.restype = C.c_int32
         L.orc_components.argtypes = [C.c_int32, _i64p, _i32p, _i32p, C.c_void_p]
         L.orc_components.restype = C.c_int32
+        L.orc_gen_rmat.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64, C.c_int,
+                                   C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
         _LIB = L
     return _LIB
 
@@ -92,6 +98,24 @@ def load_edgelist(path: str) -> Graph:
     L.orc_free(rp)
     L.orc_free(cp)
     return Graph(row, col, st.value)
+
+
+def gen_rmat(scale: int, edge_factor: int, a=0.57, b=0.19, c=0.19, seed=1, permute=True, nthreads=0) -> Graph:
+    """Seeded R-MAT graph, the same arrays as the product's generator
+    (bc_gb300.gen_rmat) for the same arguments, built without it."""
+    L = lib()
+    n = C.c_int32()
+    rp, cp = C.c_void_p(), C.c_void_p()
+    rc = L.orc_gen_rmat(scale, edge_factor, a, b, c, seed, int(bool(permute)), nthreads or (os.cpu_count() or 1),
+                        C.byref(n), C.byref(rp), C.byref(cp))
+    if rc != 0:
+        raise ValueError(f"orc_gen_rmat failed: {rc}")
+    row = np.ctypeslib.as_array(C.cast(rp, C.POINTER(C.c_int64)), shape=(n.value + 1,)).copy()
+    m = int(row[-1])
+    col = np.ctypeslib.as_array(C.cast(cp, C.POINTER(C.c_int32)), shape=(max(m, 1),))[:m].copy()
+    L.orc_free(rp)
+    L.orc_free(cp)
+    return Graph(row, col)
 
 
 def sssp(g: Graph, s: int):

@@ -169,3 +169,16 @@ def test_threaded_oracle_matches_serial(orc, datasets):
     b, _ = orc.bc(g, src, nthreads=6)
     assert np.allclose(a, b, rtol=1e-12, atol=1e-12)
     assert np.array_equal(orc.cc(g, src, nthreads=1), orc.cc(g, src, nthreads=5))
+
+
+@pytest.mark.parametrize("scale,ef,permute", [(12, 8, False), (16, 16, True)])
+def test_oracle_rmat_generator_equals_product(gbc, orc, scale, ef, permute):
+    """bench.py's CPU legs build the R-MAT workload with the oracle's
+    restatement of the generator, so that the reference arm never loads the
+    product library; both generators must give the same arrays and the same
+    sampled sources."""
+    import bench
+    a = orc.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed=1, permute=permute)
+    b = gbc.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed=1, permute=permute)
+    assert np.array_equal(a.row, b.row) and np.array_equal(a.col, b.col)
+    assert np.array_equal(bench.sample_sources(a.row, 1024), bench.sample_sources(b.row, 1024))
