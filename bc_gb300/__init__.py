@@ -86,6 +86,7 @@ _PROTOS = [
     ("gbc_graph_create", _st, [_i64p, _i32p, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_create_device", _st, [_vp, _vp, C.c_int32, C.c_int64, C.POINTER(_vp)]),
     ("gbc_graph_destroy", _st, [_vp]),
+    ("gbc_graph_set_weights", _st, [_vp, _vp, _vp]),
     ("gbc_graph_from_edges", _st, [_i32p, _i32p, C.c_int64, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_from_edges_device", _st, [_vp, _vp, C.c_int64, C.c_int32, C.POINTER(_vp)]),
     ("gbc_graph_export", _st, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
@@ -117,6 +118,8 @@ _PROTOS = [
     ("gbc_gen_er", _st, [C.c_int32, C.c_double, C.c_uint64, C.POINTER(_vp), C.POINTER(_vp)]),
     ("gbc_add_pendants", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_vp),
                                C.POINTER(_vp), C.POINTER(C.c_int32)]),
+    ("gbc_add_cycles", _st, [_i64p, _i32p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                             C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32)]),
     ("gbc_read_edgelist", _st, [C.c_char_p, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32)]),
     ("gbc_write_scores", _st, [C.c_char_p, _f64p, C.c_int32, C.c_int32, C.c_int32]),
@@ -238,6 +241,14 @@ def add_pendants(g: CSR, trees: int, max_depth: int, seed: int) -> CSR:
     return _take_csr(rp, cp, n.value)
 
 
+def add_cycles(g: CSR, cycles: int, min_len: int, max_len: int, seed: int) -> CSR:
+    """Attach cycles of min_len..max_len vertices through uniformly chosen vertices."""
+    rp, cp, n = _vp(), _vp(), C.c_int32()
+    check(lib().gbc_add_cycles(g.row, g.col, g.n, cycles, min_len, max_len, seed, C.byref(rp), C.byref(cp),
+                               C.byref(n)))
+    return _take_csr(rp, cp, n.value)
+
+
 def read_edgelist(path: str) -> CSR:
     rp, cp, n, st = _vp(), _vp(), C.c_int32(), C.c_int32()
     check(lib().gbc_read_edgelist(path.encode(), C.byref(rp), C.byref(cp), C.byref(n), C.byref(st)))
@@ -268,6 +279,17 @@ class Graph:
         g.n = int(n)
         g.csr = g.export()
         return g
+
+    def set_weights(self, w=None, ff=None):
+        """Vertex weights (gbc_graph_set_weights): closeness then sums
+        ff[v] + d*w[v], betweenness weighs pairs by w[s]*w[t]; None clears."""
+        self._w = None if w is None else np.ascontiguousarray(w, dtype=np.int32)
+        self._ff = None if ff is None else np.ascontiguousarray(ff, dtype=np.int64)
+        for a in (self._w, self._ff):
+            if a is not None and len(a) != self.n:
+                raise ValueError("weights must have one entry per vertex")
+        check(lib().gbc_graph_set_weights(self.h, None if self._w is None else self._w.ctypes.data_as(_vp),
+                                          None if self._ff is None else self._ff.ctypes.data_as(_vp)))
 
     def export(self) -> CSR:
         """The device CSR, copied to the host."""

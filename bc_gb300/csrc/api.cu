@@ -35,6 +35,9 @@ struct gbc_graph_s {
     int32_t* d_inv = nullptr;
     std::vector<int32_t> h_inv;
     double* d_bc_out = nullptr;   // BC in the caller's ids (gbc_bc)
+    // vertex weights set by gbc_graph_set_weights, in internal ids (nullable)
+    int32_t* d_w = nullptr;
+    int64_t* d_ff = nullptr;
     // settings chosen by gbc_autotune; used where the options ask for autotuning
     struct {
         bool done = false;
@@ -55,6 +58,8 @@ struct gbc_graph_s {
         dev_release(d_order, sizeof(int32_t) * (size_t)g.n);
         dev_release(d_inv, sizeof(int32_t) * (size_t)g.n);
         cudaFree(d_bc_out);
+        cudaFree(d_w);
+        cudaFree(d_ff);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -195,6 +200,19 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (o.group_lanes != 0 && o.group_lanes != 32 && o.group_lanes != 128) { set_error("group_lanes must be 0, 32 or 128"); return GBC_ERR_ARG; }
     if (o.group_lanes == 128 && o.lanes % 128) { set_error("group_lanes 128 needs lanes = 0 or a multiple of 128"); return GBC_ERR_ARG; }
     if (o.direction != 0 && o.direction != 1) { set_error("direction must be 0 or 1"); return GBC_ERR_ARG; }
+    return GBC_OK;
+}
+
+// Calls on a graph with vertex weights: the lane engine only (the plain
+// engine has none), and for betweenness the Brandes semantics only (the
+// reference's per-predecessor count does not combine with pair weights).
+static gbc_status check_weighted(const gbc_graph_s* G, const gbc_options& o, bool bc) {
+    if (!G->g.w && !G->g.ff) return GBC_OK;
+    if (o.engine == GBC_ENGINE_PLAIN) { set_error("the plain engine has no vertex weights (gbc_graph_set_weights)"); return GBC_ERR_ARG; }
+    if (bc && o.semantics != GBC_BC_BRANDES) {
+        set_error("betweenness with vertex weights supports GBC_BC_BRANDES only");
+        return GBC_ERR_ARG;
+    }
     return GBC_OK;
 }
 
@@ -622,6 +640,58 @@ gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, i
     return GBC_OK;
 }
 
+gbc_status gbc_graph_set_weights(gbc_graph G, const int32_t* w, const int64_t* ff) {
+    if (!G) { set_error("graph is NULL"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const int32_t n = G->g.n;
+    if (w)
+        for (int32_t v = 0; v < n; v++)
+            if (w[v] < 0) { set_error("weight w[%d] = %d is negative", v, w[v]); return GBC_ERR_ARG; }
+    if (ff)
+        for (int32_t v = 0; v < n; v++)
+            if (ff[v] < 0) { set_error("ff[%d] = %lld is negative", v, (long long)ff[v]); return GBC_ERR_ARG; }
+    // the captured level loops hold the old pointers
+    G->eng.reset();
+    G->g.w = nullptr;
+    G->g.ff = nullptr;
+    cudaFree(G->d_w);
+    cudaFree(G->d_ff);
+    G->d_w = nullptr;
+    G->d_ff = nullptr;
+    if (!w && !ff) return GBC_OK;
+    // caller ids -> internal ids: internal[new] = caller[order[new]]
+    void* tmp = nullptr;
+    if (cudaMalloc(&tmp, sizeof(int64_t) * std::max<int32_t>(n, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("weight staging buffer");
+        return GBC_ERR_NOMEM;
+    }
+    std::unique_ptr<void, void (*)(void*)> keep(tmp, [](void* p) { cudaFree(p); });
+    if (w) {
+        if (cudaMalloc(&G->d_w, sizeof(int32_t) * std::max<int32_t>(n, 1)) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("weight buffer");
+            return GBC_ERR_NOMEM;
+        }
+        GBC_CUDA(cudaMemcpyAsync(tmp, w, sizeof(int32_t) * n, cudaMemcpyHostToDevice, G->stream));
+        GBC_TRY(gather_to_caller<int32_t>(static_cast<const int32_t*>(tmp), G->d_order, n, 1, G->d_w, G->stream));
+        G->g.w = G->d_w;
+    }
+    if (ff) {
+        if (cudaMalloc(&G->d_ff, sizeof(int64_t) * std::max<int32_t>(n, 1)) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("ff buffer");
+            return GBC_ERR_NOMEM;
+        }
+        GBC_CUDA(cudaMemcpyAsync(tmp, ff, sizeof(int64_t) * n, cudaMemcpyHostToDevice, G->stream));
+        GBC_TRY(gather_to_caller<uint64_t>(static_cast<const uint64_t*>(tmp), G->d_order, n, 1,
+                                           reinterpret_cast<uint64_t*>(G->d_ff), G->stream));
+        G->g.ff = G->d_ff;
+    }
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    return GBC_OK;
+}
+
 gbc_status gbc_graph_destroy(gbc_graph g) {
     if (!g) { set_error("graph is NULL"); return GBC_ERR_ARG; }
     delete g;
@@ -655,6 +725,7 @@ gbc_status gbc_bc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
+    GBC_TRY(check_weighted(G, o, true));
     std::vector<int32_t> hsrc, pos;
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
     GBC_TRY(order_sources(G, o, true, hsrc, pos));
@@ -685,6 +756,7 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
+    GBC_TRY(check_weighted(G, o, true));
     cudaStream_t us = (cudaStream_t)stream;
     GBC_CUDA(cudaEventRecord(G->ev0, us));
     GBC_CUDA(cudaStreamWaitEvent(G->stream, G->ev0, 0));
@@ -752,6 +824,7 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
     std::lock_guard<std::mutex> lk(G->mu);
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
+    GBC_TRY(check_weighted(G, o, true));
     if (o.engine == GBC_ENGINE_PLAIN) { set_error("autotuning applies to the lane engine"); return GBC_ERR_ARG; }
     std::vector<int32_t> hsrc, pos;
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
@@ -826,6 +899,7 @@ gbc_status gbc_cc(gbc_graph G, const int32_t* sources, int32_t k, const gbc_opti
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
+    GBC_TRY(check_weighted(G, o, false));
     std::vector<int32_t> hsrc, pos;
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
     GBC_TRY(order_sources(G, o, false, hsrc, pos));
@@ -861,6 +935,7 @@ gbc_status gbc_cc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
     const double t0 = now_ms();
     gbc_options o;
     GBC_TRY(resolve_options(opt, o));
+    GBC_TRY(check_weighted(G, o, false));
     if (o.engine == GBC_ENGINE_PLAIN) { set_error("gbc_cc_device runs the lane engine only"); return GBC_ERR_ARG; }
     cudaStream_t us = (cudaStream_t)stream;
     GBC_CUDA(cudaEventRecord(G->ev0, us));

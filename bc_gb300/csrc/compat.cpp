@@ -261,6 +261,54 @@ int* computeCC(struct CSR* c, int* CCs) {
 
 void computeCC_shareBased(struct CSR* c, int* CCs) { closeness_into(c, true, GBC_ENGINE_LANES, CCs, true); }
 
+void compute_D1_CC(struct CSR* c, int* CCs) {
+    D1Folding(c);
+    const int32_t N = c->csrVSize - 1;
+    // live ranges of the unfolded vertices (folded neighbours sit before csrV[v]); folded vertices get empty rows
+    std::vector<int64_t> row(N + 1, 0);
+    std::vector<int32_t> col;
+    std::vector<int32_t> w(N, 1);
+    std::vector<int64_t> ff(N, 0);
+    col.reserve(c->csrESize > 0 ? c->csrESize : 0);
+    for (int32_t v = 0; v < N; v++) {
+        if (v >= c->startNodeID && v <= c->endNodeID && c->nodesType[v] != D1) {
+            for (int e = c->csrV[v]; e < c->oriCsrV[v + 1]; e++) col.push_back(c->csrE[e]);
+            w[v] = c->representNode[v];
+            ff[v] = c->ff[v];
+        }
+        row[v + 1] = (int64_t)col.size();
+    }
+    std::vector<int32_t> src(c->notD1Node, c->notD1Node + c->ordinaryNodeCount);
+    gbc_graph g = nullptr;
+    ok(gbc_graph_create(row.data(), col.data(), N, &g), "gbc_graph_create");
+    ok(gbc_graph_set_weights(g, w.data(), ff.data()), "gbc_graph_set_weights");
+    std::vector<int64_t> cc(src.size());
+    gbc_options o;
+    gbc_options_default(&o);
+    if (!src.empty()) ok(gbc_cc(g, src.data(), (int32_t)src.size(), &o, cc.data()), "gbc_cc");
+    gbc_graph_destroy(g);
+    for (size_t i = 0; i < src.size(); i++) CCs[src[i]] += (int)cc[i];
+    // vertex count of every connected component, over the original rows
+    std::vector<int32_t> parent(N);
+    for (int32_t v = 0; v < N; v++) parent[v] = v;
+    auto find = [&](int32_t x) {
+        while (parent[x] != x) x = parent[x] = parent[parent[x]];
+        return x;
+    };
+    for (int32_t v = c->startNodeID; v <= c->endNodeID; v++)
+        for (int e = c->oriCsrV[v]; e < c->oriCsrV[v + 1]; e++) {
+            const int32_t a = find(v), b = find(c->csrE[e]);
+            if (a != b) parent[std::max(a, b)] = std::min(a, b);
+        }
+    std::vector<int32_t> size(N, 0);
+    for (int32_t v = c->startNodeID; v <= c->endNodeID; v++) size[find(v)]++;
+    const struct qQueue* q = c->degreeOneNodesQ;
+    for (int i = q->rear; i >= 0; i--) {
+        const int d1 = q->dataArr[i];
+        CCs[d1] = CCs[c->D1Parent[d1]] + size[find(d1)] - 2 * c->representNode[d1];
+    }
+}
+
 void compute_D1_AP_CC_shareBased_DegreeOrder(struct CSR* c, int* CCs) { reduced_closeness_into(c, CCs); }
 
 void gpu_fan(struct Graph* g, struct CSR* c) {
@@ -329,7 +377,7 @@ void D1Folding(struct CSR* c) {
     order.reserve(q->rear + 1);
     for (int i = 0; i <= q->rear; i++) {
         const int v = q->dataArr[i];
-        if (c->nodesType[v] == D1 && (order.empty() || true)) order.push_back(v);
+        if (c->nodesType[v] == D1) order.push_back(v);
     }
     // each folded vertex appears once (popped when its degree was 1)
     std::vector<char> seen(vs, 0);

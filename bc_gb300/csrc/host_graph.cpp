@@ -390,6 +390,37 @@ gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, i
     return export_csr(g, row_out, col_out);
 }
 
+// Cycles of min_len..max_len vertices (uniform), each through one uniformly
+// chosen vertex of the input and len - 1 new vertices: every chosen vertex
+// becomes an articulation point and every cycle a block of its own.
+gbc_status gbc_add_cycles(const int64_t* row, const int32_t* col, int32_t n, int32_t cycles, int32_t min_len,
+                          int32_t max_len, uint64_t seed, int64_t** row_out, int32_t** col_out, int32_t* n_out) {
+    gbc_status st = validate_csr(row, col, n);
+    if (st != GBC_OK) return st;
+    if (cycles < 0 || min_len < 3 || max_len < min_len) { set_error("bad cycle parameters"); return GBC_ERR_ARG; }
+    if ((int64_t)n + (int64_t)cycles * (max_len - 1) >= INT32_MAX) { set_error("too many vertices"); return GBC_ERR_ARG; }
+    std::vector<int32_t> eu, ev;
+    eu.reserve(row[n] / 2 + (int64_t)cycles * max_len);
+    ev.reserve(row[n] / 2 + (int64_t)cycles * max_len);
+    for (int32_t x = 0; x < n; x++)
+        for (int64_t e = row[x]; e < row[x + 1]; e++)
+            if (x < col[e]) { eu.push_back(x); ev.push_back(col[e]); }
+    Rng r(seed, 13);
+    int32_t next = n;
+    for (int32_t c = 0; c < cycles; c++) {
+        const int32_t host = (int32_t)r.below(n);
+        const int32_t len = min_len + (int32_t)r.below(max_len - min_len + 1);
+        int32_t prev = host;
+        for (int32_t i = 1; i < len; i++) { eu.push_back(prev); ev.push_back(next); prev = next++; }
+        eu.push_back(prev);
+        ev.push_back(host);
+    }
+    HostCSR g;
+    csr_from_edges(next, eu, ev, g);
+    *n_out = next;
+    return export_csr(g, row_out, col_out);
+}
+
 // "start end" header, then one "%f" line per vertex of values rounded to FP32
 // (the reference prints its float BC array this way).
 gbc_status gbc_write_scores(const char* path, const double* values, int32_t start, int32_t end, int32_t append) {

@@ -1,5 +1,5 @@
-// D1 folding + articulation-point (block) reduction for closeness, and D1
-// folding for betweenness.
+// D1 folding + articulation-point (block) reduction for closeness and
+// betweenness.
 //
 // Folding (as Lib/D1Process/D1Process.c:32-73): degree-1 vertices are peeled
 // repeatedly into their neighbour, which accumulates reach r (vertices it
@@ -46,10 +46,6 @@ struct Reduction {
     HostCSR core;
     std::vector<int32_t> core_v;      // core id -> vertex
     std::vector<int32_t> core_w;      // reach of each core vertex
-    std::unique_ptr<DevGraph> cdg;
-    int32_t* d_cw = nullptr;
-    int32_t* d_cinv = nullptr;        // core id -> internal id of the degree-relabelled device core graph
-    std::unique_ptr<LaneEngine> ceng;
     int32_t n_hub = 0;
     // connected components of the folded graph (alive vertices)
     std::vector<int32_t> comp;        // per vertex slot (-1 for the phantom slot)
@@ -85,20 +81,16 @@ struct Reduction {
     int32_t* d_w = nullptr;
     std::vector<int32_t> b_inv;       // slot -> internal id of the degree-relabelled device block graph
     cudaStream_t stream = nullptr;
-    std::unique_ptr<LaneEngine> eng;
-    // lane grouping of the two device graphs: level-profile order of their
-    // vertices (internal ids) and the group width it implies
-    std::vector<int32_t> b_order, c_order;
-    int32_t b_group = 0, c_group = 0;
+    std::unique_ptr<LaneEngine> eng;  // lane engine on the block graph (closeness; betweenness state once asked for)
+    // lane grouping of the block graph: level-profile order of its slots
+    // (internal ids) and the group width it implies
+    std::vector<int32_t> b_order;
+    int32_t b_group = 0;
     std::mutex mu;
     ~Reduction() {
         eng.reset();
-        ceng.reset();
         if (dg) { cudaFree(dg->row); cudaFree(dg->col); }
-        if (cdg) { cudaFree(cdg->row); cudaFree(cdg->col); }
         cudaFree(d_w);
-        cudaFree(d_cw);
-        cudaFree(d_cinv);
         cudaFree(d_core_row);
         cudaFree(d_core_col);
         cudaFree(d_bg_row);
@@ -423,23 +415,37 @@ static gbc_status profile_order(const DevGraph& g, cudaStream_t s, std::vector<i
     return GBC_OK;
 }
 
+// The lane engine over the block graph for a call: lanes and group width
+// from the options or the slot count and the memory budget, as graph handles
+// choose them; an engine with betweenness state also serves closeness.
+static gbc_status block_engine(Reduction& R, const gbc_options& o, bool bc, LaneEngine** out) {
+    const int32_t ns = R.bg.n;
+    if (R.b_order.empty()) GBC_TRY(profile_order(*R.dg, R.stream, R.b_order, R.b_group));
+    int32_t group = o.group_lanes ? o.group_lanes : R.b_group;
+    if (o.lanes % group) group = 32;
+    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + group - 1) / group) * group);
+    const size_t fr = dev_free_bytes() + (R.eng ? R.eng->device_bytes() : 0);
+    while (!o.lanes && lanes > group && LaneEngine::bytes_needed(ns, lanes, bc) > fr / 2) lanes -= group;
+    if (!R.eng || R.eng->lanes() != lanes || R.eng->group_lanes() != group || (bc && !R.eng->has_bc())) {
+        R.eng.reset();
+        auto e = std::make_unique<LaneEngine>();
+        GBC_TRY(e->init(R.dg.get(), lanes, bc, o.sparse_lanes, o.levels_per_graph, R.stream, group));
+        R.eng = std::move(e);
+    }
+    R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+    *out = R.eng.get();
+    return GBC_OK;
+}
+
 // D_B(slot) for every slot, by the lane engine over the block graph.
 static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<int64_t>& D) {
     GBC_TRY(upload(R));
     const int32_t ns = R.bg.n;
     D.assign(ns, 0);
     if (ns == 0) return GBC_OK;
-    if (R.b_order.empty()) GBC_TRY(profile_order(*R.dg, R.stream, R.b_order, R.b_group));
-    int32_t group = o.group_lanes ? o.group_lanes : R.b_group;
-    if (o.lanes % group) group = 32;
-    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + group - 1) / group) * group);
-    const size_t fr = dev_free_bytes();
-    while (!o.lanes && lanes > group && LaneEngine::bytes_needed(ns, lanes, false) > fr / 2) lanes -= group;
-    if (!R.eng || R.eng->lanes() != lanes || R.eng->group_lanes() != group) {
-        R.eng = std::make_unique<LaneEngine>();
-        GBC_TRY(R.eng->init(R.dg.get(), lanes, false, o.sparse_lanes, o.levels_per_graph, R.stream, group));
-    }
-    R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+    LaneEngine* E = nullptr;
+    GBC_TRY(block_engine(R, o, false, &E));
+    const int32_t lanes = E->lanes();
     int32_t* d_src = nullptr;
     unsigned long long* d_cc = nullptr;
     if (cudaMalloc(&d_src, sizeof(int32_t) * ns) != cudaSuccess || cudaMalloc(&d_cc, sizeof(unsigned long long) * ns) != cudaSuccess) {
@@ -462,7 +468,7 @@ static gbc_status weighted_sums(Reduction& R, const gbc_options& o, std::vector<
         rq.kb = std::min(lanes, ns - b0);
         rq.d_cc = d_cc + b0;
         rq.top_down_only = o.direction == 1;
-        GBC_TRY(R.eng->run(rq, res));
+        GBC_TRY(E->run(rq, res));
     }
     std::vector<int64_t> Dl(ns);
     GBC_CUDA(cudaMemcpyAsync(Dl.data(), d_cc, sizeof(int64_t) * ns, cudaMemcpyDeviceToHost, R.stream));
@@ -549,91 +555,91 @@ static void fold_bc(const Reduction& R, std::vector<double>& bc) {
     }
 }
 
-static gbc_status core_upload(Reduction& R) {
-    if (R.cdg) return GBC_OK;
-    int nd = 0;
-    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) { cudaGetLastError(); set_error("no CUDA device"); return GBC_ERR_NO_DEVICE; }
-    if (!R.stream) GBC_CUDA(cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking));
-    auto g = std::make_unique<DevGraph>();
-    g->n = R.core.n;
-    g->m = core_entries(R);
-    bool ok = cudaMalloc(&g->row, sizeof(int64_t) * (g->n + 1)) == cudaSuccess;
-    ok &= cudaMalloc(&g->col, sizeof(int32_t) * std::max<int64_t>(g->m, 1)) == cudaSuccess;
-    ok &= cudaMalloc(&R.d_cw, sizeof(int32_t) * std::max<int32_t>(g->n, 1)) == cudaSuccess;
-    if (!ok) { cudaGetLastError(); set_error("core graph allocation"); cudaFree(g->row); cudaFree(g->col); return GBC_ERR_NOMEM; }
-    GBC_TRY(graph_rows(*g, R.core, R.d_core_row, R.d_core_col));
-    if (g->n) GBC_CUDA(cudaMemcpy(R.d_cw, R.core_w.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
-    std::vector<int32_t> cinv;
-    GBC_TRY(relabel_weighted(*g, R.stream, &R.d_cw, cinv));
-    if (g->n) {
-        if (cudaMalloc(&R.d_cinv, sizeof(int32_t) * g->n) != cudaSuccess) { cudaGetLastError(); set_error("core id map"); return GBC_ERR_NOMEM; }
-        GBC_CUDA(cudaMemcpy(R.d_cinv, cinv.data(), sizeof(int32_t) * g->n, cudaMemcpyHostToDevice));
-    }
-    g->w = R.d_cw;
-    g->ff = nullptr;
-    R.cdg = std::move(g);
-    return GBC_OK;
-}
-
-// Reach-weighted Brandes over every core vertex on the device.
-static gbc_status core_bc(Reduction& R, const gbc_options& o, std::vector<double>& out) {
-    GBC_TRY(core_upload(R));
-    const int32_t nc = R.core.n;
-    out.assign(nc, 0.0);
-    if (nc == 0) return GBC_OK;
-    if (R.c_order.empty()) GBC_TRY(profile_order(*R.cdg, R.stream, R.c_order, R.c_group));
-    int32_t group = o.group_lanes ? o.group_lanes : R.c_group;
-    if (o.lanes % group) group = 32;
-    int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((nc + group - 1) / group) * group);
-    const size_t fr = dev_free_bytes();
-    while (!o.lanes && lanes > group && LaneEngine::bytes_needed(nc, lanes, true) > fr / 2) lanes -= group;
-    if (!R.ceng || R.ceng->lanes() != lanes || R.ceng->group_lanes() != group) {
-        R.ceng = std::make_unique<LaneEngine>();
-        GBC_TRY(R.ceng->init(R.cdg.get(), lanes, true, o.sparse_lanes, o.levels_per_graph, R.stream, group));
-    }
-    R.ceng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+// Betweenness through the block split.  A shortest path between vertices on
+// different sides of an articulation point b passes through b, and its part
+// inside a block B runs between the two vertices of B through which its ends
+// reach B.  The clone weight w'_B(a) counts every vertex that reaches B
+// through a (a's own reach for a vertex that is no articulation point), so
+// reach-weighted Brandes inside every block, every slot a source,
+//     BC_B(v) = sum over a != v != c in B of w'_B(a) w'_B(c) sigma^B_ac(v) / sigma^B_ac,
+// counts every pair of unfolded vertices whose shortest paths cross B with v
+// inside.  An articulation point v also lies on every path between two of the
+// sides it separates.  With N the total reach of v's component, the side
+// behind block B holds R_B = N - w'_B(v), and those sides hold N - r_v in all,
+// so the separated ordered pairs add (N - r_v)^2 - sum_B R_B^2.  With the
+// folded pendant trees' pair counts (fold_bc):
+//     BC(v) = fold(v) + sum_{B holding v} BC_B(v) + [v is an AP] ((N - r_v)^2 - sum_B (N - w'_B(v))^2).
+// The reference has no betweenness through these reductions; its AP clones
+// (Lib/AP_Process/AP_Process.c:916-1020) carry the same reach w'.
+static gbc_status block_bc(Reduction& R, const gbc_options& o, std::vector<double>& out) {
+    GBC_TRY(upload(R));
+    const int32_t ns = R.bg.n;
+    out.assign(ns, 0.0);
+    if (ns == 0) return GBC_OK;
+    LaneEngine* E = nullptr;
+    GBC_TRY(block_engine(R, o, true, &E));
+    const int32_t lanes = E->lanes();
     int32_t* d_src = nullptr;
     double* d_bc = nullptr;
-    if (cudaMalloc(&d_src, sizeof(int32_t) * nc) != cudaSuccess || cudaMalloc(&d_bc, sizeof(double) * nc) != cudaSuccess) {
+    if (cudaMalloc(&d_src, sizeof(int32_t) * ns) != cudaSuccess || cudaMalloc(&d_bc, sizeof(double) * ns) != cudaSuccess) {
         cudaGetLastError();
         cudaFree(d_src);
-        set_error("core buffers");
+        set_error("slot buffers");
         return GBC_ERR_NOMEM;
     }
     std::unique_ptr<void, void (*)(void*)> f1(d_src, [](void* p) { cudaFree(p); });
     std::unique_ptr<void, void (*)(void*)> f2(d_bc, [](void* p) { cudaFree(p); });
-    // every core vertex once, in level-profile order (internal ids)
-    GBC_CUDA(cudaMemcpyAsync(d_src, R.c_order.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice, R.stream));
-    GBC_TRY(R.ceng->bc_begin());
+    // every slot once, in level-profile order (internal ids)
+    GBC_CUDA(cudaMemcpyAsync(d_src, R.b_order.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, R.stream));
+    GBC_TRY(E->bc_begin());
     LaneResult res;
     bool wide = o.sigma_mode == GBC_SIGMA_WIDE;   // AUTO: later batches start wide after an overflow
-    for (int32_t b0 = 0; b0 < nc; b0 += lanes) {
+    for (int32_t b0 = 0; b0 < ns; b0 += lanes) {
         LaneRequest rq;
         rq.job = LaneJob::BC;
         rq.d_src = d_src + b0;
-        rq.kb = std::min(lanes, nc - b0);
+        rq.kb = std::min(lanes, ns - b0);
         rq.delta_f64 = o.delta_precision == GBC_DELTA_F64;
         rq.semantics = GBC_BC_BRANDES;
         rq.sigma_wide = wide;
         rq.abort_on_overflow = !rq.sigma_wide;
-        gbc_status st = R.ceng->run(rq, res);
+        gbc_status st = E->run(rq, res);
         if (st == GBC_ERR_OVERFLOW && o.sigma_mode == GBC_SIGMA_AUTO && !wide) {
             wide = true;
             rq.sigma_wide = 1;
             rq.abort_on_overflow = false;
-            st = R.ceng->run(rq, res);
+            st = E->run(rq, res);
         }
         if (st != GBC_OK) return st;
     }
-    GBC_TRY(R.ceng->bc_finish(d_bc));
-    // core BC in internal ids -> core ids
-    double* d_bc2 = nullptr;
-    if (cudaMalloc(&d_bc2, sizeof(double) * nc) != cudaSuccess) { cudaGetLastError(); set_error("core buffers"); return GBC_ERR_NOMEM; }
-    std::unique_ptr<void, void (*)(void*)> f3(d_bc2, [](void* p) { cudaFree(p); });
-    GBC_TRY(gather_to_caller<double>(d_bc, R.d_cinv, nc, 1, d_bc2, R.stream));
-    GBC_CUDA(cudaMemcpyAsync(out.data(), d_bc2, sizeof(double) * nc, cudaMemcpyDeviceToHost, R.stream));
+    GBC_TRY(E->bc_finish(d_bc));
+    std::vector<double> h(ns);
+    GBC_CUDA(cudaMemcpyAsync(h.data(), d_bc, sizeof(double) * ns, cudaMemcpyDeviceToHost, R.stream));
     GBC_CUDA(cudaStreamSynchronize(R.stream));
+    for (int32_t sl = 0; sl < ns; sl++) out[sl] = h[R.b_inv[sl]];
     return GBC_OK;
+}
+
+// bc[n] from the per-slot block terms, the separated pairs of the
+// articulation points and the folded pair counts.
+static void assemble_block_bc(const Reduction& R, const std::vector<double>& slot_bc, double* bc) {
+    std::vector<double> fb;
+    fold_bc(R, fb);
+    for (int32_t v = 0; v < R.n; v++) bc[v] = fb[v];
+    std::vector<double> sq(R.ap_child_blocks.size(), 0.0);
+    for (int64_t sl = 0; sl < (int64_t)R.slot_v.size(); sl++) {
+        const int32_t v = R.slot_v[sl];
+        bc[v] += slot_bc[sl];
+        if (R.is_ap[v]) {
+            const double side = (double)(R.comp_w[R.comp[v]] - R.slot_w[sl]);
+            sq[R.ap_index[v]] += side * side;
+        }
+    }
+    for (int32_t v = 0; v < R.n; v++) {
+        if (!R.is_ap[v]) continue;
+        const double others = (double)(R.comp_w[R.comp[v]] - R.r[v]);
+        bc[v] += others * others - sq[R.ap_index[v]];
+    }
 }
 
 }  // namespace gbc
@@ -890,11 +896,9 @@ gbc_status gbc_bc_reduced(gbc_reduced h, const gbc_options* opt, double* bc) {
         return GBC_ERR_ARG;
     }
     if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("bad lanes"); return GBC_ERR_ARG; }
-    std::vector<double> cb, fb;
-    GBC_TRY(core_bc(h->R, o, cb));
-    fold_bc(h->R, fb);
-    for (int32_t v = 0; v < h->R.n; v++) bc[v] = fb[v];
-    for (size_t i = 0; i < h->R.core_v.size(); i++) bc[h->R.core_v[i]] += cb[i];
+    std::vector<double> sb;
+    GBC_TRY(block_bc(h->R, o, sb));
+    assemble_block_bc(h->R, sb, bc);
     return GBC_OK;
 }
 

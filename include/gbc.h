@@ -128,6 +128,16 @@ gbc_status gbc_graph_create(const int64_t* row, const int32_t* col, int32_t n, g
 gbc_status gbc_graph_create_device(const int64_t* d_row, const int32_t* d_col, int32_t n,
                                    int64_t m_directed, gbc_graph* out);
 gbc_status gbc_graph_destroy(gbc_graph g);
+/* Vertex weights for the reduced-graph forms of the reference's algorithms
+ * (the reach "representNode" and folded distance sums "ff" that D1Folding
+ * leaves, Lib/D1Process/D1Process.c:43-46; used by compute_D1_CC,
+ * Seq_CC/CC.cpp:418).  w[n] >= 0 and ff[n] >= 0 are host arrays in the
+ * caller's ids; either may be NULL (w = 1, ff = 0); both NULL clears them.
+ * With weights set, gbc_cc returns sum over reached v of (ff[v] + d(s,v)*w[v])
+ * (v = s included), and gbc_bc (GBC_BC_BRANDES only) returns
+ * sum_s w[s] sum_t w[t] sigma_st(v)/sigma_st.  The plain engine refuses
+ * weighted graphs. */
+gbc_status gbc_graph_set_weights(gbc_graph g, const int32_t* w, const int64_t* ff);
 /* Device-side ingest: edge list (u[i], v[i]), i < m, ids in [0, n) -> the
  * symmetric CSR without self-loops or repeated edges, rows in ascending
  * neighbour order, built on the GPU (radix sort of both directions, unique,
@@ -189,8 +199,11 @@ gbc_status gbc_sssp(gbc_graph g, const int32_t* sources, int32_t k, const gbc_op
  * allocated on the host or the device.  Every call shares that array and
  * re-initialises it; calls that overlap on the GPU race and must be
  * serialised by the caller.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  Runs on
- * `stream` (a cudaStream_t) and returns when the results are written. */
+ * device address; make that first call before any stream capture.  Every
+ * call first checks the CSR on the device (row[0] == 0, rows non-decreasing,
+ * col entries in [0,n)) and refuses a bad one with GBC_ERR_ARG before the BFS
+ * touches the array.  Runs on `stream` (a cudaStream_t) and returns when the
+ * results are written. */
 #define GBC_NOALLOC_MAX_VERTICES (1 << 21)
 gbc_status gbc_cc_noalloc(const int64_t* d_row, const int32_t* d_col, int32_t n, const int32_t* d_sources,
                           int32_t k, int64_t* d_cc, void* stream);
@@ -233,10 +246,11 @@ gbc_status gbc_reduced_info_get(gbc_reduced r, gbc_reduced_info* info);
 /* Closeness of every vertex slot through the reduction: cc[n] (host).
  * Equal to gbc_cc over all vertices of the unreduced graph. */
 gbc_status gbc_cc_reduced(gbc_reduced r, const gbc_options* opt, int64_t* cc);
-/* Betweenness (GBC_BC_BRANDES) of every vertex slot through D1 folding:
- * reach-weighted Brandes over the unfolded vertices on the device plus the
- * exact pair counts of the folded pendant trees.  Equal to gbc_bc over all
- * vertices of the unreduced graph. */
+/* Betweenness (GBC_BC_BRANDES) of every vertex slot through D1 folding and
+ * the block split: reach-weighted Brandes inside every block with the clone
+ * weights w' on the device (every slot a source), plus the pairs each
+ * articulation point separates and the exact pair counts of the folded
+ * pendant trees.  Equal to gbc_bc over all vertices of the unreduced graph. */
 gbc_status gbc_bc_reduced(gbc_reduced r, const gbc_options* opt, double* bc);
 gbc_status gbc_reduced_destroy(gbc_reduced r);
 /* The block graph the reduction hands to the device: slot CSR (malloc'd,
@@ -266,6 +280,12 @@ gbc_status gbc_gen_er(int32_t n, double avg_degree, uint64_t seed, int64_t** row
  * chosen vertices of a CSR; returns a new CSR. */
 gbc_status gbc_add_pendants(const int64_t* row, const int32_t* col, int32_t n, int32_t trees, int32_t max_depth,
                             uint64_t seed, int64_t** row_out, int32_t** col_out, int32_t* n_out);
+/* Attach `cycles` cycles of min_len..max_len vertices (uniform, min_len >= 3)
+ * to uniformly chosen vertices of a CSR (each through its chosen vertex and
+ * len - 1 new ones): articulation points with small blocks behind them;
+ * returns a new CSR. */
+gbc_status gbc_add_cycles(const int64_t* row, const int32_t* col, int32_t n, int32_t cycles, int32_t min_len,
+                          int32_t max_len, uint64_t seed, int64_t** row_out, int32_t** col_out, int32_t* n_out);
 /* Edge-list text file (header "n m", then "u v" lines; 0- or 1-based as in
  * Lib/AdjList/AdjList.c:13) -> CSR over n (0-based) or n+1 (1-based) slots;
  * *start = 0 or 1.  Neighbours ordered by neighbour degree ascending. */

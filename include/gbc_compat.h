@@ -164,6 +164,16 @@ int* computeCC(struct CSR* csr, int* CCs);
  * batched lanes of the device engine stand in for the 32-neighbour sharing. */
 void computeCC_shareBased(struct CSR* csr, int* CCs);
 
+/* D1-folded closeness (Seq_CC/CC.cpp:418 compute_D1_CC): runs D1Folding on
+ * the struct first, as the reference does, then adds to CCs[s] of every
+ * unfolded vertex s the weighted distance sum ff[s] + sum over the other
+ * reached unfolded v of (ff[v] + d(s,v) * representNode[v]) over the live
+ * ranges, on the device; then sets the folded vertices in reverse folding
+ * order: CCs[d1] = CCs[parent] + N - 2 * representNode[d1].  N is the vertex
+ * count of d1's connected component; the reference uses totalNodeNumber,
+ * which is wrong on disconnected graphs. */
+void compute_D1_CC(struct CSR* csr, int* CCs);
+
 /* Release path (Seq_CC/CC.cpp:1728): D1 folding + articulation-point
  * splitting, then closeness of every vertex into CCs.  Also sets the
  * structural fields foldedDegreeOneCount, hubNodeCount, ordinaryNodeCount,

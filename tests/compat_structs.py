@@ -39,7 +39,7 @@ def bind(L):
         getattr(L, name).restype = None
     L.computeCC.argtypes = [P(CSR), P(I)]
     L.computeCC.restype = P(I)
-    for name in ("computeCC_shareBased", "compute_D1_AP_CC_shareBased_DegreeOrder"):
+    for name in ("computeCC_shareBased", "compute_D1_CC", "compute_D1_AP_CC_shareBased_DegreeOrder"):
         getattr(L, name).argtypes = [P(CSR), P(I)]
         getattr(L, name).restype = None
     for name in ("D1Folding", "AP_detection", "gpu_vb", "preprocess_then_parallel_sharedBased_DegreeOrder"):

@@ -77,6 +77,100 @@ def test_dropin_entry_points(gpu, datasets):
         assert (c2.contents.foldedDegreeOneCount, c2.contents.ap_count) == (st["d1"], st["ap"])
 
 
+@pytest.mark.parametrize("name", sorted(STRUCT))
+def test_dropin_closeness_variants(gpu, datasets, name):
+    """computeCC_shareBased (Seq_CC/CC.cpp:122), compute_D1_CC (CC.cpp:418)
+    and preprocess_then_parallel_sharedBased_DegreeOrder
+    (parallel_CC/para_CC.cu:61) through the struct-CSR drop-in on every
+    shipped dataset, against the reference's own closeness outputs."""
+    L = bind(gpu.lib())
+    fx = fixture(name)
+    g, c = load(L, datasets[name])
+    vs, s = c.contents.csrVSize, c.contents.startNodeID
+    out = (C.c_int * (2 * vs))()
+    L.computeCC_shareBased(c, out)
+    assert np.array_equal(np.frombuffer(out, np.int32)[s:vs - 1], fx["cc_ref"][s:].astype(np.int32))
+    g, c = load(L, datasets[name])
+    out = (C.c_int * (2 * vs))()
+    L.compute_D1_CC(c, out)
+    assert np.array_equal(np.frombuffer(out, np.int32)[s:vs - 1], fx["cc_ref"][s:].astype(np.int32))
+    assert c.contents.foldedDegreeOneCount == STRUCT[name]["d1"]   # the struct is left folded, as the reference leaves it
+    g, c = load(L, datasets[name])
+    L.preprocess_then_parallel_sharedBased_DegreeOrder(c)
+    got = np.ctypeslib.as_array(c.contents.CCs, shape=(vs - 1,))
+    assert np.array_equal(got[s:], fx["d1ap_cc_ref"][s:].astype(np.int32))
+
+
+def write_edgelist_1based(csr, path):
+    """The reference's text format, 1-based ids (slot 0 stays phantom, so an
+    isolated vertex 0 cannot flip the base detection)."""
+    u = np.repeat(np.arange(csr.n), np.diff(csr.row))
+    v = csr.col
+    keep = u < v
+    with open(path, "w") as f:
+        f.write(f"{csr.n} {int(keep.sum())}\n")
+        for a, b in zip(u[keep] + 1, v[keep] + 1):
+            f.write(f"{a} {b}\n")
+
+
+@pytest.mark.parametrize("case", ["er+pendants", "rmat+pendants", "counterexample"])
+def test_dropin_d1_cc_disconnected(gpu, orc, tmp_path, case):
+    """compute_D1_CC on disconnected graphs with pendant trees equals plain
+    BFS closeness: the folded vertices are recovered with their own
+    component's size (the reference's totalNodeNumber is wrong there)."""
+    if case == "er+pendants":
+        csr = gpu.add_pendants(gpu.gen_er(3000, 1.5, seed=7), 500, 3, 4)
+    elif case == "rmat+pendants":
+        csr = gpu.add_pendants(gpu.gen_rmat(12, 4, seed=3), 800, 3, 5)
+    else:   # a triangle with a pendant vertex, and a separate triangle
+        csr = gpu.CSR(np.array([0, 2, 4, 7, 8, 10, 12, 14]),
+                      np.array([1, 2, 0, 2, 0, 1, 3, 2, 5, 6, 4, 6, 4, 5], np.int32))
+    path = str(tmp_path / "g.txt")
+    write_edgelist_1based(csr, path)
+    L = bind(gpu.lib())
+    g, c = load(L, path)
+    vs = c.contents.csrVSize
+    assert vs - 1 == csr.n + 1
+    out = (C.c_int * (2 * vs))()
+    L.compute_D1_CC(c, out)
+    got = np.frombuffer(out, np.int32)[1:vs - 1].astype(np.int64)
+    ref = orc.cc(orc.Graph(csr.row, csr.col), np.arange(csr.n), nthreads=8)
+    assert np.array_equal(got, ref)
+    assert c.contents.foldedDegreeOneCount > 0
+
+
+def test_graph_vertex_weights(gpu, orc):
+    """gbc_graph_set_weights: weighted closeness sums against the oracle's
+    weighted form; reach-weighted betweenness of the folded graph, assembled
+    with the folding's pair counts, against plain Brandes of the whole
+    graph; weights cleared give the unweighted results back."""
+    csr = gpu.add_pendants(gpu.gen_rmat(11, 6, seed=4), 300, 3, 6)
+    rng = np.random.default_rng(2)
+    w = rng.integers(0, 6, csr.n).astype(np.int32)
+    ff = rng.integers(0, 1000, csr.n).astype(np.int64)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.arange(0, csr.n, 3, dtype=np.int32)
+    with gpu.Graph(csr) as G:
+        G.set_weights(w, ff)
+        got = G.cc(src)
+        with pytest.raises(gpu.GbcError):
+            G.cc(src[:4], engine=gpu.ENGINE_PLAIN)
+        with pytest.raises(gpu.GbcError):
+            G.bc(src[:4], semantics=gpu.BC_REFERENCE)
+        G.set_weights(None, None)
+        plain = G.cc(src)
+    assert np.array_equal(got, orc.cc(og, src, w=w, ff=ff, nthreads=8))
+    assert np.array_equal(plain, orc.cc(og, src, nthreads=8))
+    R = gpu.Reduced(csr)
+    core, cw, cv = R.core_graph()
+    with gpu.Graph(core) as G:
+        G.set_weights(cw)
+        core_bc = G.bc(None, delta_precision=gpu.DELTA_F64)
+    full = R.assemble_bc(core_bc)
+    ref, _ = orc.bc(og, np.arange(csr.n), nthreads=8)
+    assert float(np.max(np.abs(full - ref) / np.maximum(np.abs(ref), 1.0))) < 1e-9
+
+
 @pytest.mark.parametrize("name", ["tech-WHOIS.mtx", "ca-HepPh.mtx", "caida.mtx", "ia-email-EU.mtx"])
 def test_dropin_bc_vs_reference_large_datasets(gpu, datasets, name):
     """computeBC through the drop-in against the reference's own FP32 output on
@@ -132,23 +226,42 @@ def test_device_pointer_entry_points(gpu, orc):
     L.gbc_graph_destroy(h)
 
 
-@pytest.mark.parametrize("case", ["karate", "ca-HepPh", "rmat13+pendants", "forest+er"])
-def test_reduced_bc_matches_plain_brandes(gpu, orc, datasets, case):
-    """Betweenness through D1 folding (reach-weighted Brandes on the device
-    plus the folded pair counts) equals plain Brandes of the whole graph."""
+@pytest.mark.parametrize("case", ["karate", "ca-HepPh", "caida", "rmat13+pendants", "forest+er", "rmat13+cycles",
+                                  "rmat13+cycles+pendants", "chain-of-blocks", "grid-holes"])
+@pytest.mark.parametrize("host", [False, True])
+def test_reduced_bc_matches_plain_brandes(gpu, orc, datasets, case, host):
+    """Betweenness through D1 folding and the block split (reach-weighted
+    Brandes inside every block with clone weights on the device, plus the
+    pairs each articulation point separates and the folded pair counts)
+    equals plain Brandes of the whole graph, on graphs with hundreds to
+    thousands of articulation points, for both reductions."""
     if case == "karate":
         csr = gpu.read_edgelist(datasets["karate.txt"])
     elif case == "ca-HepPh":
         csr = gpu.read_edgelist(datasets["ca-HepPh.mtx"])
+    elif case == "caida":
+        csr = gpu.read_edgelist(datasets["caida.mtx"])
     elif case == "rmat13+pendants":
         csr = gpu.add_pendants(gpu.gen_rmat(13, 4, seed=5), 2500, 3, 9)
-    else:
+    elif case == "forest+er":
         csr = gpu.add_pendants(gpu.gen_er(3000, 1.2, seed=7), 800, 3, 11)
+    elif case == "rmat13+cycles":
+        csr = gpu.add_cycles(gpu.gen_rmat(13, 4, seed=5), 2000, 3, 6, 4)
+    elif case == "rmat13+cycles+pendants":
+        csr = gpu.add_pendants(gpu.add_cycles(gpu.gen_rmat(13, 4, seed=5), 1500, 3, 6, 4), 1500, 3, 9)
+    elif case == "chain-of-blocks":
+        csr = _chain_of_blocks(gpu)
+    else:
+        csr = gpu.gen_grid(60, 60, 0.3, seed=2, largest_only=False)
     og = orc.Graph(csr.row, csr.col, csr.start)
     ref, _ = orc.bc(og, np.arange(csr.start, csr.n), semantics=orc.BC_BRANDES, nthreads=8)
-    R = gpu.Reduced(csr)
-    got = R.bc()
-    assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+    R = gpu.Reduced(csr, on_host=host)
+    info = R.info()
+    if case in ("ca-HepPh", "caida", "rmat13+cycles", "rmat13+cycles+pendants", "chain-of-blocks"):
+        assert info["articulation_points"] > 50, info
+    for delta, tol in ((gpu.DELTA_F64, 1e-9), (gpu.DELTA_F32, 1e-6)):
+        got = R.bc(delta_precision=delta)
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < tol, (case, delta)
     with pytest.raises(gpu.GbcError):
         R.bc(semantics=gpu.BC_REFERENCE)
 

@@ -104,3 +104,39 @@ def test_grid1024_sampled_sources_vs_oracle(gpu, orc, grid1024):
     # the identity on the same sources (one component)
     interior = int(cc.sum()) - len(src) * (csr.n - 1)
     assert abs(float(b64.sum()) - interior) / interior < TOL_F64
+
+
+def test_c1_ba4096_all_sources(gpu, orc):
+    """The plain exact configuration whole: BA n=4096, m=4, seed 1, every
+    vertex a source, betweenness with FP64 delta in both semantics and
+    closeness, against the FP64 oracle (about 1.5 s of oracle time)."""
+    csr = gpu.gen_ba(4096, 4, 1)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.arange(csr.n, dtype=np.int32)
+    with gpu.Graph(csr) as G:
+        for sem in (orc.BC_BRANDES, orc.BC_REFERENCE):
+            ref, novf = orc.bc(og, src, semantics=sem, nthreads=16)
+            assert novf == 0
+            got = G.bc(None, semantics=sem, delta_precision=gpu.DELTA_F64, sigma_mode=gpu.SIGMA_EXACT)
+            assert relerr(got, ref) < TOL_F64, sem
+            assert G.stats()["sources"] == csr.n
+        cc = G.cc(None)
+    assert np.array_equal(cc, orc.cc(og, src, nthreads=16))
+
+
+def test_grid1024_256_of_8192_sources_vs_oracle(gpu, orc, grid1024):
+    """The deep configuration on 256 of its 8,192 uniformly sampled sources
+    (seed 3, as the bench draws them): betweenness in wide form against the
+    oracle's level-normalised FP64 form, closeness bit-exact."""
+    csr = grid1024
+    sample = np.random.default_rng(3).choice(csr.n, 8192, replace=False).astype(np.int32)
+    src = sample[:256]
+    og = orc.Graph(csr.row, csr.col)
+    ref, _ = orc.bc(og, src, semantics=orc.BC_BRANDES, scaled=True, nthreads=16)
+    with gpu.Graph(csr) as G:
+        b64 = G.bc(src, delta_precision=gpu.DELTA_F64)
+        b32 = G.bc(src, delta_precision=gpu.DELTA_F32)
+        cc = G.cc(src)
+    assert relerr(b64, ref) < TOL_F64
+    assert relerr(b32, ref) < TOL_F32_DEEP
+    assert np.array_equal(cc, orc.cc(og, src, nthreads=16))
