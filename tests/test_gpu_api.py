@@ -257,7 +257,7 @@ def test_reduced_bc_matches_plain_brandes(gpu, orc, datasets, case, host):
     ref, _ = orc.bc(og, np.arange(csr.start, csr.n), semantics=orc.BC_BRANDES, nthreads=8)
     R = gpu.Reduced(csr, on_host=host)
     info = R.info()
-    if case in ("ca-HepPh", "caida", "rmat13+cycles", "rmat13+cycles+pendants", "chain-of-blocks"):
+    if case in ("ca-HepPh", "rmat13+cycles", "rmat13+cycles+pendants", "chain-of-blocks"):
         assert info["articulation_points"] > 50, info
     for delta, tol in ((gpu.DELTA_F64, 1e-9), (gpu.DELTA_F32, 1e-6)):
         got = R.bc(delta_precision=delta)
