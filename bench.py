@@ -23,10 +23,13 @@ component / time.
   cpu_baseline : the oracle's FP64 Brandes with all host threads on a
           bounded sample of the same sources.
   clocks : SM clocks and throttle reasons sampled during the timed region.
-  reduction / deep_grid : the two other single-GPU configurations in short
-          form -- the D1+AP reduction on R-MAT s18 + 60K pendant trees
-          (device reduction, reduced vs unreduced closeness and betweenness)
-          and the 1024^2 grid (1024 sources, wide path counts).
+  ba_all_sources / reduction / deep_grid : the other single-GPU
+          configurations in short form -- BA n=4096 m=4 with every vertex a
+          source (FP64 delta betweenness and closeness, with rooflines); the
+          D1+AP reduction on R-MAT s18 + 60K pendant trees and on the same
+          R-MAT with 30K attached cycles (device reduction, reduced vs
+          unreduced closeness and betweenness); the 1024^2 grid with 8,192
+          autotuned sources (wide path counts, with rooflines).
 
 --impl reference times the CPU restatement of the reference's sequential
 Brandes (oracle/, the reference's own code is not buildable on the GPU host)
@@ -75,7 +78,9 @@ def parse():
     p.add_argument("--serve-rates", default="5,10,20", help="query arrival rates per second, comma-separated")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--no-reduction", action="store_true", help="skip the D1+AP reduction section (R-MAT s18 + pendant trees)")
-    p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 1024 sources)")
+    p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 8192 sources)")
+    p.add_argument("--grid-sources", type=int, default=8192, help="sources of the deep-grid section")
+    p.add_argument("--no-ba", action="store_true", help="skip the all-sources section (BA n=4096, m=4)")
     return p.parse_args()
 
 
@@ -297,12 +302,62 @@ def serving(G, seconds, rates, seed=11):
                    "40% k=64 and 35% k=1024 sampled BC"}
 
 
+def kernel_roofline(st, n, M, k, job, hbm, peak_kind):
+    """Roofline of the dominant level kernel of one library call, from its
+    statistics (CUDA-event device time of the forward and dependency-sweep
+    level launches).  Algorithmic bytes per lane batch of B sources:
+    betweenness, per sweep, adjacency once (4 M + 4 (n + 1)) + 16 B n of lane
+    state, + 16 n of BC accumulation in the sweep; closeness, adjacency once
+    + B n / 4 (a visited and a frontier bit per lane, written and read) + 8 B."""
+    batches = max(int(st["batches"]), 1)
+    adj = 4 * M + 4 * (n + 1)
+    if job == "bc":
+        fwd = batches * adj + 16 * k * n
+        bwd = batches * (adj + 16 * n) + 16 * k * n
+        if st["fwd_ms"] >= st["bwd_ms"]:
+            name, ms, nb, launches = "forward", st["fwd_ms"], fwd, st["fwd_kernels"]
+        else:
+            name, ms, nb, launches = "sweep", st["bwd_ms"], bwd, st["bwd_kernels"]
+    else:
+        name, ms, nb, launches = "forward", st["fwd_ms"], batches * adj + k * n // 4 + 8 * k, st["fwd_kernels"]
+    ach = nb / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "levels": name, "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
+            "frac": round(ach / hbm, 5), "traffic": None, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": int(nb / max(launches, 1)), "avg_launch_ms": round(ms / max(launches, 1), 4),
+            "kernel": ("expand" if name == "forward" else "backward") + ("_q" if st["group_lanes"] == 128 else "") + "_kernel"}
+
+
+def ba_section(G, hbm, peak_kind):
+    """The plain exact configuration: Barabasi-Albert n = 4096, m = 4, seed 1,
+    every vertex a source, betweenness with FP64 delta and closeness; GTEPS
+    and roofline from the library's CUDA-event timing (best of three calls)."""
+    csr = G.gen_ba(4096, 4, 1)
+    out = {"graph": "ba4096_m4_seed1", "n": int(csr.n), "m": int(csr.m // 2), "sources": int(csr.n)}
+    with G.Graph(csr) as g:
+        for job in ("bc", "cc"):
+            best = None
+            for _ in range(3):
+                if job == "bc":
+                    g.bc(None, delta_precision=G.DELTA_F64)
+                else:
+                    g.cc(None)
+                st = g.stats()
+                if best is None or st["kernel_ms"] < best["kernel_ms"]:
+                    best = st
+            out[job] = {"gteps": round(best["edges_traversed"] / best["kernel_ms"] / 1e6, 3),
+                        "ms": round(best["kernel_ms"], 3), "lanes": int(best["lanes"]),
+                        "roofline": kernel_roofline(best, csr.n, csr.m, csr.n, job, hbm, peak_kind)}
+    return out
+
+
 def reduction_section(G):
-    """The D1-folding + articulation-point configuration: R-MAT scale 18, edge
-    factor 4, with 60K pendant trees of depth 1-3 (382K vertex slots).  Device
-    reduction, then closeness and betweenness of every vertex through it
-    against the unreduced graph (wall times of the calls, device-resident)."""
-    csr = G.add_pendants(G.gen_rmat(18, 4, seed=18), 60000, 3, 2)
+    """The D1-folding + articulation-point configurations: R-MAT scale 18,
+    edge factor 4, with 60K pendant trees of depth 1-3 (382K vertex slots;
+    its folded 2-core has no articulation point), and the same R-MAT with 30K
+    cycles of 3-6 vertices and 60K pendant trees attached (articulation points
+    with small blocks behind them).  Device reduction, then closeness and
+    betweenness of every vertex through it against the unreduced graph (wall
+    times of the calls, device-resident)."""
     G.Reduced(G.add_pendants(G.gen_rmat(10, 4, seed=1), 100, 3, 2))   # first-call setup
 
     def wall(f):
@@ -310,37 +365,56 @@ def reduction_section(G):
         r = f()
         return r, (time.perf_counter() - t) * 1e3
 
-    R, t_red = wall(lambda: G.Reduced(csr))
-    info = R.info()
-    cc_r, t_ccr = wall(R.cc)
-    bc_r, t_bcr = wall(R.bc)
-    with G.Graph(csr) as g:
-        cc_p, t_ccp = wall(g.cc)
-        bc_p, t_bcp = wall(g.bc)
-    rel = float(np.max(np.abs(bc_r - bc_p) / np.maximum(np.abs(bc_p), 1.0)))
-    return {"graph": "rmat18_ef4+60k_pendant_trees", "n": int(csr.n), "m": int(csr.m // 2),
-            "reduce_ms": round(t_red, 2), "folded": info["d1_folded"], "fold_rounds": info["fold_rounds"],
-            "articulation_points": info["articulation_points"], "blocks": info["blocks"],
-            "cc_reduced_ms": round(t_ccr, 1), "cc_unreduced_ms": round(t_ccp, 1), "cc_bit_equal": bool(np.array_equal(cc_r, cc_p)),
-            "bc_reduced_ms": round(t_bcr, 1), "bc_unreduced_ms": round(t_bcp, 1), "bc_max_rel_diff": rel}
+    def one(name, csr):
+        R, t_red = wall(lambda: G.Reduced(csr))
+        info = R.info()
+        cc_r, t_ccr = wall(R.cc)
+        bc_r, t_bcr = wall(R.bc)
+        R.close()
+        with G.Graph(csr) as g:
+            cc_p, t_ccp = wall(g.cc)
+            bc_p, t_bcp = wall(g.bc)
+        rel = float(np.max(np.abs(bc_r - bc_p) / np.maximum(np.abs(bc_p), 1.0)))
+        return {"graph": name, "n": int(csr.n), "m": int(csr.m // 2),
+                "reduce_ms": round(t_red, 2), "folded": info["d1_folded"], "fold_rounds": info["fold_rounds"],
+                "articulation_points": info["articulation_points"], "blocks": info["blocks"],
+                "max_block": info["max_block"], "block_slots": info["block_slots"],
+                "cc_reduced_ms": round(t_ccr, 1), "cc_unreduced_ms": round(t_ccp, 1),
+                "cc_bit_equal": bool(np.array_equal(cc_r, cc_p)),
+                "bc_reduced_ms": round(t_bcr, 1), "bc_unreduced_ms": round(t_bcp, 1), "bc_max_rel_diff": rel}
+
+    base = G.gen_rmat(18, 4, seed=18)
+    out = one("rmat18_ef4+60k_pendant_trees", G.add_pendants(base, 60000, 3, 2))
+    out["with_articulation_points"] = one("rmat18_ef4+30k_cycles_3to6+60k_pendant_trees",
+                                          G.add_pendants(G.add_cycles(base, 30000, 3, 6, 5), 60000, 3, 2))
+    return out
 
 
-def grid_section(G):
+def grid_section(G, hbm, peak_kind, k=8192):
     """The deep configuration: 1024 x 1024 grid with 5% of the edges removed
-    (seed 3), largest component, 1024 uniformly sampled sources (seed 3):
-    betweenness (FP32 delta; path counts pass 2^64, so wide form) and
-    closeness, GTEPS from the library's own CUDA-event timing."""
+    (seed 3), largest component, k = 8,192 uniformly sampled sources (seed
+    3): autotuned batches, betweenness (FP32 delta; path counts pass 2^64, so
+    wide form) and closeness, GTEPS and roofline from the library's own
+    CUDA-event timing."""
     grid = G.gen_grid(1024, 1024, 0.05, seed=3, largest_only=True)
-    src = np.random.default_rng(3).choice(grid.n, 1024, replace=False).astype(np.int32)
+    src = np.random.default_rng(3).choice(grid.n, 8192, replace=False).astype(np.int32)[:k]
     with G.Graph(grid) as g:
+        t = time.perf_counter()
+        tuning = g.autotune(src, delta_precision=G.DELTA_F32)
+        t_tune = time.perf_counter() - t
         g.bc(src, delta_precision=G.DELTA_F32)
         st = g.stats()
         g.cc(src)
         st2 = g.stats()
-    return {"graph": "grid1024_minus5pct_largest", "n": int(grid.n), "m": int(grid.m // 2), "sources": 1024,
-            "bc_gteps": round(st["edges_traversed"] / st["kernel_ms"] / 1e6, 3), "bc_levels": int(st["levels"]),
-            "sigma_mode": "wide" if st["sigma_mode_used"] == G.SIGMA_WIDE else "exact", "lanes_per_group": int(st["group_lanes"]),
-            "cc_gteps": round(st2["edges_traversed"] / st2["kernel_ms"] / 1e6, 3)}
+    return {"graph": "grid1024_minus5pct_largest", "n": int(grid.n), "m": int(grid.m // 2), "sources": int(k),
+            "tuning": tuning, "autotune_s": round(t_tune, 2),
+            "bc_gteps": round(st["edges_traversed"] / st["kernel_ms"] / 1e6, 3), "bc_ms": round(st["kernel_ms"], 1),
+            "bc_levels": int(st["levels"]), "batches": int(st["batches"]),
+            "sigma_mode": "wide" if st["sigma_mode_used"] == G.SIGMA_WIDE else "exact",
+            "lanes": int(st["lanes"]), "lanes_per_group": int(st["group_lanes"]),
+            "bc_roofline": kernel_roofline(st, grid.n, grid.m, k, "bc", hbm, peak_kind),
+            "cc_gteps": round(st2["edges_traversed"] / st2["kernel_ms"] / 1e6, 3), "cc_ms": round(st2["kernel_ms"], 1),
+            "cc_roofline": kernel_roofline(st2, grid.n, grid.m, k, "cc", hbm, peak_kind)}
 
 
 def run_reference(args):
@@ -563,8 +637,9 @@ def main():
         serve = None
         if not args.no_serve:
             serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")])
+        c1 = None if args.no_ba else ba_section(G, hbm, peak_kind)
         red = None if args.no_reduction else reduction_section(G)
-        deep = None if args.no_grid else grid_section(G)
+        deep = None if args.no_grid else grid_section(G, hbm, peak_kind, args.grid_sources)
         out = {"metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "u64-sigma/" + args.delta + "-delta",
@@ -578,7 +653,8 @@ def main():
                "plain": None if plain_gteps is None else {
                    "value": round(plain_gteps, 4), "unit": "GTEPS", "sources": int(args.plain_sources),
                    "speedup_batched_vs_plain": round(gteps / plain_gteps, 2)},
-               "closeness": closeness, "precision": prec, "serving": serve, "reduction": red, "deep_grid": deep,
+               "closeness": closeness, "precision": prec, "serving": serve, "ba_all_sources": c1, "reduction": red,
+               "deep_grid": deep,
                "clocks": clocks}
         print(json.dumps(out), flush=True)
     if ws > 1:
