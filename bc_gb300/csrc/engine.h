@@ -145,6 +145,7 @@ private:
     int light_ = 16;
     int lpg_ = 16;
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
+    int hub_lim_ = -1;    // ids below this are the hubs (ids in descending degree order), -1: unknown
     size_t lvl_sz_ = 0, vmark_sz_ = 0, sig_sz_ = 0, rho_sz_ = 0, bcg_sz_ = 0;   // bytes of the cached buffers
     cudaStream_t stream_ = nullptr;
     size_t bytes_ = 0;

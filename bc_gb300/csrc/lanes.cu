@@ -100,6 +100,9 @@ struct KArgs {
     int32_t* lcomp;        // component label of every lane's source (-1: empty lane)
     uint32_t* done;        // [ng][ceil(n/32)] bits: (vertex, group) has no reachable unreached lane
     unsigned long long mtot;   // directed entries x lane groups
+    // vertices numbered by descending degree: the hubs are exactly the ids below hub_lim
+    // (-1: not known to be so numbered; the degree is read instead)
+    int hub_lim;
 };
 
 constexpr int HUB_DEG = 1024;   // 32-lane groups: entries of higher-degree vertices are expanded by a whole CTA
@@ -121,7 +124,9 @@ __device__ __forceinline__ size_t sidx(int g, int n, int v, int t, int gs) {
     return ((((size_t)g * (size_t)n) + (size_t)v) << gs) + (size_t)t;
 }
 
-__device__ __forceinline__ bool is_hub(const KArgs& A, int x) { return (A.row[x + 1] - A.row[x]) > A.hub_deg; }
+__device__ __forceinline__ bool is_hub(const KArgs& A, int x) {
+    return A.hub_lim >= 0 ? x < A.hub_lim : (A.row[x + 1] - A.row[x]) > A.hub_deg;
+}
 
 // ---- wide-exponent path counts ---------------------------------------------
 // Path counts past uint64 are held as (1 + f/2^44) * 2^(e - WBIAS) in one
@@ -276,6 +281,10 @@ __device__ __forceinline__ void warp_append(const KArgs& A, Stage& S, bool has, 
 }
 
 // First claim of (x, g) for level lev: a plain read filters repeats before the atomic.
+// Only a thread that saw one of x's active lanes unreached (and wrote d+1
+// there) claims: a lane already at d+1 was written by a thread that claimed,
+// so the claim happens once per discovered (x, g) without a vmark round trip
+// for the (many) later visits of the level.
 __device__ __forceinline__ bool claim(const KArgs& A, size_t gbase, int x, int lev) {
     int32_t* p = &A.vmark[gbase + x];
     if (*(volatile int32_t*)p == lev) return false;
@@ -468,14 +477,13 @@ __device__ __forceinline__ void fwd_lanes(const KArgs& A, Stage& S, int d, int g
             if (k >= kmax) break;
             const int q = k * SLOTS + s;
             const unsigned un = Sd::eq(Lw[k], 0xFFFFFFFFu) & act4;   // unreached, in active lanes
-            const unsigned gm = Sd::gt(Lw[k], d4) & act4;            // unreached or already at d+1
             if (un) {
                 LT* px = lv + ((size_t)xs[k] << 5) + w * LPW;
 #pragma unroll
                 for (int j = 0; j < LPW; j++)
                     if (Sd::has(un, j)) px[j] = (LT)(d + 1);
             }
-            const unsigned bal = __ballot_sync(FULL, gm != 0u);
+            const unsigned bal = __ballot_sync(FULL, un != 0u);
             const unsigned slotm = (bal >> (s * WPV)) & ((1u << WPV) - 1u);
             const bool has = (w == 0) && (q < cnt) && slotm && claim(A, gbase, xs[k], d + 1);
             warp_append(A, S, has, has && is_hub(A, xs[k]), ((uint32_t)xs[k] << 5) | (uint32_t)g);
@@ -659,8 +667,8 @@ __device__ __forceinline__ void fwd_scan(const KArgs& A, Stage& S, int d, int g,
                             wadd(ps, pe, sv);
                         }
                     }
-                    if (Lx > dl) {
-                        if (Lx == INF) *px = dnext;
+                    if (Lx == INF) {
+                        *px = dnext;
                         has = claim(A, gbase, x, d + 1);
                     }
                 }
@@ -752,8 +760,8 @@ __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint3
                     wadd(ws, we, sv);
                 }
             }
-            if (Lx > dl) {
-                if (Lx == INF) *px = dnext;
+            if (Lx == INF) {
+                *px = dnext;
                 has = claim(A, gbase, x, d + 1);
                 hub = has && is_hub(A, x);
             }
@@ -1198,14 +1206,12 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                     for (int j = 0; j < 4; j++)
                         if ((un >> j) & 1u) px[j] = (LT)(d + 1);
                 }
-                const unsigned gm = inr ? (q[i].gt(d) & act4) : 0u;
-                if (__ballot_sync(FULL, gm != 0u)) want |= 1u << i;
+                if (__ballot_sync(FULL, un != 0u)) want |= 1u << i;
             }
             const int xi = __shfl_sync(FULL, xm, (k0 + (t & (Q_ITER - 1))) & 31);
             const bool has = (t < Q_ITER) && ((want >> t) & 1u) && claim(A, gbase, xi, d + 1);
-            const long long dx = has ? A.row[xi + 1] - A.row[xi] : 0;
-            if (MODE == 0) S.fdeg += (unsigned long long)dx;
-            warp_append(A, S, has, dx > A.hub_deg, ((uint32_t)xi << 5) | (uint32_t)g);
+            if (MODE == 0 && has) S.fdeg += (unsigned long long)(A.row[xi + 1] - A.row[xi]);
+            warp_append(A, S, has, has && is_hub(A, xi), ((uint32_t)xi << 5) | (uint32_t)g);
         }
     }
 }
@@ -1268,14 +1274,13 @@ __device__ __forceinline__ void q_fwd_edges(const KArgs& A, Stage& S, int d, int
                             wadd(ps, pe, sv);
                         }
                     }
-                    if (Lx > dl) {
-                        if (Lx == INF) *px = dnext;
+                    if (Lx == INF) {
+                        *px = dnext;
                         has = claim(A, gbase, x, d + 1);
                     }
                 }
-                const long long dx = has ? A.row[x + 1] - A.row[x] : 0;
-                if (MODE == 0) S.fdeg += (unsigned long long)dx;
-                warp_append(A, S, has, dx > A.hub_deg, ((uint32_t)x << 5) | (uint32_t)g);
+                if (MODE == 0 && has) S.fdeg += (unsigned long long)(A.row[x + 1] - A.row[x]);
+                warp_append(A, S, has, has && is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
             }
             if (MODE == 1) {
 #pragma unroll
@@ -1365,7 +1370,7 @@ __device__ __forceinline__ bool q_bu_vertex(const KArgs& A, Stage& S, int d, int
             A.vmark[(size_t)g * A.n + x] = d + 1;
             S.fdeg += (unsigned long long)dx;
         }
-        warp_append(A, S, t == 0, dx > A.hub_deg, ((uint32_t)x << 5) | (uint32_t)g);
+        warp_append(A, S, t == 0, is_hub(A, x), ((uint32_t)x << 5) | (uint32_t)g);
     }
     if (open && t == 0) mu += (unsigned long long)dx;
     return !open;
@@ -1916,6 +1921,13 @@ __global__ void count_hubs_kernel(const int64_t* __restrict__ row, int32_t n, in
     }
 }
 
+// *out = 1 when some vertex has more neighbours than the one before it (ids
+// not in descending degree order).
+__global__ void degree_order_kernel(const int64_t* __restrict__ row, int32_t n, uint32_t* __restrict__ out) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x + 1; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (row[v + 1] - row[v] > row[v] - row[v - 1]) *out = 1u;
+}
+
 // bc[v] = sum over lane groups of the per-group partials (fixed order).
 __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, double* __restrict__ bc) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -1959,6 +1971,7 @@ struct LaneAccess {
         A.lcomp = e.lcomp_;
         A.done = e.done_;
         A.mtot = (unsigned long long)e.g_->m * (unsigned long long)e.ng_;
+        A.hub_lim = e.hub_lim_;
         return A;
     }
     // Reset the lane state a batch touched: per task when few were touched,
@@ -2101,11 +2114,18 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     {
         uint32_t nh = 0;
         GBC_CUDA(cudaMemsetAsync(ovf_, 0, sizeof(uint32_t), stream_));
+        uint32_t unsorted = 0;
+        GBC_CUDA(cudaMemsetAsync(ovf_ + 1, 0, sizeof(uint32_t), stream_));
         count_hubs_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(g->row, g->n, gs_ == 7 ? HUB_DEG_Q : HUB_DEG, ovf_);
         GBC_CUDA(cudaGetLastError());
+        degree_order_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(g->row, g->n, ovf_ + 1);
+        GBC_CUDA(cudaGetLastError());
         GBC_CUDA(cudaMemcpyAsync(&nh, ovf_, sizeof nh, cudaMemcpyDeviceToHost, stream_));
+        GBC_CUDA(cudaMemcpyAsync(&unsorted, ovf_ + 1, sizeof unsorted, cudaMemcpyDeviceToHost, stream_));
         GBC_CUDA(cudaStreamSynchronize(stream_));
         n_hubs_ = nh;
+        // ids in descending degree order (every device graph of this library): hub <=> id < n_hubs_
+        hub_lim_ = unsorted ? -1 : (int)nh;
     }
     GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));
