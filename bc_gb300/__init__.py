@@ -129,6 +129,7 @@ _PROTOS = [
     ("gbc_server_add_graph", _st, [_vp, _i64p, _i32p, C.c_int32, C.POINTER(C.c_int32)]),
     ("gbc_server_submit", _st, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(Options), C.c_double,
                                 C.POINTER(C.c_int64)]),
+    ("gbc_server_request_bytes", _st, [_vp, C.c_int32, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("gbc_server_poll", _st, [_vp, C.c_int64, C.POINTER(C.c_int32)]),
     ("gbc_server_wait", _st, [_vp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
     ("gbc_server_fetch", _st, [_vp, C.c_int64, _vp, _vp, C.POINTER(C.c_double)]),

@@ -11,9 +11,18 @@
 // (closeness or betweenness), oldest first; a request takes whole lane groups
 // (128 lanes on small-world graphs, else 32, as graph handles choose them), so
 // its betweenness partials stay separate and are added into its own FP64
-// result vector after each batch.  Its sources run in level-profile order.  Requests that arrive while a batch runs join the next batch.
-// Engines are created under an HBM budget and idle ones are released when a
-// new graph needs room.
+// result vector after each batch.  Its sources run in level-profile order.
+// Requests that arrive while a batch runs join the next batch.
+//
+// Device memory is admitted against one budget: a request is admitted, in
+// arrival order, only while the result vectors of the admitted (not yet
+// fetched) requests, the engines of the graphs with admitted work (or the
+// narrowest engine a graph could run with, while it has none) and its own
+// share fit.  Later requests wait behind one that does not fit; one that
+// could never fit fails.  Result vectors come from the library's device-buffer
+// cache when the request's first batch runs, not at submission.  Engines are
+// created under the same budget and idle ones are released when another
+// graph needs room.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,7 +60,10 @@ struct SGraph {
     // level-profile key of every internal id: a request's sources are sorted by
     // it, so that each 32-lane group holds sources whose BFS levels move together
     std::vector<uint32_t> key;
+    std::vector<int32_t> all_sorted;   // every caller id in that order (exact queries)
     int32_t group = 32;          // lanes per lane group: 128 on small-world graphs, as on graph handles
+    // device bytes of the narrowest lane engine this graph runs with
+    size_t engine_floor() const { return LaneEngine::bytes_needed(g.n, group, true); }
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
@@ -76,11 +88,12 @@ struct Req {
     gbc_status err = GBC_OK;
     std::string msg;
     double t_submit = 0, t_done = 0, deadline = 0;
-    double* d_bc = nullptr;      // device FP64 result (BC kinds)
+    double* d_bc = nullptr;      // device FP64 result (BC kinds), from the buffer cache at the first batch
+    size_t res_bytes = 0;        // device bytes of that result (admission charges them until fetched)
     std::vector<int64_t> cc;     // host result (CC), indexed by vertex
     bool admitted = false;
     int32_t inflight = 0;        // lane batches holding this request's sources or result buffer
-    ~Req() { cudaFree(d_bc); }
+    ~Req() { dev_release(d_bc, res_bytes); }
     bool bc() const { return kind != GBC_Q_CC; }
 };
 
@@ -112,6 +125,13 @@ struct gbc_server_s {
         for (auto& g : graphs) if (g->eng) b += g->eng->device_bytes();
         return b;
     }
+    // result bytes of admitted requests not yet fetched
+    size_t results_bytes() const {
+        size_t b = 0;
+        for (auto& kv : reqs) if (kv.second->admitted) b += kv.second->res_bytes;
+        return b;
+    }
+    void admit();
     void fail(Req& r, gbc_status st, const char* why) {
         r.state = GBC_REQ_FAILED;
         r.err = st;
@@ -122,31 +142,37 @@ struct gbc_server_s {
 
 namespace {
 
-// Engine for graph gi, as wide as its pending sources need (up to max_lanes),
-// making room under the budget by releasing the engines of graphs that
-// neither have pending work nor are held by a worker.  A narrower engine is
-// replaced when more sources wait than it holds; its buffers go to the cache.
+// Engine for graph gi, as wide as its pending sources need (up to max_lanes)
+// and the budget allows, counting the result vectors of admitted requests.
+// Idle engines (graphs that neither have admitted work nor are held by a
+// worker) are released to make room.  A graph's engine is replaced only by a
+// wider one that fits; its buffers go to the cache.
 gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy, int64_t pending) {
     SGraph& G = *S->graphs[gi];
     const int32_t gr = G.group;
     const int32_t cap = S->max_lanes / gr * gr;
     const int32_t want = (int32_t)std::min<int64_t>(cap, std::max<int64_t>(gr, (pending + gr - 1) / gr * gr));
     if (G.eng && (G.eng->lanes() >= want || G.eng->lanes() >= cap)) return GBC_OK;
-    G.eng.reset();
+    // bytes that stay held: results plus the engines of other graphs that are not idle
+    size_t held = S->results_bytes();
+    for (size_t j = 0; j < S->graphs.size(); j++)
+        if ((int32_t)j != gi && S->graphs[j]->eng && graph_busy[j]) held += S->graphs[j]->eng->device_bytes();
     int32_t lanes = want;
-    for (;;) {
-        const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true);
-        size_t used = S->engines_bytes();
-        if (used + need > S->budget) {
-            for (size_t j = 0; j < S->graphs.size() && used + need > S->budget; j++) {
-                if ((int32_t)j == gi || !S->graphs[j]->eng || graph_busy[j]) continue;
-                used -= S->graphs[j]->eng->device_bytes();
-                S->graphs[j]->eng.reset();
-            }
-        }
-        if (used + need <= S->budget) break;
-        if (lanes <= gr) { set_error("graph does not fit the HBM budget"); return GBC_ERR_BUSY; }
+    while (lanes > gr && held + LaneEngine::bytes_needed(G.g.n, lanes, true) > S->budget)
         lanes = std::max(gr, lanes / 2 / gr * gr);
+    if (held + LaneEngine::bytes_needed(G.g.n, lanes, true) > S->budget) {
+        if (G.eng) return GBC_OK;   // keep the engine it has
+        set_error("graph does not fit the HBM budget");
+        return GBC_ERR_BUSY;
+    }
+    if (G.eng && G.eng->lanes() >= lanes) return GBC_OK;   // nothing wider fits
+    G.eng.reset();
+    size_t used = S->engines_bytes() + S->results_bytes();
+    const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true);
+    for (size_t j = 0; j < S->graphs.size() && used + need > S->budget; j++) {
+        if ((int32_t)j == gi || !S->graphs[j]->eng || graph_busy[j]) continue;
+        used -= S->graphs[j]->eng->device_bytes();
+        S->graphs[j]->eng.reset();
     }
     auto e = std::make_unique<LaneEngine>();
     GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream, gr));
@@ -168,6 +194,47 @@ gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& g
 }
 
 }  // namespace
+
+// Admit queued requests in arrival order while their device bytes fit the
+// budget (and fewer than max_inflight hold sources).  Charged: the result
+// vectors of every admitted request not yet fetched, and per graph with
+// admitted work its engine, or the narrowest engine it could run with.
+// Called with mu held.
+void gbc_server_s::admit() {
+    int32_t inflight = 0;
+    for (int64_t id : fifo) inflight += reqs[id]->admitted;
+    std::vector<char> charged(graphs.size(), 0);
+    size_t reserved = results_bytes();
+    auto engine_bytes = [&](int32_t gi) {
+        const SGraph& G = *graphs[gi];
+        return G.eng ? std::max(G.eng->device_bytes(), G.engine_floor()) : G.engine_floor();
+    };
+    for (int64_t id : fifo) {
+        Req* r = reqs[id].get();
+        if (r->admitted && !charged[r->gid]) {
+            charged[r->gid] = 1;
+            reserved += engine_bytes(r->gid);
+        }
+    }
+    for (int64_t id : fifo) {
+        Req* r = reqs[id].get();
+        if (r->admitted || r->state != GBC_REQ_QUEUED) continue;
+        if (inflight >= max_inflight) break;
+        const size_t own = r->res_bytes + graphs[r->gid]->engine_floor();
+        if (own > budget) {
+            fail(*r, GBC_ERR_NOMEM, "the request's result and its graph's narrowest engine exceed the server's HBM budget");
+            cv_done.notify_all();
+            continue;
+        }
+        const size_t need = r->res_bytes + (charged[r->gid] ? 0 : engine_bytes(r->gid));
+        if (reserved + need > budget) break;   // first come, first served: later requests wait behind it
+        r->admitted = true;
+        r->state = GBC_REQ_RUNNING;
+        inflight++;
+        reserved += need;
+        charged[r->gid] = 1;
+    }
+}
 
 void gbc_server_s::run() {
     std::vector<int32_t> hsrc;
@@ -198,13 +265,7 @@ void gbc_server_s::run() {
                     }
                     ++it;
                 }
-                // admission: up to max_inflight requests hold sources in flight
-                int32_t inflight = 0;
-                for (int64_t id : fifo) inflight += reqs[id]->admitted;
-                for (int64_t id : fifo) {
-                    Req* r = reqs[id].get();
-                    if (!r->admitted && inflight < max_inflight) { r->admitted = true; r->state = GBC_REQ_RUNNING; inflight++; }
-                }
+                admit();
                 // pick a graph with pending sources that no other worker holds, round robin
                 std::vector<bool> busy(graphs.size(), false);
                 for (int64_t id : fifo) {
@@ -268,13 +329,32 @@ void gbc_server_s::run() {
         hdst.assign(ng, nullptr);
         int32_t kb = 0;
         const bool bc_batch = kind > 0;
+        gbc_status st = GBC_OK;
+        // result vectors of requests in their first batch: from the buffer cache, zeroed on this stream
+        for (auto& sl : slots) {
+            Req* r = sl.r;
+            if (!bc_batch || r->d_bc || st != GBC_OK) continue;
+            double* p = nullptr;
+            if (dev_alloc((void**)&p, r->res_bytes) != cudaSuccess) {
+                cudaGetLastError();
+                set_error("result vector of %zu bytes", r->res_bytes);
+                st = GBC_ERR_NOMEM;
+            } else if (cudaMemsetAsync(p, 0, r->res_bytes, stream) != cudaSuccess) {
+                cudaGetLastError();
+                dev_release(p, r->res_bytes);
+                set_error("result vector reset failed");
+                st = GBC_ERR_CUDA;
+            } else {
+                r->d_bc = p;   // only the worker holding this graph touches it until the request is fetched
+            }
+        }
         for (auto& sl : slots) {
             for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = G.h_inv[sl.r->src[sl.first + i]];
             for (int32_t gg = sl.lane0 / grp; gg < (sl.lane0 + sl.count + grp - 1) / grp; gg++) hdst[gg] = sl.r->d_bc;
             kb = std::max(kb, ((sl.lane0 + sl.count + grp - 1) / grp) * grp);
         }
-        gbc_status st = GBC_OK;
-        if (cudaMemcpyAsync(G.d_src, hsrc.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+        if (st == GBC_OK &&
+            cudaMemcpyAsync(G.d_src, hsrc.data(), sizeof(int32_t) * kb, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
             cudaGetLastError();
             st = GBC_ERR_CUDA;
             set_error("source upload failed");
@@ -310,6 +390,9 @@ void gbc_server_s::run() {
             hcc.assign(kb, 0);
             if (st == GBC_OK) st = G.eng->cc_read(hcc.data(), kb);
         }
+        // a failed batch may leave copies or kernels queued: let them finish before
+        // its requests' buffers can go back to the cache
+        if (st != GBC_OK && cudaStreamSynchronize(stream) != cudaSuccess) cudaGetLastError();
         {
             std::lock_guard<std::mutex> lk(mu);
             G.running = false;
@@ -405,6 +488,13 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     int32_t depth = 0;
     GBC_TRY(level_profile_key(G->g, G->stream, G->key, depth));
     G->group = (depth > 0 && depth <= SMALL_WORLD_DEPTH && s->max_lanes % 128 == 0) ? 128 : 32;
+    G->all_sorted.resize(n);
+    for (int32_t i = 0; i < n; i++) G->all_sorted[i] = i;
+    {
+        const SGraph* SG = G.get();
+        std::stable_sort(G->all_sorted.begin(), G->all_sorted.end(),
+                         [SG](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
+    }
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
@@ -438,27 +528,19 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
     if (r->opt.semantics != GBC_BC_BRANDES && r->opt.semantics != GBC_BC_REFERENCE) { set_error("bad semantics"); return GBC_ERR_ARG; }
     r->gid = gid;
     r->kind = kind;
+    // sources in level-profile order (results are per vertex, so the order is free)
     if (kind == GBC_Q_BC_SAMPLED) {
         if (k < 1) { set_error("sampled BC needs k >= 1"); return GBC_ERR_ARG; }
         Rng rng(seed, 17);
         r->src.resize(k);
         for (int32_t i = 0; i < k; i++) r->src[i] = (int32_t)rng.below((uint64_t)n);
+        std::stable_sort(r->src.begin(), r->src.end(),
+                         [&](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
     } else {
-        r->src.resize(n);
-        for (int32_t i = 0; i < n; i++) r->src[i] = i;
+        r->src = SG->all_sorted;
     }
-    // sources in level-profile order (results are per vertex, so the order is free)
-    std::stable_sort(r->src.begin(), r->src.end(),
-                     [&](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
-    if (r->bc()) {
-        if (cudaMalloc(&r->d_bc, sizeof(double) * n) != cudaSuccess || cudaMemset(r->d_bc, 0, sizeof(double) * n) != cudaSuccess) {
-            cudaGetLastError();
-            set_error("result allocation");
-            return GBC_ERR_NOMEM;
-        }
-    } else {
-        r->cc.assign(n, 0);
-    }
+    if (r->bc()) r->res_bytes = sizeof(double) * (size_t)n;
+    else r->cc.assign(n, 0);
     r->t_submit = now_ms();
     r->deadline = deadline_ms > 0 ? r->t_submit + deadline_ms : 0;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -467,6 +549,17 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
     s->fifo.push_back(r->id);
     s->reqs[r->id] = std::move(r);
     s->cv_work.notify_all();
+    return GBC_OK;
+}
+
+gbc_status gbc_server_request_bytes(gbc_server s, int32_t gid, int32_t kind, size_t* result_bytes, size_t* engine_bytes) {
+    if (!s) { set_error("NULL server"); return GBC_ERR_ARG; }
+    if (kind < GBC_Q_CC || kind > GBC_Q_BC_SAMPLED) { set_error("bad query kind"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (gid < 0 || gid >= (int32_t)s->graphs.size()) { set_error("unknown graph %d", gid); return GBC_ERR_NOT_FOUND; }
+    const SGraph& G = *s->graphs[gid];
+    if (result_bytes) *result_bytes = kind == GBC_Q_CC ? 0 : sizeof(double) * (size_t)G.g.n;
+    if (engine_bytes) *engine_bytes = G.engine_floor();
     return GBC_OK;
 }
 
@@ -527,8 +620,9 @@ gbc_status gbc_server_fetch(gbc_server s, int64_t id, double* bc, int64_t* cc, d
     if (r->bc() && bc) {
         // the result accumulated in internal ids: gather to the caller's, through a scratch vector
         double* tmp = nullptr;
-        if (cudaMalloc(&tmp, sizeof(double) * n) != cudaSuccess) { cudaGetLastError(); set_error("fetch buffer"); return GBC_ERR_NOMEM; }
-        std::unique_ptr<double, void (*)(double*)> ft(tmp, [](double* p) { cudaFree(p); });
+        const size_t bytes = sizeof(double) * (size_t)n;
+        if (dev_alloc((void**)&tmp, bytes) != cudaSuccess) { cudaGetLastError(); set_error("fetch buffer"); return GBC_ERR_NOMEM; }
+        struct Tmp { double* p; size_t b; ~Tmp() { dev_release(p, b); } } ft{tmp, bytes};   // after the synchronous copy below
         const int32_t* d_inv = nullptr;
         {
             std::lock_guard<std::mutex> lk(s->mu);

@@ -75,7 +75,8 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
-    p.add_argument("--serve-rates", default="5,10,20", help="query arrival rates per second, comma-separated")
+    p.add_argument("--serve-rates", default="5,10,20,40", help="query arrival rates per second, comma-separated")
+    p.add_argument("--serve-burst", type=int, default=96, help="queries submitted at once for the saturation point")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--no-reduction", action="store_true", help="skip the D1+AP reduction section (R-MAT s18 + pendant trees)")
     p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 8192 sources)")
@@ -210,14 +211,16 @@ def cpu_baseline(csr, sample, n_src, threads):
     return dt
 
 
-def serving(G, seconds, rates, seed=11):
+def serving(G, seconds, rates, burst=96, seed=11):
     """The serving mix: a Poisson stream of queries over 64 device-resident
     graphs of 1K-2M vertices (BA m=2-8, Erdos-Renyi average degree 4-32,
     square grids, R-MAT scale 10-21; seeded sizes, log-uniform).  Queries:
     exact CC and exact BC on the smaller graphs, k = 64 / 1024 sampled BC
     everywhere.  One stream per arrival rate, on the same server; per rate the
     p50/p99 latency and the GTEPS delivered over the stream's wall time
-    (first arrival to last completion)."""
+    (first arrival to last completion).  The saturation point submits `burst`
+    queries of the same mix at once: its delivered GTEPS is the server's
+    capacity on this mix (the GPU busy nearly all of the time)."""
     import ctypes as C
     import random
     L = G.lib()
@@ -252,26 +255,31 @@ def serving(G, seconds, rates, seed=11):
         G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
         return [x.value for x in v]
 
-    def stream(rate):
+    def draw():
+        gi = rng.randrange(len(specs))
+        n = specs[gi][1].n
+        r = rng.random()
+        if r < 0.15 and n <= 32768:
+            kind, k = G.Q_CC, 0
+        elif r < 0.25 and n <= 16384:
+            kind, k = G.Q_BC, 0
+        elif r < 0.65:
+            kind, k = G.Q_BC_SAMPLED, 64
+        else:
+            kind, k = G.Q_BC_SAMPLED, 1024
+        rid = C.c_int64()
+        G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
+        return rid.value, gi
+
+    def stream(rate, count=0):
         reqs = []
         c0 = counters()
         t0 = time.perf_counter()
         t_end = t0 + seconds
-        while time.perf_counter() < t_end:
-            gi = rng.randrange(len(specs))
-            n = specs[gi][1].n
-            r = rng.random()
-            if r < 0.15 and n <= 32768:
-                kind, k = G.Q_CC, 0
-            elif r < 0.25 and n <= 16384:
-                kind, k = G.Q_BC, 0
-            elif r < 0.65:
-                kind, k = G.Q_BC_SAMPLED, 64
-            else:
-                kind, k = G.Q_BC_SAMPLED, 1024
-            rid = C.c_int64()
-            G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
-            reqs.append((rid.value, gi))
+        if count:
+            reqs = [draw() for _ in range(count)]
+        while not count and time.perf_counter() < t_end:
+            reqs.append(draw())
             time.sleep(rng.expovariate(rate))
         lats = []
         for rid, gi in reqs:
@@ -288,16 +296,19 @@ def serving(G, seconds, rates, seed=11):
         c1 = counters()
         lats = np.array(lats)
         busy = c1[4] - c0[4]
-        return {"rate_per_s": rate, "queries": len(lats), "p50_ms": round(float(np.percentile(lats, 50)), 3),
+        return {"rate_per_s": rate if not count else "burst", "queries": len(lats),
+                "p50_ms": round(float(np.percentile(lats, 50)), 3),
                 "p99_ms": round(float(np.percentile(lats, 99)), 3), "wall_s": round(wall, 3),
                 "lane_batches": c1[1] - c0[1], "shared_batches": c1[2] - c0[2],
                 "gteps_delivered": round((c1[3] - c0[3]) / wall / 1e9, 3),
                 "busy_frac": round(busy * 1e-3 / wall, 3)}
 
     points = [stream(r) for r in rates]
+    sat = stream(0.0, count=burst) if burst else None
     L.gbc_server_destroy(h)
     return {"graphs": len(specs), "vertices": [min(c.n for _, c in specs), max(c.n for _, c in specs)],
             "directed_entries": int(sum(c.m for _, c in specs)), "workers": 4, "points": points,
+            "saturation": sat,
             "mix": "uniform over graphs: 15% exact CC (graphs <= 32K vertices), 10% exact BC (<= 16K), "
                    "40% k=64 and 35% k=1024 sampled BC"}
 
@@ -636,7 +647,7 @@ def main():
                    "sample": f"first {n_cpu} of the {args.k} sampled sources, reference semantics, FP64"}
         serve = None
         if not args.no_serve:
-            serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")])
+            serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")], args.serve_burst)
         c1 = None if args.no_ba else ba_section(G, hbm, peak_kind)
         red = None if args.no_reduction else reduction_section(G)
         deep = None if args.no_grid else grid_section(G, hbm, peak_kind, args.grid_sources)

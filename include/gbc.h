@@ -306,16 +306,20 @@ gbc_status gbc_release_cached_memory(void);
 
 /* ---- serving: continuous batching over device-resident graphs ---------
  * A server owns a set of registered graphs and worker threads.  Requests
- * (exact CC, exact BC, or k-source sampled BC) are admitted while their lane
- * state fits the HBM budget; sources of concurrent requests on the same graph
- * share lane batches.  Results are identical (FP64 tolerance) alone and
- * mixed. */
+ * (exact CC, exact BC, or k-source sampled BC) are admitted in arrival order
+ * while their device bytes fit the HBM budget: the result vectors of the
+ * admitted requests not yet fetched (n FP64 values per BC request) plus, per
+ * graph with admitted work, its lane engine or the narrowest engine it could
+ * run with.  A request that does not fit waits, and later ones wait behind
+ * it; one that could never fit fails with GBC_ERR_NOMEM.  Sources of
+ * concurrent requests on the same graph share lane batches.  Results are
+ * identical (FP64 tolerance) alone and mixed. */
 typedef struct gbc_server_s* gbc_server;
 enum { GBC_Q_CC = 0, GBC_Q_BC = 1, GBC_Q_BC_SAMPLED = 2 };
 enum { GBC_REQ_QUEUED = 0, GBC_REQ_RUNNING = 1, GBC_REQ_DONE = 2, GBC_REQ_FAILED = 3, GBC_REQ_CANCELLED = 4 };
 
 typedef struct {
-    size_t  hbm_budget_bytes;   /* lane-state budget; 0 = 50% of free device memory */
+    size_t  hbm_budget_bytes;   /* engines + result vectors; 0 = 50% of free device memory */
     int32_t max_lanes;          /* lanes per shared batch (multiple of 32), 0 = 1024 */
     int32_t max_inflight;       /* requests admitted at once, 0 = 64 */
     int32_t workers;            /* lane batches in flight at once, on different graphs; 0 = 4 */
@@ -330,6 +334,11 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
  * uniformly with the seed.  deadline_ms <= 0 means none.  *req_id out. */
 gbc_status gbc_server_submit(gbc_server s, int32_t graph_id, int32_t kind, int32_t k, uint64_t seed,
                              const gbc_options* opt, double deadline_ms, int64_t* req_id);
+/* Device bytes a request of this kind on this graph is charged at
+ * admission: its result vector (until fetched) and the narrowest lane engine
+ * of the graph (charged once per graph with admitted work). */
+gbc_status gbc_server_request_bytes(gbc_server s, int32_t graph_id, int32_t kind, size_t* result_bytes,
+                                    size_t* engine_bytes);
 /* Poll: *state = GBC_REQ_*; when DONE, result buffers may be fetched. */
 gbc_status gbc_server_poll(gbc_server s, int64_t req_id, int32_t* state);
 /* Block until the request finishes (timeout_ms <= 0: no timeout). */

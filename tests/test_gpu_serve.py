@@ -179,6 +179,82 @@ def test_admission_under_small_budget(gpu, orc, graphs):
     S.close()
 
 
+def request_bytes(S, gid, kind):
+    res, eng = C.c_size_t(), C.c_size_t()
+    S.g.check(S.L.gbc_server_request_bytes(S.h, gid, kind, C.byref(res), C.byref(eng)))
+    return res.value, eng.value
+
+
+def test_admission_by_device_footprint(gpu, orc, graphs):
+    """A budget that holds one exact-BC request (result vector + the graph's
+    narrowest engine) but not two: the second waits, queued, while the first
+    one's result is held, is admitted once it is fetched, and both equal the
+    oracle.  A request that could never fit fails with GBC_ERR_NOMEM."""
+    g = graphs[3]
+    probe = Server(gpu)
+    gid0 = probe.add(g)
+    res, eng = request_bytes(probe, gid0, gpu.Q_BC)
+    assert res == 8 * g.n and eng > 0
+    assert request_bytes(probe, gid0, gpu.Q_CC)[0] == 0
+    probe.close()
+    S = Server(gpu, budget=eng + res + res // 2, workers=1)
+    gid = S.add(g)
+    r1 = S.submit(gid, gpu.Q_BC)
+    r2 = S.submit(gid, gpu.Q_BC)
+    assert S.wait(r1) == gpu.REQ_DONE
+    time.sleep(0.3)
+    st = C.c_int32()
+    S.g.check(S.L.gbc_server_poll(S.h, r2, C.byref(st)))
+    assert st.value == gpu.REQ_QUEUED, "the second request was admitted past the budget"
+    st1, bc1, _, _ = S.fetch(r1, gid)
+    assert st1 == 0
+    assert S.wait(r2) == gpu.REQ_DONE
+    st2, bc2, _, _ = S.fetch(r2, gid)
+    assert st2 == 0
+    S.close()
+    ref, _ = orc.bc(orc.Graph(g.row, g.col), np.arange(g.n), nthreads=8)
+    assert relerr(bc1, ref) < TOL and relerr(bc2, ref) < TOL
+    tiny = Server(gpu, budget=eng + res - 1)
+    gid = tiny.add(g)
+    r = tiny.submit(gid, gpu.Q_BC)
+    assert tiny.wait(r) == gpu.REQ_FAILED
+    assert tiny.fetch(r, gid)[0] == 3   # GBC_ERR_NOMEM
+    r = tiny.submit(gid, gpu.Q_CC)       # closeness results live on the host: it fits
+    assert tiny.wait(r) == gpu.REQ_DONE
+    tiny.close()
+
+
+def test_c5_size_mixed_equals_alone(gpu, graphs):
+    """Serving at the size of the serving mix: a k=1024 sampled-BC request on
+    an R-MAT scale-20 graph (1M vertices) submitted among small requests on
+    other graphs gives the same result as alone, and the same as a graph
+    handle's gbc_bc over the request's own sources."""
+    big = gpu.gen_rmat(20, 16, seed=21)
+    S = Server(gpu)
+    gb = S.add(big)
+    small = [S.add(g) for g in graphs]
+    rng = random.Random(9)
+    pre = [(gi, S.submit(small[gi], gpu.Q_BC_SAMPLED, 256, 500 + j)) for j, gi in
+           enumerate(rng.choice(range(len(graphs))) for _ in range(6))]
+    rb = S.submit(gb, gpu.Q_BC_SAMPLED, 1024, 77)
+    src = S.sources(rb)
+    post = [(gi, S.submit(small[gi], gpu.Q_CC if j % 2 else gpu.Q_BC_SAMPLED, 64, 600 + j)) for j, gi in
+            enumerate(rng.choice(range(len(graphs))) for _ in range(6))]
+    for gi, r in pre + post:
+        assert S.wait(r) == gpu.REQ_DONE
+        assert S.fetch(r, small[gi])[0] == 0
+    assert S.wait(rb, 600000.0) == gpu.REQ_DONE
+    st, mixed, _, _ = S.fetch(rb, gb)
+    assert st == 0
+    S.close()
+    alone, _ = run_alone(gpu, big, gpu.Q_BC_SAMPLED, 1024, 77, 0)
+    assert relerr(mixed, alone) < TOL
+    with gpu.Graph(big) as h:
+        direct = h.bc(src)
+    assert relerr(mixed, direct) < TOL
+    assert np.count_nonzero(mixed) > big.n // 4
+
+
 def test_worker_count(gpu, orc, graphs):
     """One worker and eight workers give the same results on the same
     stream; out-of-range worker counts are rejected."""
