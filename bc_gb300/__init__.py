@@ -36,7 +36,8 @@ class Options(C.Structure):
     _fields_ = [("semantics", C.c_int32), ("delta_precision", C.c_int32), ("sigma_mode", C.c_int32),
                 ("engine", C.c_int32), ("lanes", C.c_int32), ("sparse_lanes", C.c_int32),
                 ("levels_per_graph", C.c_int32), ("source_order", C.c_int32), ("light_steps", C.c_int32),
-                ("group_lanes", C.c_int32), ("direction", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("group_lanes", C.c_int32), ("direction", C.c_int32), ("block_threads", C.c_int32),
+                ("bu_share", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class RunStats(C.Structure):
@@ -330,11 +331,14 @@ class Graph:
     def autotune(self, sources=None, **opt) -> dict:
         """Time candidate expansion settings on these sources; later calls
         that leave them to autotuning use the fastest.  Returns the chosen
-        lanes / sparse_lanes / light_steps / levels_per_graph."""
+        lanes / sparse_lanes / light_steps / levels_per_graph / group_lanes /
+        block_threads, and on 128-lane groups the closeness direction
+        threshold (bu_share; direction 1 when top-down only was fastest)."""
         p, k, keep = self._src(sources)
         ch = Options()
         check(lib().gbc_autotune(self.h, p, k, C.byref(options(**opt)), C.byref(ch)))
-        return {f: getattr(ch, f) for f in ("lanes", "sparse_lanes", "light_steps", "levels_per_graph", "group_lanes")}
+        return {f: getattr(ch, f) for f in ("lanes", "sparse_lanes", "light_steps", "levels_per_graph", "group_lanes",
+                                            "block_threads", "bu_share", "direction")}
 
     def cc(self, sources=None, **opt) -> np.ndarray:
         p, k, keep = self._src(sources)

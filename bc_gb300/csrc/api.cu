@@ -42,6 +42,8 @@ struct gbc_graph_s {
     struct {
         bool done = false;
         int32_t lanes = 0, sparse = -1, light = -1, lpg = 0, group = 0;
+        int32_t block = 0;    // threads per CTA of the level kernels (0: default)
+        int32_t share = -1;   // closeness direction-switch share (0: top-down only; -1: default)
     } tuned;
     ~gbc_graph_s() {
         eng.reset();
@@ -200,6 +202,11 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (o.group_lanes != 0 && o.group_lanes != 32 && o.group_lanes != 128) { set_error("group_lanes must be 0, 32 or 128"); return GBC_ERR_ARG; }
     if (o.group_lanes == 128 && o.lanes % 128) { set_error("group_lanes 128 needs lanes = 0 or a multiple of 128"); return GBC_ERR_ARG; }
     if (o.direction != 0 && o.direction != 1) { set_error("direction must be 0 or 1"); return GBC_ERR_ARG; }
+    if (o.block_threads != 0 && o.block_threads != 128 && o.block_threads != 256 && o.block_threads != 512) {
+        set_error("block_threads must be 0, 128, 256 or 512");
+        return GBC_ERR_ARG;
+    }
+    if (o.bu_share < 0 || o.bu_share > 4096) { set_error("bu_share must be in [0,4096]"); return GBC_ERR_ARG; }
     return GBC_OK;
 }
 
@@ -245,26 +252,30 @@ static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requ
 
 // Expansion settings of a call: the options' values, or the graph's tuned ones
 // where the options leave them to autotuning.
-static void tuning_of(const gbc_graph_s* G, const gbc_options& o, int& sparse, int& light, int& lpg) {
+struct Tuning { int sparse, light, lpg, block, share; };
+static Tuning tuning_of(const gbc_graph_s* G, const gbc_options& o) {
     const bool t = G->tuned.done;
-    sparse = (o.sparse_lanes < 0 && t) ? G->tuned.sparse : o.sparse_lanes;
-    light = (o.light_steps < 0 && t) ? G->tuned.light : o.light_steps;
-    lpg = (o.levels_per_graph <= 0 && t) ? G->tuned.lpg : o.levels_per_graph;
+    Tuning u;
+    u.sparse = (o.sparse_lanes < 0 && t) ? G->tuned.sparse : o.sparse_lanes;
+    u.light = (o.light_steps < 0 && t) ? G->tuned.light : o.light_steps;
+    u.lpg = (o.levels_per_graph <= 0 && t) ? G->tuned.lpg : o.levels_per_graph;
+    u.block = (o.block_threads == 0 && t) ? G->tuned.block : o.block_threads;
+    u.share = o.bu_share > 0 ? o.bu_share : (t ? G->tuned.share : -1);
+    return u;
 }
 
 static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
-    int sparse, light, lpg;
-    tuning_of(G, o, sparse, light, lpg);
+    const Tuning u = tuning_of(G, o);
     const int32_t group = (lanes % 128 == 0) ? group_of(G, o) : 32;
     if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc) && G->eng->group_lanes() == group) {
-        G->eng->set_tuning(sparse, light, lpg);
+        G->eng->set_tuning(u.sparse, u.light, u.lpg, u.block, u.share);
         *out = G->eng.get();
         return GBC_OK;
     }
     G->eng.reset();
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G->g, lanes, bc, sparse, lpg, G->stream, group));
-    e->set_tuning(sparse, light, lpg);
+    GBC_TRY(e->init(&G->g, lanes, bc, u.sparse, u.lpg, G->stream, group));
+    e->set_tuning(u.sparse, u.light, u.lpg, u.block, u.share);
     G->eng = std::move(e);
     *out = G->eng.get();
     return GBC_OK;
@@ -789,12 +800,12 @@ gbc_status gbc_bc_device(gbc_graph G, const int32_t* d_sources, int32_t k, const
 // Device time (forward + dependency sweep) of one betweenness batch of the
 // staged sources d_src[0..kb) with the given expansion settings.
 static gbc_status tune_batch(gbc_graph_s* G, int32_t lanes, int32_t kb, const gbc_options& o, int sparse, int light,
-                             int lpg, int group, double& ms) {
+                             int lpg, int group, int block, double& ms) {
     LaneEngine* E = nullptr;
     gbc_options og = o;
     og.group_lanes = group;
     GBC_TRY(get_engine(G, lanes, true, og, &E));
-    E->set_tuning(sparse, light, lpg);
+    E->set_tuning(sparse, light, lpg, block, -1);
     GBC_TRY(E->bc_begin());
     LaneRequest rq;
     rq.job = LaneJob::BC;
@@ -819,6 +830,22 @@ static gbc_status tune_batch(gbc_graph_s* G, int32_t lanes, int32_t kb, const gb
     return GBC_OK;
 }
 
+// One closeness batch on the tuned engine with direction-switch share `share`
+// (0: top-down only); its forward device time.
+static gbc_status tune_cc_batch(gbc_graph_s* G, int32_t kb, int share, double& ms) {
+    LaneEngine* E = G->eng.get();
+    E->set_tuning(G->tuned.sparse, G->tuned.light, G->tuned.lpg, G->tuned.block, share);
+    LaneRequest rq;
+    rq.job = LaneJob::CC;
+    rq.d_src = G->d_src;
+    rq.kb = kb;
+    LaneResult res;
+    GBC_TRY(E->run(rq, res));
+    GBC_CUDA(cudaStreamSynchronize(G->stream));
+    ms = res.fwd_ms;
+    return GBC_OK;
+}
+
 gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gbc_options* opt, gbc_options* chosen) {
     if (!G) { set_error("graph is NULL"); return GBC_ERR_ARG; }
     std::lock_guard<std::mutex> lk(G->mu);
@@ -838,30 +865,34 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
     const int li0 = o.light_steps >= 0 ? o.light_steps : 16;
     const int lp0 = o.levels_per_graph > 0 ? o.levels_per_graph : 16;
     const int gr0 = o.group_lanes ? o.group_lanes : 32;
-    int best_sp = sp0, best_li = li0, best_lp = lp0, best_gr = gr0;
+    const int bt0 = o.block_threads ? o.block_threads : 256;
+    int best_sp = sp0, best_li = li0, best_lp = lp0, best_gr = gr0, best_bt = bt0;
     double best = 0;
     const int32_t kb = std::min(lanes, k0);
-    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, best));   // warm-up: level width, queue size, graph capture
-    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, best));
-    auto consider = [&](int sp, int li, int lp) -> gbc_status {
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, bt0, best));   // warm-up: level width, queue size, graph capture
+    GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, gr0, bt0, best));
+    auto consider = [&](int sp, int li, int lp, int bt) -> gbc_status {
         double ms = 0;
-        GBC_TRY(tune_batch(G, lanes, kb, o, sp, li, lp, best_gr, ms));
-        if (ms < best) { best = ms; best_sp = sp; best_li = li; best_lp = lp; }
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp, li, lp, best_gr, bt, ms));
+        if (ms < best) { best = ms; best_sp = sp; best_li = li; best_lp = lp; best_bt = bt; }
         return GBC_OK;
     };
     // lanes per group first: 128-lane groups (four lanes per thread) against 32
     if (o.group_lanes == 0 && lanes % 128 == 0) {
         double ms = 0;
-        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, ms));   // warm-up of the 128-lane engine
-        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, ms));
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, bt0, ms));   // warm-up of the 128-lane engine
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, bt0, ms));
         if (ms < best) { best = ms; best_gr = 128; }
     }
     // one-thread tasks, then the edge-parallel threshold, then the level-loop graph length
     if (o.light_steps < 0)
-        for (int li : {0, 8, 32}) GBC_TRY(consider(best_sp, li, best_lp));
+        for (int li : {0, 8, 32}) GBC_TRY(consider(best_sp, li, best_lp, best_bt));
     if (o.sparse_lanes < 0)
-        for (int sp : {1, 4}) GBC_TRY(consider(sp, best_li, best_lp));
-    if (o.levels_per_graph <= 0 && G->eng && G->eng->level_bytes() == 2) GBC_TRY(consider(best_sp, best_li, 64));
+        for (int sp : {1, 4}) GBC_TRY(consider(sp, best_li, best_lp, best_bt));
+    if (o.levels_per_graph <= 0 && G->eng && G->eng->level_bytes() == 2) GBC_TRY(consider(best_sp, best_li, 64, best_bt));
+    // CTA shape of the level kernels
+    if (o.block_threads == 0)
+        for (int bt : {128, 512}) GBC_TRY(consider(best_sp, best_li, best_lp, bt));
     // batch width: halve while the time per source drops (down to 32 lanes)
     int32_t best_lanes = lanes;
     if (o.lanes == 0 && kb == lanes) {
@@ -869,19 +900,37 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         for (int32_t w = lanes / 2; w >= 32; w /= 2) {
             double ms = 0;
             const int gw = (w % 128 == 0) ? best_gr : 32;
-            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, ms));   // warm-up of the narrower engine
-            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, ms));
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, best_bt, ms));   // warm-up of the narrower engine
+            GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, best_bt, ms));
             if (ms / w >= per_src) break;
             per_src = ms / w;
             best_lanes = w;
         }
     }
-    G->tuned.done = true;
     G->tuned.lanes = o.lanes ? 0 : best_lanes;
     G->tuned.sparse = best_sp;
     G->tuned.light = best_li;
     G->tuned.lpg = best_lp;
     G->tuned.group = best_gr;
+    G->tuned.block = best_bt;
+    G->tuned.share = -1;
+    // closeness direction threshold (128-lane groups only switch direction):
+    // one closeness batch of the same sources per share, 0 = top-down only
+    int best_share = o.bu_share > 0 ? o.bu_share : 16;
+    bool bu_tuned = false;
+    if (o.bu_share == 0 && o.direction == 0 && best_gr == 128 && G->eng && G->eng->group_lanes() == 128) {
+        const int32_t kc = std::min(G->eng->lanes(), k0);
+        double ms = 0, best_cc = 0;
+        GBC_TRY(tune_cc_batch(G, kc, 16, ms));        // warm-up: component labels, graph capture
+        GBC_TRY(tune_cc_batch(G, kc, 16, best_cc));
+        for (int sh : {0, 4, 8, 32, 64}) {
+            GBC_TRY(tune_cc_batch(G, kc, sh, ms));
+            if (ms < best_cc) { best_cc = ms; best_share = sh; }
+        }
+        G->tuned.share = best_share;
+        bu_tuned = true;
+    }
+    G->tuned.done = true;
     if (chosen) {
         *chosen = o;
         chosen->lanes = best_lanes;
@@ -889,6 +938,9 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         chosen->light_steps = best_li;
         chosen->levels_per_graph = best_lp;
         chosen->group_lanes = best_gr;
+        chosen->block_threads = best_bt;
+        chosen->bu_share = best_share;
+        if (bu_tuned && best_share == 0) chosen->direction = 1;
     }
     return GBC_OK;
 }

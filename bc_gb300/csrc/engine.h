@@ -109,9 +109,15 @@ public:
     // group_lanes: sources per lane group (32: one per warp thread; 128: four per thread).
     gbc_status init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
                     cudaStream_t stream, int group_lanes = 32);
-    // Expansion tuning (negative = default).  A change drops the captured
-    // level-loop graphs, which hold the old values.
-    void set_tuning(int sparse_lanes, int light_steps, int levels_per_graph);
+    // Expansion tuning (negative = default: 2 / 16 / 16 / 256 threads / 16;
+    // levels_per_graph 0 and block_threads 0 = default too).  block_threads: threads per CTA of the level kernels (128, 256 or
+    // 512); bu_share: closeness levels on 128-lane groups go bottom-up once
+    // past the frontier peak while frontier edges x bu_share exceed all edges x
+    // groups (0: never).  A change drops the captured level-loop graphs, which
+    // hold the old values.
+    void set_tuning(int sparse_lanes, int light_steps, int levels_per_graph, int block_threads = -1, int bu_share = -1);
+    int block_threads() const { return block_; }
+    int bu_share() const { return bu_share_; }
     // One batch of rq.kb <= lanes sources (forward, then backward for BC).
     gbc_status run(const LaneRequest& rq, LaneResult& res);
     // BC accumulation across batches: zero the per-group partials / reduce them into d_bc[n].
@@ -144,6 +150,8 @@ private:
     int sparse_ = 2;
     int light_ = 16;
     int lpg_ = 16;
+    int block_ = 256;     // threads per CTA of the level kernels
+    int bu_share_ = 16;   // direction-switch threshold of closeness levels (0: top-down only)
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
     int hub_lim_ = -1;    // ids below this are the hubs (ids in descending degree order), -1: unknown
     size_t lvl_sz_ = 0, vmark_sz_ = 0, sig_sz_ = 0, rho_sz_ = 0, bcg_sz_ = 0;   // bytes of the cached buffers

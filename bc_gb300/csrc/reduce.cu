@@ -432,7 +432,7 @@ static gbc_status block_engine(Reduction& R, const gbc_options& o, bool bc, Lane
         GBC_TRY(e->init(R.dg.get(), lanes, bc, o.sparse_lanes, o.levels_per_graph, R.stream, group));
         R.eng = std::move(e);
     }
-    R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph);
+    R.eng->set_tuning(o.sparse_lanes, o.light_steps, o.levels_per_graph, o.block_threads, o.bu_share > 0 ? o.bu_share : -1);
     *out = R.eng.get();
     return GBC_OK;
 }

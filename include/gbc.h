@@ -81,7 +81,12 @@ typedef struct {
                                  thread; lanes must then be a multiple of 128); 0 = automatic */
     int32_t direction;        /* closeness with 128-lane groups: 0 = switch between top-down and
                                  bottom-up levels by frontier size (default); 1 = top-down only */
-    int32_t reserved[5];
+    int32_t block_threads;    /* threads per CTA of the level kernels: 128, 256 or 512; 0 = the
+                                 autotuned value, else 256 */
+    int32_t bu_share;         /* closeness with 128-lane groups: a level goes bottom-up once the
+                                 frontier is past its peak while its edges x bu_share exceed all
+                                 edges x lane groups; 0 = the autotuned value, else 16 */
+    int32_t reserved[3];
 } gbc_options;
 
 typedef struct {
@@ -161,11 +166,14 @@ gbc_status gbc_bc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const
                          double* d_bc, void* stream);
 
 /* Autotuner: time one betweenness batch of the given sources (k = 0: all
- * vertices) per candidate expansion setting -- one-thread task threshold
- * (light_steps 0/8/16/32), edge-parallel threshold (sparse_lanes 1/2/4), level
- * kernels per captured graph (16/64, deep graphs) and batch width (halved from the
- * widest while the time per source drops, down to 32 lanes), one at a time -- and
- * keep the fastest on the graph.  Later calls whose
+ * vertices) per candidate expansion setting -- lane-group width (32/128),
+ * one-thread task threshold (light_steps 0/8/16/32), edge-parallel threshold
+ * (sparse_lanes 1/2/4), level kernels per captured graph (16/64, deep graphs),
+ * threads per CTA of the level kernels (block_threads 128/256/512) and batch
+ * width (halved from the widest while the time per source drops, down to 32
+ * lanes), one at a time -- and keep the fastest on the graph.  On 128-lane
+ * groups it then times one closeness batch per direction-switch share
+ * (bu_share 4/8/16/32/64, or top-down only).  Later calls whose
  * options leave a setting to autotuning (-1 / 0) use the tuned value; values
  * set in the options are not tuned.  *chosen (nullable) receives the options
  * with the chosen settings filled in.  Results do not depend on the settings

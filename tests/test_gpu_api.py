@@ -429,7 +429,29 @@ def test_autotune_choices_and_results(gpu, orc):
         assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
         ch2 = G.autotune(src)
         assert ch2["light_steps"] in (0, 8, 16, 32)
+        assert ch2["block_threads"] in (128, 256, 512)
         assert np.array_equal(G.cc(src), orc.cc(og, src))
+        ch3 = G.autotune(src, block_threads=512)
+        assert ch3["block_threads"] == 512
+        assert np.max(np.abs(G.bc(src) - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
+
+
+def test_autotune_direction_share(gpu, orc):
+    """On a small-world graph the autotuner also picks the closeness
+    direction-switch share (or top-down only); closeness under the choice
+    equals the oracle.  Out-of-range shapes and shares are refused."""
+    csr = gpu.gen_rmat(14, 16, seed=3)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.nonzero(np.diff(csr.row) > 0)[0][:512].astype(np.int32)
+    with gpu.Graph(csr) as G:
+        ch = G.autotune(src)
+        assert ch["group_lanes"] == 128
+        assert ch["bu_share"] in (0, 4, 8, 16, 32, 64)
+        assert (ch["direction"] == 1) == (ch["bu_share"] == 0)
+        assert np.array_equal(G.cc(src), orc.cc(og, src, nthreads=8))
+        for bad in (dict(block_threads=384), dict(bu_share=-1), dict(bu_share=5000)):
+            with pytest.raises(gpu.GbcError):
+                G.cc(src, **bad)
 
 
 def _canonical_csr(u, v, n):

@@ -105,6 +105,27 @@ def test_cc_direction_switching(gpu, orc, graphs, name):
         assert st["bottom_up_levels"] > 0
 
 
+@pytest.mark.parametrize("name", ["rmat14", "grid24", "star+grid", "er2k"])
+@pytest.mark.parametrize("threads", [128, 512])
+def test_cta_shapes(gpu, orc, graphs, name, threads):
+    """The level kernels of every CTA shape (128 / 512 threads against the
+    default 256) give the oracle's betweenness and closeness, on 32- and
+    128-lane groups, and closeness is the same for every direction-switch
+    share (bu_share) and for top-down only."""
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = sources_of(csr, 300)
+    ref, _ = orc.bc(og, src, scaled=(name == "grid24"), nthreads=8)
+    ref_cc = orc.cc(og, src, nthreads=8)
+    with gpu.Graph(csr) as G:
+        for group in (32, 128):
+            got = G.bc(src, lanes=256, group_lanes=group, block_threads=threads)
+            assert relerr(got, ref) < TOL_F64, (group, threads)
+            assert np.array_equal(G.cc(src, lanes=256, group_lanes=group, block_threads=threads), ref_cc)
+        for share in (1, 4, 64, 4096):
+            assert np.array_equal(G.cc(src, lanes=256, group_lanes=128, block_threads=threads, bu_share=share), ref_cc)
+
+
 @pytest.mark.parametrize("name", ["ba4096", "rmat12", "er2k", "karate", "rmat14", "star+grid"])
 @pytest.mark.parametrize("sem", [0, 1])
 def test_bc_fp64(gpu, orc, graphs, name, sem):
