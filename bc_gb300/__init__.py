@@ -130,6 +130,8 @@ _PROTOS = [
     ("gbc_server_add_graph", _st, [_vp, _i64p, _i32p, C.c_int32, C.POINTER(C.c_int32)]),
     ("gbc_server_submit", _st, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(Options), C.c_double,
                                 C.POINTER(C.c_int64)]),
+    ("gbc_graph_last_levels", _st, [_vp, _vp, C.c_int32, _vp, _vp, C.c_int32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     ("gbc_server_request_bytes", _st, [_vp, C.c_int32, C.c_int32, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     ("gbc_server_poll", _st, [_vp, C.c_int64, C.POINTER(C.c_int32)]),
     ("gbc_server_wait", _st, [_vp, C.c_int64, C.c_double, C.POINTER(C.c_int32)]),
@@ -359,6 +361,18 @@ class Graph:
         st = RunStats()
         check(lib().gbc_graph_last_stats(self.h, C.byref(st)))
         return st.as_dict()
+
+    def levels(self) -> dict:
+        """Level profile of the last lane batch: frontier entries per BFS
+        level and device ms per forward / sweep graph launch."""
+        nl, nf, nb = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib().gbc_graph_last_levels(self.h, None, 0, None, None, 0, C.byref(nl), C.byref(nf), C.byref(nb)))
+        ent = np.zeros(max(nl.value, 1), np.int64)
+        cap = max(nf.value, nb.value, 1)
+        fw, bw = np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+        check(lib().gbc_graph_last_levels(self.h, ent.ctypes.data_as(C.c_void_p), nl.value, fw.ctypes.data_as(C.c_void_p),
+                                          bw.ctypes.data_as(C.c_void_p), cap, C.byref(nl), C.byref(nf), C.byref(nb)))
+        return {"entries": ent[: nl.value], "fwd_ms": fw[: nf.value], "bwd_ms": bw[: nb.value]}
 
 
 class Reduced:

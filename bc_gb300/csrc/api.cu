@@ -33,6 +33,9 @@ struct gbc_graph_s {
     // internal ids are by descending degree: order[new] = old, inv[old] = new
     int32_t* d_order = nullptr;
     int32_t* d_inv = nullptr;
+    // per-level profile of the last batch of the last call (gbc_graph_last_levels)
+    std::vector<int64_t> last_level_entries;
+    std::vector<float> last_fwd_launch_ms, last_bwd_launch_ms;
     std::vector<int32_t> h_inv;
     double* d_bc_out = nullptr;   // BC in the caller's ids (gbc_bc)
     // vertex weights set by gbc_graph_set_weights, in internal ids (nullable)
@@ -425,6 +428,9 @@ static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t
     s.group_lanes = lanes == 1 ? 1 : (G->eng ? G->eng->group_lanes() : 32);
     s.bottom_up_levels = (int32_t)r.bottom_up_levels;
     G->last_src = hsrc;
+    G->last_level_entries = r.level_entries;
+    G->last_fwd_launch_ms = r.fwd_launch_ms;
+    G->last_bwd_launch_ms = r.bwd_launch_ms;
 }
 
 // Betweenness over device-staged sources d_src[0..k) into d_bc[n].
@@ -714,6 +720,22 @@ gbc_status gbc_graph_info(gbc_graph G, int32_t* n, int64_t* m, size_t* bytes) {
     if (n) *n = G->g.n;
     if (m) *m = G->g.m;
     if (bytes) *bytes = sizeof(int64_t) * (G->g.n + 1) + sizeof(int32_t) * G->g.m + (G->eng ? G->eng->device_bytes() : 0);
+    return GBC_OK;
+}
+
+gbc_status gbc_graph_last_levels(gbc_graph G, int64_t* entries, int32_t entries_cap, float* fwd_ms, float* bwd_ms,
+                                 int32_t launch_cap, int32_t* levels, int32_t* fwd_launches, int32_t* bwd_launches) {
+    if (!G) { set_error("graph is NULL"); return GBC_ERR_ARG; }
+    if (entries_cap < 0 || launch_cap < 0) { set_error("negative capacity"); return GBC_ERR_ARG; }
+    std::lock_guard<std::mutex> lk(G->mu);
+    const int32_t nl = (int32_t)G->last_level_entries.size();
+    const int32_t nf = (int32_t)G->last_fwd_launch_ms.size(), nb = (int32_t)G->last_bwd_launch_ms.size();
+    if (levels) *levels = nl;
+    if (fwd_launches) *fwd_launches = nf;
+    if (bwd_launches) *bwd_launches = nb;
+    if (entries) std::memcpy(entries, G->last_level_entries.data(), sizeof(int64_t) * std::min(nl, entries_cap));
+    if (fwd_ms) std::memcpy(fwd_ms, G->last_fwd_launch_ms.data(), sizeof(float) * std::min(nf, launch_cap));
+    if (bwd_ms) std::memcpy(bwd_ms, G->last_bwd_launch_ms.data(), sizeof(float) * std::min(nb, launch_cap));
     return GBC_OK;
 }
 

@@ -97,6 +97,11 @@ struct LaneResult {
     double fwd_ms = 0, bwd_ms = 0;      // device time inside the level-loop graphs
     int64_t fwd_kernels = 0, bwd_kernels = 0;
     int64_t bottom_up_levels = 0;       // closeness levels discovered bottom-up
+    // last batch only: frontier entries per BFS level (regular + hub queue) and
+    // device time per forward / dependency-sweep graph launch (levels_per_graph
+    // levels each)
+    std::vector<int64_t> level_entries;
+    std::vector<float> fwd_launch_ms, bwd_launch_ms;
 };
 
 class LaneEngine {

@@ -130,6 +130,7 @@ struct Lv {
 constexpr int HUB_DEG = 1024;   // 32-lane groups: entries of higher-degree vertices are expanded by a whole CTA
 constexpr int HUB_DEG_Q = 1024; // the same for 128-lane groups
 constexpr int FETCH = 32;       // regular entries a warp takes per fetch, one per thread
+constexpr int LIGHT_U = 4;      // one-thread tasks: neighbours whose loads are issued together
 constexpr int STG = 128;        // regular-queue entries a warp stages in shared memory per append
 // Minimum resident CTAs per SM of the forward kernels.  Deep graphs (16-bit
 // levels) have small, latency-bound levels and need 4 (64 registers); so do
@@ -139,7 +140,8 @@ constexpr int STG = 128;        // regular-queue entries a warp stages in shared
 // forcing 4 or 5 (48 registers); unbounded (113+ registers, 2 CTAs) is 35%
 // slower.  The dependency sweep is always compiled for 4 (its compensated
 // sums would otherwise take 80 registers, 5% slower on R-MAT scale 22).
-template <typename LT, bool WIDE, int NT> constexpr int MINB = (sizeof(LT) == 2 || WIDE) ? 4 * 256 / NT : 0;
+// Other CTA shapes are held to the same 64 registers (1024 / NT CTAs per SM).
+template <typename LT, bool WIDE, int NT> constexpr int MINB = (sizeof(LT) == 2 || WIDE || NT != 256) ? 1024 / NT : 0;
 
 __device__ __forceinline__ size_t sidx(int g, int n, int v, int t, int gs) {
     return ((((size_t)g * (size_t)n) + (size_t)v) << gs) + (size_t)t;
@@ -739,6 +741,7 @@ template <int MODE, typename LT>
 __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint32_t ent, unsigned am, long long r0,
                                           long long r1, unsigned long long* cc_sh) {
     constexpr LT INF = (LT)Lv<LT>::INF;
+    constexpr int U = LIGHT_U;
     const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const int v = (int)(ent >> 5), g = (int)(ent & 31u);
     const size_t gbase = (size_t)g * (size_t)A.n;
@@ -747,7 +750,8 @@ __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint3
         const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
         for (unsigned r = am; r; r &= r - 1u) atomicAdd(&cc_sh[g * 32 + __ffs(r) - 1], (unsigned long long)c);
     }
-    const int steps = __popc(am) * (int)(r1 - r0);
+    // one step = up to U neighbours of one active lane, their loads issued together
+    const int steps = __popc(am) * (int)((r1 - r0 + U - 1) / U);
     const int maxs = __reduce_max_sync(FULL, steps);
     unsigned rem = am;
     int a = 0;
@@ -757,39 +761,54 @@ __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint3
     int we = WEMPTY;
     double ws = 0.0;
     for (int it = 0; it < maxs; it++) {
-        bool has = false, hub = false;
-        int x = 0;
-        if (it < steps) {
-            if (j == r1) {
-                a = __ffs(rem) - 1;
-                rem &= rem - 1u;
-                j = r0;
-                acc = 0;
-                of = false;
-                we = WEMPTY;
-                ws = 0.0;
-            }
-            x = A.col[j];
-            LT* px = lv + ((size_t)x << 5) + a;
-            const LT Lx = *px;
-            if (MODE != 0 && d > 0 && Lx == dprev) {
-                const uint64_t sv = A.sig[((gbase + (size_t)x) << 5) + a];
+        const bool on = it < steps;
+        if (on && j == r1) {
+            a = __ffs(rem) - 1;
+            rem &= rem - 1u;
+            j = r0;
+            acc = 0;
+            of = false;
+            we = WEMPTY;
+            ws = 0.0;
+        }
+        int x[U];
+        LT L[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) x[u] = (on && j + u < r1) ? A.col[j + u] : -1;
+#pragma unroll
+        for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[((size_t)x[u] << 5) + a] : dl;   // dl: neither case below
+        if (MODE != 0 && d > 0) {
+            uint64_t sv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) sv[u] = L[u] == dprev ? A.sig[((gbase + (size_t)x[u]) << 5) + a] : 0ULL;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (L[u] != dprev) continue;
                 if (MODE == 1) {
-                    const uint64_t na = acc + sv;
+                    const uint64_t na = acc + sv[u];
                     of |= (na < acc);
                     acc = na;
                 } else {
-                    wadd(ws, we, sv);
+                    wadd(ws, we, sv[u]);
                 }
             }
-            if (Lx == INF) {
-                *px = dnext;
-                has = claim(A, gbase, x, d + 1);
-                hub = has && is_hub(A, x);
-            }
-            if (++j == r1 && MODE != 0 && d > 0) fwd_store<MODE>(A, g, gbase, v, a, acc, of, we, ws);
         }
-        warp_append(A, S, has, hub, ((uint32_t)x << 5) | (uint32_t)g);
+        // discovery: level stores, then every first-claim check, then the atomics
+        int32_t mk[U];
+        bool has[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (L[u] == INF) lv[((size_t)x[u] << 5) + a] = dnext;
+#pragma unroll
+        for (int u = 0; u < U; u++) mk[u] = L[u] == INF ? *(volatile int32_t*)&A.vmark[gbase + x[u]] : d + 1;
+#pragma unroll
+        for (int u = 0; u < U; u++) has[u] = mk[u] != d + 1 && atomicExch(&A.vmark[gbase + x[u]], d + 1) != d + 1;
+        if (on) {
+            j = min(j + U, r1);
+            if (j == r1 && MODE != 0 && d > 0) fwd_store<MODE>(A, g, gbase, v, a, acc, of, we, ws);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) warp_append(A, S, has[u], has[u] && is_hub(A, x[u]), ((uint32_t)x[u] << 5) | (uint32_t)g);
     }
 }
 
@@ -988,7 +1007,8 @@ template <bool WIDE, typename T, typename LT>
 __device__ __forceinline__ void bwd_light(const KArgs& A, int d, uint32_t ent, unsigned am, long long r0, long long r1,
                                           bool refsem) {
     if (!am) return;
-    const LT dprev = (LT)(d - 1), dnext = (LT)(d + 1);
+    constexpr int U = LIGHT_U;
+    const LT dl = (LT)d, dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const int v = (int)(ent >> 5), g = (int)(ent & 31u);
     const size_t gbase = (size_t)g * (size_t)A.n;
     const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 5);
@@ -1006,14 +1026,33 @@ __device__ __forceinline__ void bwd_light(const KArgs& A, int d, uint32_t ent, u
         }
         Sum<T> acc;
         int pc = 0;
-        for (long long j = r0; j < r1; j++) {
-            const int x = A.col[j];
-            const LT Lx = lv[((size_t)x << 5) + a];
-            if (Lx == dnext) {
-                const size_t xi = ((gbase + (size_t)x) << 5) + a;
-                acc.add(WIDE ? wterm<T>(mv, ev, rw[xi]) : rho[xi]);
-            } else if (Lx == dprev) {
-                pc++;
+        // U neighbours per step: their column, level and rho loads issued together
+        for (long long j = r0; j < r1; j += U) {
+            int x[U];
+            LT L[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) x[u] = j + u < r1 ? A.col[j + u] : -1;
+#pragma unroll
+            for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[((size_t)x[u] << 5) + a] : dl;
+            uint64_t rv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const size_t xi = ((gbase + (size_t)x[u]) << 5) + a;
+                rv[u] = 0;
+                if (L[u] == dnext) {
+                    if (WIDE || sizeof(T) == 8) rv[u] = rw[xi];
+                    else rv[u] = __float_as_uint(reinterpret_cast<const float*>(rho)[xi]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (L[u] == dnext) {
+                    if (WIDE) acc.add(wterm<T>(mv, ev, rv[u]));
+                    else if (sizeof(T) == 8) acc.add((T)__longlong_as_double((long long)rv[u]));
+                    else acc.add((T)__uint_as_float((unsigned)rv[u]));
+                } else if (L[u] == dprev) {
+                    pc++;
+                }
             }
         }
         contrib += bwd_lane<WIDE, T>(A, g, gbase, v, a, mv, ev, acc.value(), pc, refsem);

@@ -451,6 +451,9 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
     }
     // retries: a queue overflow (grown up to its bound, below), a level-width switch, a sigma re-run
     for (int attempt = 0; attempt < 8; attempt++) {
+        res.level_entries.clear();
+        res.fwd_launch_ms.clear();
+        res.bwd_launch_ms.clear();
         KArgs A = LaneAccess::args(*this, rq.semantics);
         GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
         if (mode == 0) GBC_CUDA(cudaMemsetAsync(ccbuf_, 0, lanes_ * sizeof(unsigned long long), stream_));
@@ -478,6 +481,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             float ms = 0;
             cudaEventElapsedTime(&ms, ev_[0], ev_[1]);
             res.fwd_ms += ms;
+            res.fwd_launch_ms.push_back(ms);
             if (h->done) break;
             if (h->any_ovf && rq.abort_on_overflow) break;   // the batch is redone in wide form anyway
             if (launched > (int64_t)MAX_LEVEL + 2 * lpg_) { set_error("forward level loop did not terminate"); return GBC_ERR_LIMIT; }
@@ -517,6 +521,16 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         }
         res.levels += maxlevel + 1;
         res.bottom_up_levels += h->bu_levels;
+        {
+            // frontier entries of every level of this batch: foff / hoff hold the level bounds
+            std::vector<unsigned long long> fo(maxlevel + 2), ho(maxlevel + 2);
+            GBC_CUDA(cudaMemcpyAsync(fo.data(), foff_, sizeof(unsigned long long) * (maxlevel + 2), cudaMemcpyDeviceToHost, stream_));
+            GBC_CUDA(cudaMemcpyAsync(ho.data(), hoff_, sizeof(unsigned long long) * (maxlevel + 2), cudaMemcpyDeviceToHost, stream_));
+            GBC_CUDA(cudaStreamSynchronize(stream_));
+            res.level_entries.resize(maxlevel + 1);
+            for (int dl = 0; dl <= maxlevel; dl++)
+                res.level_entries[dl] = (int64_t)(fo[dl + 1] - fo[dl]) + (int64_t)(ho[dl + 1] - ho[dl]);
+        }
         res.frontier_entries += (int64_t)(entries + hentries);
         if (rq.d_profile_key) {
             profile_key_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, lvl_bytes_, rq.d_profile_key);
@@ -576,6 +590,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
                 float ms = 0;
                 cudaEventElapsedTime(&ms, ev_[2 * i], ev_[2 * i + 1]);
                 res.bwd_ms += ms;
+                res.bwd_launch_ms.push_back(ms);
             }
         }
         if (mode == 0 && rq.d_cc) {

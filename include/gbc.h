@@ -156,6 +156,14 @@ gbc_status gbc_graph_export(gbc_graph g, int64_t** row, int32_t** col, int32_t* 
 gbc_status gbc_graph_info(gbc_graph g, int32_t* n, int64_t* m_directed, size_t* device_bytes);
 /* Statistics of the last compute call on this graph. */
 gbc_status gbc_graph_last_stats(gbc_graph g, gbc_run_stats* st);
+/* Level profile of the last lane batch of the last compute call on this
+ * graph: *levels = BFS levels, entries[d] (up to entries_cap) = frontier
+ * (vertex, lane-group) entries of level d; fwd_ms / bwd_ms (up to launch_cap)
+ * = device time of each forward / dependency-sweep graph launch, which runs
+ * levels_per_graph level kernels (set levels_per_graph = 1 for per-level
+ * times).  Output arrays may be NULL. */
+gbc_status gbc_graph_last_levels(gbc_graph g, int64_t* entries, int32_t entries_cap, float* fwd_ms, float* bwd_ms,
+                                 int32_t launch_cap, int32_t* levels, int32_t* fwd_launches, int32_t* bwd_launches);
 
 /* ---- betweenness --------------------------------------------------------
  * bc[n] (host) receives sum over the k sources of the per-source

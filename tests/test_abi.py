@@ -51,6 +51,10 @@ def test_argument_validation_before_device(gbc):
     dec = np.array([0, 2, 1], np.int64)       # decreasing offsets
     assert L.gbc_graph_create(dec, np.array([1, 0], np.int32), 2, C.byref(h)) == 1
     assert L.gbc_bc(None, None, 0, None, np.zeros(1)) == 1
+    n = C.c_int32()
+    assert L.gbc_graph_last_levels(None, None, 0, None, None, 0, C.byref(n), None, None) == 1
+    sz = C.c_size_t()
+    assert L.gbc_server_request_bytes(None, 0, 0, C.byref(sz), C.byref(sz)) == 1
     if gbc.device_count() == 0:
         ok = np.array([1, 0], np.int32)
         assert L.gbc_graph_create(row, ok, 2, C.byref(h)) == 9   # GBC_ERR_NO_DEVICE

@@ -436,6 +436,27 @@ def test_autotune_choices_and_results(gpu, orc):
         assert np.max(np.abs(G.bc(src) - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-9
 
 
+def test_level_profile(gpu, orc):
+    """gbc_graph_last_levels: the last batch's frontier entries per level add
+    up to the run's frontier entries, the level count matches the oracle's
+    deepest distance, and with one level kernel per graph there is one forward
+    launch per level (plus the tail launch that finds the frontier empty) and
+    one sweep launch per level below the deepest."""
+    csr = gpu.gen_grid(20, 20, 0.05, seed=6)      # path counts stay exact (no wide re-run)
+    src = np.arange(0, csr.n, 11, dtype=np.int32)[:32]
+    with gpu.Graph(csr) as G:
+        G.bc(src, lanes=32, levels_per_graph=1, sigma_mode=gpu.SIGMA_EXACT)
+        st = G.stats()
+        lv = G.levels()
+    og = orc.Graph(csr.row, csr.col)
+    depth = max(int(orc.sssp(og, s)[0].max()) for s in src) + 1
+    assert len(lv["entries"]) == depth == st["levels"]
+    assert int(lv["entries"].sum()) == st["frontier_entries"]
+    assert lv["entries"][0] == 32 and np.all(lv["entries"] > 0)
+    assert depth <= len(lv["fwd_ms"]) <= depth + 1 and len(lv["bwd_ms"]) == depth - 1
+    assert np.all(lv["fwd_ms"] > 0) and np.all(lv["bwd_ms"] > 0)
+
+
 def test_autotune_direction_share(gpu, orc):
     """On a small-world graph the autotuner also picks the closeness
     direction-switch share (or top-down only); closeness under the choice
