@@ -427,6 +427,7 @@ static void finish_stats(gbc_graph_s* G, const LaneResult& r, int64_t k, int64_t
     s.edges_traversed = -1;   // filled in lazily by gbc_graph_last_stats
     s.group_lanes = lanes == 1 ? 1 : (G->eng ? G->eng->group_lanes() : 32);
     s.bottom_up_levels = (int32_t)r.bottom_up_levels;
+    s.sigma_bytes = r.sigma_bytes;
     G->last_src = hsrc;
     G->last_level_entries = r.level_entries;
     G->last_fwd_launch_ms = r.fwd_launch_ms;

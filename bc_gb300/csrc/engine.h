@@ -66,6 +66,9 @@ struct DevGraph {
     // Level width new lane engines on this graph start with: 2 once some BFS on
     // it went deeper than 8-bit levels allow, so later engines skip that pass.
     mutable int level_bytes_hint = 1;
+    // Bytes per exact path count that 128-lane engines on this graph start with:
+    // 2, widened to 4 and then 8 once a batch's counts did not fit.
+    mutable int sigma_bytes_hint = 2;
 };
 
 // Which computation a lane batch performs.
@@ -97,6 +100,7 @@ struct LaneResult {
     double fwd_ms = 0, bwd_ms = 0;      // device time inside the level-loop graphs
     int64_t fwd_kernels = 0, bwd_kernels = 0;
     int64_t bottom_up_levels = 0;       // closeness levels discovered bottom-up
+    int32_t sigma_bytes = 8;            // bytes per exact path count of the last batch
     // last batch only: frontier entries per BFS level (regular + hub queue) and
     // device time per forward / dependency-sweep graph launch (levels_per_graph
     // levels each)
@@ -158,6 +162,8 @@ private:
     int block_ = 256;     // threads per CTA of the level kernels
     int bu_share_ = 16;   // direction-switch threshold of closeness levels (0: top-down only)
     int lvl_bytes_ = 1;   // 1 while every BFS stays under 254 levels, else 2
+    int sig_bytes_ = 8;   // bytes per exact path count (128-lane groups: 2 or 4 while the counts fit)
+    int width_index() const;
     int hub_lim_ = -1;    // ids below this are the hubs (ids in descending degree order), -1: unknown
     size_t lvl_sz_ = 0, vmark_sz_ = 0, sig_sz_ = 0, rho_sz_ = 0, bcg_sz_ = 0;   // bytes of the cached buffers
     cudaStream_t stream_ = nullptr;

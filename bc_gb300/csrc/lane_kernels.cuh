@@ -97,14 +97,16 @@ struct KArgs {
     // closeness direction switching: bottom-up once past the frontier peak while
     // frontier edges x bu_share exceed mtot (0: never)
     unsigned long long bu_share;
+    // bytes per exact path count (128-lane groups: 2 or 4 while every count fits, else 8)
+    int sig_bytes;
 };
 
 // Entry points of the level kernels of one CTA shape.
 struct LevelKernels {
     void (*expand[2][3])(KArgs);       // 32-lane groups: [16-bit levels][MODE]
     void (*backward[2][4])(KArgs);     // [16-bit levels][wide sigma * 2 + FP64 delta]
-    void (*expand_q[2][3])(KArgs);     // 128-lane groups
-    void (*backward_q[2][4])(KArgs);
+    void (*expand_q[2][3][3])(KArgs);    // 128-lane groups: [16-bit levels][MODE][path-count width 8/4/2 bytes]
+    void (*backward_q[2][4][3])(KArgs);  // [16-bit levels][wide sigma * 2 + FP64 delta][width]
 };
 void level_kernels_128(LevelKernels& k);   // lanes_nt128.cu
 void level_kernels_256(LevelKernels& k);   // lanes_nt256.cu
@@ -345,6 +347,7 @@ __device__ __forceinline__ void fwd_last_block(const KArgs& A, int d, int done, 
                     A.ctl->next = A.foff[d + 1];
                     A.ctl->hnext = A.hoff[d + 1];
                     if (tail == A.foff[d + 1] && htail == A.hoff[d + 1]) { A.ctl->done = 1; A.ctl->maxlevel = d; }
+                    else if (A.sig_bytes < 8 && *(volatile int*)&A.ctl->any_ovf) { A.ctl->done = 1; A.ctl->maxlevel = d; }
                     else if (d + 1 >= maxd) { A.ctl->err |= 2; A.ctl->done = 1; A.ctl->maxlevel = d; }
                     else A.ctl->level = d + 1;
                     if (dir && !A.ctl->td_only) {
@@ -1193,6 +1196,14 @@ template <> struct Quad<uint16_t> {
     }
 };
 
+// Exact path counts of 128-lane groups are stored in SB bytes per lane (8,
+// or 4 / 2 while every count of the graph fits, which keeps the predecessor
+// reads of the forward at 512 / 256 instead of 1024 bytes per neighbour row).
+template <int SB> struct SigW;
+template <> struct SigW<8> { using type = uint64_t; static constexpr uint64_t MAXV = ~0ULL; };
+template <> struct SigW<4> { using type = uint32_t; static constexpr uint64_t MAXV = 0xFFFFFFFFULL; };
+template <> struct SigW<2> { using type = uint16_t; static constexpr uint64_t MAXV = 0xFFFFULL; };
+
 constexpr int Q_ITER = 8;   // neighbours whose level quads are loaded before any is used
 constexpr int FETCH_Q = 8;  // regular tasks a warp takes per fetch in 128-lane groups (8: 3% faster than 32 on R-MAT s22)
 constexpr unsigned long long TAIL_Q = 16384;   // fewer regular tasks left than this: take one per fetch
@@ -1215,7 +1226,7 @@ __device__ __forceinline__ unsigned long long q_fetch(const KArgs& A, unsigned l
 // Forward scan of one (v, g) task over neighbour chunks r0 + 32*sub, step
 // 32*nsub: thread t pulls sigma for its active lanes (act4) and discovers
 // level d+1.  Results stay in the thread: acc/ofm (exact) or ws/we (wide).
-template <int MODE, typename LT>
+template <int MODE, typename LT, int SB>
 __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, unsigned act4,
                                            long long r0, long long r1, int sub, int nsub, uint64_t (&acc)[4],
                                            unsigned& ofm, int (&we)[4], double (&ws)[4]) {
@@ -1236,6 +1247,23 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                 for (int i = 0; i < Q_ITER; i++) {
                     const unsigned pm = (k0 + i < cnt) ? (q[i].eq(d - 1) & act4) : 0u;
                     if (!pm) continue;
+                    if (MODE == 1 && SB < 8) {
+                        // narrow counts: the four lanes in one 8- or 16-byte load; no carry in a 64-bit sum
+                        const typename SigW<SB>::type* sn =
+                            reinterpret_cast<const typename SigW<SB>::type*>(A.sig) + ((gbase + (size_t)xs[i]) << 7) + 4 * t;
+                        unsigned w4[4];
+                        if (SB == 4) {
+                            const uint4 w = *reinterpret_cast<const uint4*>(sn);
+                            w4[0] = w.x; w4[1] = w.y; w4[2] = w.z; w4[3] = w.w;
+                        } else {
+                            const uint2 w = *reinterpret_cast<const uint2*>(sn);
+                            w4[0] = w.x & 0xFFFFu; w4[1] = w.x >> 16; w4[2] = w.y & 0xFFFFu; w4[3] = w.y >> 16;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++)
+                            if ((pm >> j) & 1u) acc[j] += w4[j];
+                        continue;
+                    }
                     const uint64_t* sg = A.sig + ((gbase + (size_t)xs[i]) << 7) + 4 * t;
 #pragma unroll
                     for (int pr = 0; pr < 2; pr++) {
@@ -1280,17 +1308,19 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
 }
 
 // Store sigma of thread t's active lanes of (v, g); flag lanes past the range.
-template <int MODE>
+template <int MODE, int SB>
 __device__ __forceinline__ void q_fwd_store(const KArgs& A, int g, size_t gbase, int v, unsigned act4,
                                             const uint64_t (&acc)[4], unsigned ofm, const int (&we)[4],
                                             const double (&ws)[4]) {
     const int t = threadIdx.x & 31;
-    uint64_t* sv = A.sig + ((gbase + (size_t)v) << 7) + 4 * t;
+    typedef typename SigW<(MODE == 1 ? SB : 8)>::type ST;
+    ST* sv = reinterpret_cast<ST*>(A.sig) + ((gbase + (size_t)v) << 7) + 4 * t;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (!((act4 >> j) & 1u)) continue;
         bool of = (ofm >> j) & 1u;
-        sv[j] = MODE == 2 ? wpack(ws[j], we[j], of) : acc[j];
+        if (MODE == 1 && SB < 8) of = of || acc[j] > SigW<(MODE == 1 ? SB : 8)>::MAXV;   // the batch is redone wider
+        sv[j] = MODE == 2 ? (ST)wpack(ws[j], we[j], of) : (ST)acc[j];
         if (of) {
             const int lane = (g << 7) + 4 * t + j;
             atomicOr(&A.ovf[lane >> 5], 1u << (lane & 31));
@@ -1301,7 +1331,7 @@ __device__ __forceinline__ void q_fwd_store(const KArgs& A, int g, size_t gbase,
 
 // Edge-parallel forward for tasks with few active lanes: threads over
 // neighbours, one active lane at a time; the lane's owner keeps the sum.
-template <int MODE, typename LT>
+template <int MODE, typename LT, int SB>
 __device__ __forceinline__ void q_fwd_edges(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, unsigned act4,
                                             long long r0, long long r1, int sub, int nsub, uint64_t (&acc)[4],
                                             unsigned& ofm, int (&we)[4], double (&ws)[4]) {
@@ -1328,7 +1358,9 @@ __device__ __forceinline__ void q_fwd_edges(const KArgs& A, Stage& S, int d, int
                     LT* px = lv + ((size_t)x << 7) + a;
                     const LT Lx = *px;
                     if (MODE != 0 && d > 0 && Lx == dprev) {
-                        const uint64_t sv = A.sig[((gbase + (size_t)x) << 7) + a];
+                        const uint64_t sv = (MODE == 1 && SB < 8)
+                            ? (uint64_t)reinterpret_cast<const typename SigW<(MODE == 1 ? SB : 8)>::type*>(A.sig)[((gbase + (size_t)x) << 7) + a]
+                            : A.sig[((gbase + (size_t)x) << 7) + a];
                         if (MODE == 1) {
                             const uint64_t na = pacc + sv;
                             pof |= (na < pacc);
@@ -1505,7 +1537,7 @@ __device__ __forceinline__ void q_bottom_up(const KArgs& A, Stage& S, unsigned l
 }
 
 // Forward level kernel, 128-lane groups.
-template <int MODE, typename LT, int NT>
+template <int MODE, typename LT, int NT, int SB>
 __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
     constexpr int WARPS = NT / 32;
     __shared__ unsigned long long cc_sh[MODE == 0 ? 1024 : 1];
@@ -1547,8 +1579,8 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
             unsigned ofm = 0;
             int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
             double ws[4] = {0.0, 0.0, 0.0, 0.0};
-            if (nact > A.sparse) q_fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
-            else q_fwd_edges<MODE, LT>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
+            if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
+            else q_fwd_edges<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
             if (MODE != 0) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -1572,7 +1604,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
                             }
                         }
                     }
-                    q_fwd_store<MODE>(A, g, gbase, v, act4, acc, ofm, we, ws);
+                    q_fwd_store<MODE, SB>(A, g, gbase, v, act4, acc, ofm, we, ws);
                 }
                 __syncthreads();
             }
@@ -1602,9 +1634,9 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
                 unsigned ofm = 0;
                 int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
                 double ws[4] = {0.0, 0.0, 0.0, 0.0};
-                if (nact > A.sparse) q_fwd_scan<MODE, LT>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
-                else q_fwd_edges<MODE, LT>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
-                if (MODE != 0 && d > 0) q_fwd_store<MODE>(A, g, gbase, v, act4, acc, ofm, we, ws);
+                if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
+                else q_fwd_edges<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
+                if (MODE != 0 && d > 0) q_fwd_store<MODE, SB>(A, g, gbase, v, act4, acc, ofm, we, ws);
             }
         }
     }
@@ -1734,7 +1766,7 @@ __device__ __forceinline__ void q_bwd_edges(const KArgs& A, int d, size_t gbase,
 
 // delta, rho and BC contributions of thread t's active lanes of (v, g),
 // warp-summed into bcg.
-template <bool WIDE, typename T>
+template <bool WIDE, typename T, int SB>
 __device__ __forceinline__ void q_bwd_finish(const KArgs& A, int g, size_t gbase, int v, unsigned act4, const T (&mv)[4],
                                              const int (&ev)[4], const Sum<T> (&acc)[4], const int (&pc)[4], bool refsem) {
     const int t = threadIdx.x & 31;
@@ -1750,7 +1782,7 @@ __device__ __forceinline__ void q_bwd_finish(const KArgs& A, int g, size_t gbase
             bool of = false;
             reinterpret_cast<uint64_t*>(A.rho)[vb + j] = wpack((T)((tw + delta) / mv[j]), -ev[j], of);
         } else {
-            const T sv = (T)A.sig[vb + j];
+            const T sv = (T)reinterpret_cast<const typename SigW<SB>::type*>(A.sig)[vb + j];
             delta = sv * acc[j].value();
             reinterpret_cast<T*>(A.rho)[vb + j] = (tw + delta) / sv;
         }
@@ -1774,7 +1806,7 @@ __device__ __forceinline__ void q_sigma_of(const KArgs& A, size_t gbase, int v, 
 }
 
 // Dependency-sweep level kernel, 128-lane groups.
-template <bool WIDE, typename T, typename LT, int NT>
+template <bool WIDE, typename T, typename LT, int NT, int SB>
 __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
     constexpr int WARPS = NT / 32;
     __shared__ T h_s[WARPS][128];
@@ -1821,7 +1853,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
                         pc[j] += h_pc[w][4 * t + j];
                     }
                 }
-                q_bwd_finish<WIDE, T>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
+                q_bwd_finish<WIDE, T, SB>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
             }
             __syncthreads();
         }
@@ -1851,7 +1883,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
                 int pc[4] = {0, 0, 0, 0};
                 if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
                 else q_bwd_edges<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
-                q_bwd_finish<WIDE, T>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
+                q_bwd_finish<WIDE, T, SB>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
             }
         }
     }
@@ -1872,6 +1904,29 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
 }
 
 
+// 128-lane entry points of one level width; path-count widths 4 and 2 bytes
+// exist for the exact forward and the non-wide sweeps only.
+template <typename LT, int NT>
+void fill_q(LevelKernels& K, int lv) {
+    for (int m = 0; m < 3; m++)
+        for (int w = 0; w < 3; w++) K.expand_q[lv][m][w] = nullptr;
+    K.expand_q[lv][0][0] = expand_q_kernel<0, LT, NT, 8>;
+    K.expand_q[lv][1][0] = expand_q_kernel<1, LT, NT, 8>;
+    K.expand_q[lv][1][1] = expand_q_kernel<1, LT, NT, 4>;
+    K.expand_q[lv][1][2] = expand_q_kernel<1, LT, NT, 2>;
+    K.expand_q[lv][2][0] = expand_q_kernel<2, LT, NT, 8>;
+    for (int v = 0; v < 4; v++)
+        for (int w = 0; w < 3; w++) K.backward_q[lv][v][w] = nullptr;
+    K.backward_q[lv][0][0] = backward_q_kernel<false, float, LT, NT, 8>;
+    K.backward_q[lv][0][1] = backward_q_kernel<false, float, LT, NT, 4>;
+    K.backward_q[lv][0][2] = backward_q_kernel<false, float, LT, NT, 2>;
+    K.backward_q[lv][1][0] = backward_q_kernel<false, double, LT, NT, 8>;
+    K.backward_q[lv][1][1] = backward_q_kernel<false, double, LT, NT, 4>;
+    K.backward_q[lv][1][2] = backward_q_kernel<false, double, LT, NT, 2>;
+    K.backward_q[lv][2][0] = backward_q_kernel<true, float, LT, NT, 8>;
+    K.backward_q[lv][3][0] = backward_q_kernel<true, double, LT, NT, 8>;
+}
+
 // Entry points of every level kernel for NT-thread CTAs.
 template <int NT>
 void fill_level_kernels(LevelKernels& K) {
@@ -1889,20 +1944,8 @@ void fill_level_kernels(LevelKernels& K) {
     K.backward[1][1] = backward_kernel<false, double, uint16_t, NT>;
     K.backward[1][2] = backward_kernel<true, float, uint16_t, NT>;
     K.backward[1][3] = backward_kernel<true, double, uint16_t, NT>;
-    K.expand_q[0][0] = expand_q_kernel<0, uint8_t, NT>;
-    K.expand_q[0][1] = expand_q_kernel<1, uint8_t, NT>;
-    K.expand_q[0][2] = expand_q_kernel<2, uint8_t, NT>;
-    K.expand_q[1][0] = expand_q_kernel<0, uint16_t, NT>;
-    K.expand_q[1][1] = expand_q_kernel<1, uint16_t, NT>;
-    K.expand_q[1][2] = expand_q_kernel<2, uint16_t, NT>;
-    K.backward_q[0][0] = backward_q_kernel<false, float, uint8_t, NT>;
-    K.backward_q[0][1] = backward_q_kernel<false, double, uint8_t, NT>;
-    K.backward_q[0][2] = backward_q_kernel<true, float, uint8_t, NT>;
-    K.backward_q[0][3] = backward_q_kernel<true, double, uint8_t, NT>;
-    K.backward_q[1][0] = backward_q_kernel<false, float, uint16_t, NT>;
-    K.backward_q[1][1] = backward_q_kernel<false, double, uint16_t, NT>;
-    K.backward_q[1][2] = backward_q_kernel<true, float, uint16_t, NT>;
-    K.backward_q[1][3] = backward_q_kernel<true, double, uint16_t, NT>;
+    fill_q<uint8_t, NT>(K, 0);
+    fill_q<uint16_t, NT>(K, 1);
 }
 
 }  // namespace

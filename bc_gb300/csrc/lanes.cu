@@ -27,8 +27,13 @@ __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, in
             const size_t i = sidx(g, A.n, s, t, A.gs);
             if (lvl_bytes == 1) reinterpret_cast<uint8_t*>(A.lvl)[i] = 0;
             else reinterpret_cast<uint16_t*>(A.lvl)[i] = 0;
-            if (mode == 1) A.sig[i] = 1ULL;
-            else if (mode == 2) A.sig[i] = WONE;
+            if (mode == 1) {
+                if (A.sig_bytes == 2) reinterpret_cast<uint16_t*>(A.sig)[i] = 1;
+                else if (A.sig_bytes == 4) reinterpret_cast<uint32_t*>(A.sig)[i] = 1u;
+                else A.sig[i] = 1ULL;
+            } else if (mode == 2) {
+                A.sig[i] = WONE;
+            }
             A.srcw[l] = A.w ? A.w[s] : 1;
             if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
                 const uint32_t ent = ((uint32_t)s << 5) | (uint32_t)g;
@@ -97,7 +102,11 @@ __global__ void sssp_out_kernel(KArgs A, int kb, int32_t* dist, uint64_t* sigma,
         if (lvl_bytes == 1) { L = reinterpret_cast<const uint8_t*>(A.lvl)[i]; unreached = (L == 0xFF); }
         else { L = reinterpret_cast<const uint16_t*>(A.lvl)[i]; unreached = (L == 0xFFFF); }
         if (dist) dist[k] = unreached ? -1 : L;
-        if (sigma) sigma[k] = unreached ? 0ULL : A.sig[i];
+        if (sigma) {
+            const uint64_t sv = A.sig_bytes == 2 ? reinterpret_cast<const uint16_t*>(A.sig)[i]
+                              : A.sig_bytes == 4 ? reinterpret_cast<const uint32_t*>(A.sig)[i] : A.sig[i];
+            sigma[k] = unreached ? 0ULL : sv;
+        }
     }
 }
 
@@ -188,6 +197,7 @@ struct LaneAccess {
         A.mtot = (unsigned long long)e.g_->m * (unsigned long long)e.ng_;
         A.hub_lim = e.hub_lim_;
         A.bu_share = (unsigned long long)e.bu_share_;
+        A.sig_bytes = e.sig_bytes_;
         return A;
     }
     // Reset the lane state a batch touched: per task when few were touched,
@@ -293,6 +303,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     ng_ = lanes >> gs_;
     need_bc_ = need_bc;
     lvl_bytes_ = g->level_bytes_hint == 2 ? 2 : 1;
+    sig_bytes_ = gs_ == 7 ? g->sigma_bytes_hint : 8;
     set_tuning(sparse_lanes, -1, levels_per_graph);
     stream_ = stream;
     int dev = 0;
@@ -370,15 +381,21 @@ void LaneEngine::set_tuning(int sparse_lanes, int light_steps, int levels_per_gr
     graphs_.clear();
 }
 
-// Graph keys: 0..2 expand MODE; 3 + (wide*2 + f64)*2 + refsem: backward; +100 with 16-bit levels.
+// Graph keys: forward = MODE + 10 * w; backward = 100 + 20 * w + (wide*2 + f64)*2 + refsem;
+// w = path-count width (0: 8 bytes, 1: 4, 2: 2; 128-lane groups only); +1000 with 16-bit levels.
+int LaneEngine::width_index() const { return sig_bytes_ == 2 ? 2 : sig_bytes_ == 4 ? 1 : 0; }
+
 gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     for (auto& c : graphs_) if (c.key == key) { *out = c.exec; return GBC_OK; }
-    KArgs A = LaneAccess::args(*this, (key % 100) >= 3 ? ((((key % 100) - 3) & 1) ? GBC_BC_REFERENCE : GBC_BC_BRANDES)
-                                                       : GBC_BC_BRANDES);
+    const int lv16 = key >= 1000 ? 1 : 0, k = key % 1000;
+    const bool bwd = k >= 100;
+    KArgs A = LaneAccess::args(*this, (bwd && ((k - 100) & 1)) ? GBC_BC_REFERENCE : GBC_BC_BRANDES);
     const LevelKernels& K = level_kernels(block_);
-    const int lv16 = key >= 100 ? 1 : 0, k = key % 100;
-    void (*fn)(KArgs) = gs_ == 7 ? (k < 3 ? K.expand_q[lv16][k] : K.backward_q[lv16][(k - 3) >> 1])
-                                 : (k < 3 ? K.expand[lv16][k] : K.backward[lv16][(k - 3) >> 1]);
+    const int w = bwd ? (k - 100) / 20 : k / 10;
+    const int v = bwd ? ((k - 100) % 20) >> 1 : k % 10;
+    void (*fn)(KArgs) = gs_ == 7 ? (bwd ? K.backward_q[lv16][v][w] : K.expand_q[lv16][v][w])
+                                 : (bwd ? K.backward[lv16][v] : K.expand[lv16][v]);
+    if (!fn) { set_error("no level kernel for key %d", key); return GBC_ERR_ARG; }
     // one wave: as many CTAs as fit on every SM at once (at most 2048 threads per SM)
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block_, 0) != cudaSuccess) { cudaGetLastError(); occ = 1; }
@@ -463,8 +480,9 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         GBC_CUDA(cudaGetLastError());
         res.kernel_launches += 1;
         cudaGraphExec_t fwd;
-        const int lv16 = (lvl_bytes_ == 2) ? 100 : 0;
-        GBC_TRY(get_graph(lv16 + mode, &fwd));
+        const int lv16 = (lvl_bytes_ == 2) ? 1000 : 0;
+        const int wi = mode == 1 ? width_index() : 0;
+        GBC_TRY(get_graph(lv16 + mode + 10 * wi, &fwd));
         Ctl* h = (Ctl*)ctl_host_;
         int64_t launched = 0;
         GBC_TRY(ensure_events(2));
@@ -519,6 +537,16 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             set_error("BFS deeper than %d levels", MAX_LEVEL);
             return GBC_ERR_LIMIT;
         }
+        if (mode == 1 && sig_bytes_ < 8 && h->any_ovf) {
+            // a path count passed the narrow width: widen (for later batches on this graph too), redo
+            sig_bytes_ = sig_bytes_ == 2 ? 4 : 8;
+            g_->sigma_bytes_hint = sig_bytes_;
+            LaneAccess::reset(*this, A, entries, hentries);
+            GBC_CUDA(cudaGetLastError());
+            res.kernel_launches++;
+            continue;
+        }
+        res.sigma_bytes = mode == 1 ? sig_bytes_ : 8;
         res.levels += maxlevel + 1;
         res.bottom_up_levels += h->bu_levels;
         {
@@ -569,7 +597,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             }
         }
         if (rq.job == LaneJob::BC && maxlevel >= 1) {
-            const int key = lv16 + 3 + ((rq.sigma_wide ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
+            const int key = lv16 + 100 + 20 * wi + ((rq.sigma_wide ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
                             (rq.semantics == GBC_BC_REFERENCE ? 1 : 0);
             cudaGraphExec_t bwd;
             GBC_TRY(get_graph(key, &bwd));

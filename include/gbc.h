@@ -108,6 +108,8 @@ typedef struct {
     int64_t bwd_kernels;      /* dependency-sweep level kernels launched */
     int32_t group_lanes;      /* lanes per group of the engine that ran (32 or 128; 1 = plain engine) */
     int32_t bottom_up_levels; /* closeness levels discovered bottom-up, summed over batches */
+    int32_t sigma_bytes;      /* bytes per exact path count in the last batch: 128-lane groups store
+                                 them in 2 or 4 bytes while they fit, else 8 */
 } gbc_run_stats;
 
 typedef struct gbc_graph_s* gbc_graph;

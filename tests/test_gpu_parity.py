@@ -105,6 +105,36 @@ def test_cc_direction_switching(gpu, orc, graphs, name):
         assert st["bottom_up_levels"] > 0
 
 
+@pytest.mark.parametrize("side,width", [(6, 2), (14, 4), (30, 8)])
+def test_path_count_widths(gpu, orc, side, width):
+    """128-lane groups store exact path counts in 2 bytes and widen a batch to
+    4 and then 8 bytes when a count does not fit; results stay bit-exact.
+    Full grids from a corner: the largest count is C(2(side-1), side-1) -- 252,
+    10.4M and 3.0e16 for sides 6, 14, 30.  A later call on the same graph starts
+    at the width found (no redo)."""
+    csr = gpu.gen_grid(side, side, 0.0, seed=1)
+    og = orc.Graph(csr.row, csr.col)
+    src = np.arange(0, min(csr.n, 128), dtype=np.int32)     # vertex 0 is a corner
+    ref, novf = orc.bc(og, src, nthreads=8)
+    assert novf == 0
+    with gpu.Graph(csr) as G:
+        got = G.bc(src, lanes=128, group_lanes=128, sigma_mode=gpu.SIGMA_EXACT)
+        st = G.stats()
+        assert st["sigma_bytes"] == width and st["group_lanes"] == 128
+        assert relerr(got, ref) < TOL_F64
+        launches = st["kernel_launches"]
+        again = G.bc(src, lanes=128, group_lanes=128, sigma_mode=gpu.SIGMA_EXACT)
+        assert G.stats()["sigma_bytes"] == width
+        assert G.stats()["kernel_launches"] <= launches
+        assert relerr(again, ref) < TOL_F64
+        dist, sig, ovf = G.sssp(src[:4], lanes=128, group_lanes=128)
+    for i in range(4):
+        d0, s0, o0, _ = orc.sssp(og, int(src[i]))
+        assert np.array_equal(dist[i], d0) and np.array_equal(sig[i], s0) and not ovf[i]
+    d0, s0, _, _ = orc.sssp(og, 0)
+    assert (int(s0.max()) > 0xFFFF) == (width > 2) and (int(s0.max()) > 0xFFFFFFFF) == (width > 4)
+
+
 @pytest.mark.parametrize("name", ["rmat14", "grid24", "star+grid", "er2k"])
 @pytest.mark.parametrize("threads", [128, 512])
 def test_cta_shapes(gpu, orc, graphs, name, threads):
