@@ -47,7 +47,7 @@ class RunStats(C.Structure):
                 ("total_ms", C.c_double), ("lanes", C.c_int32), ("sigma_mode_used", C.c_int32),
                 ("fwd_ms", C.c_double), ("bwd_ms", C.c_double), ("fwd_kernels", C.c_int64),
                 ("bwd_kernels", C.c_int64), ("group_lanes", C.c_int32), ("bottom_up_levels", C.c_int32),
-                ("sigma_bytes", C.c_int32)]
+                ("sigma_bytes", C.c_int32), ("neighbour_visits", C.c_int64)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_ if f[0] != "reserved"}

@@ -101,6 +101,7 @@ struct LaneResult {
     int64_t fwd_kernels = 0, bwd_kernels = 0;
     int64_t bottom_up_levels = 0;       // closeness levels discovered bottom-up
     int32_t sigma_bytes = 8;            // bytes per exact path count of the last batch
+    int64_t neighbour_visits = 0;       // top-down forward tasks' neighbour visits (degrees summed over entries)
     // last batch only: frontier entries per BFS level (regular + hub queue) and
     // device time per forward / dependency-sweep graph launch (levels_per_graph
     // levels each)

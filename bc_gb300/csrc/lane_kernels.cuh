@@ -56,6 +56,7 @@ struct Ctl {
     unsigned long long fprev;   // the same for the running level
     unsigned long long mu;      // bottom-up level: degree sum of (vertex, group) pairs still unreached in some lane
     unsigned long long bnext;   // bottom-up level: fetch position over the done-bitmap words
+    unsigned long long visits;  // neighbour visits of top-down forward tasks (degree summed over entries)
 };
 
 struct KArgs {
@@ -280,6 +281,13 @@ __device__ __forceinline__ void stage_flush(const KArgs& A, Stage& S) {
     }
     __syncwarp();
     S.cnt = 0;
+}
+
+// Neighbour visits counted by the threads of a warp, added to the control block.
+__device__ __forceinline__ void add_visits(const KArgs& A, unsigned long long vis) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vis += __shfl_xor_sync(FULL, vis, o);
+    if ((threadIdx.x & 31) == 0 && vis) atomicAdd(&A.ctl->visits, vis);
 }
 
 // Entries of threads with has == true: hub entries straight to the hub queue,
@@ -834,6 +842,7 @@ __global__ void __launch_bounds__(NT, (MINB<LT, MODE == 2, NT>)) expand_kernel(K
     const int d = *(volatile int*)&A.ctl->level;
     const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
     Stage S{stg[wib], 0};
+    unsigned long long vis = 0;
     if (!done) {
         const LT dl = (LT)d;
         // hub entries: one CTA per entry, warps split the neighbours
@@ -851,6 +860,7 @@ __global__ void __launch_bounds__(NT, (MINB<LT, MODE == 2, NT>)) expand_kernel(K
             const bool act = (lv[((size_t)v << 5) + t] == dl);
             const unsigned am = __ballot_sync(FULL, act);
             if (am == 0u) continue;   // uniform across the CTA
+            if (threadIdx.x == 0) vis += (unsigned long long)(A.row[v + 1] - A.row[v]);
             if (MODE == 0 && act && wib == 0) {
                 const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
                 atomicAdd(&cc_sh[g * 32 + t], (unsigned long long)c);
@@ -892,6 +902,7 @@ __global__ void __launch_bounds__(NT, (MINB<LT, MODE == 2, NT>)) expand_kernel(K
             unsigned am;
             long long r0, r1;
             fetch_entry<LT>(A, d, base + t, e, ent, am, r0, r1);
+            if (am) vis += (unsigned long long)(r1 - r0);
             const bool light = am && (long long)__popc(am) * (r1 - r0) <= A.light;
             fwd_light<MODE, LT>(A, S, d, ent, light ? am : 0u, r0, r1, cc_sh);
             unsigned hv = __ballot_sync(FULL, am && !light);
@@ -919,6 +930,7 @@ __global__ void __launch_bounds__(NT, (MINB<LT, MODE == 2, NT>)) expand_kernel(K
         }
     }
     stage_flush(A, S);
+    add_visits(A, vis);
     if (MODE == 0) {
         __syncthreads();
         for (int i = threadIdx.x; i < A.ng * 32; i += blockDim.x)
@@ -1554,6 +1566,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
     const int d = *(volatile int*)&A.ctl->level;
     const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
     Stage S{stg[wib], 0};
+    unsigned long long vis = 0;
     const bool bu = MODE == 0 && A.dir && *(volatile int*)&A.ctl->bu;
     unsigned long long mu = 0;
     if (!done && bu) {
@@ -1574,6 +1587,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
             const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
             const int nact = __reduce_add_sync(FULL, __popc(act4));
             if (nact == 0) continue;   // uniform across the CTA
+            if (threadIdx.x == 0) vis += (unsigned long long)(A.row[v + 1] - A.row[v]);
             if (wib == 0) q_cc_add<MODE, LT>(A, cc_sh, d, g, v, act4);
             uint64_t acc[4] = {0, 0, 0, 0};
             unsigned ofm = 0;
@@ -1629,6 +1643,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
                 const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
                 const int nact = __reduce_add_sync(FULL, __popc(act4));
                 if (nact == 0) continue;
+                if (t == 0) vis += (unsigned long long)(r1 - r0);
                 q_cc_add<MODE, LT>(A, cc_sh, d, g, v, act4);
                 uint64_t acc[4] = {0, 0, 0, 0};
                 unsigned ofm = 0;
@@ -1641,6 +1656,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
         }
     }
     stage_flush(A, S);
+    add_visits(A, vis);
     if (MODE == 0) {
         if (A.dir) {   // the next level's frontier edges, and the edges left unreached by a bottom-up level
             unsigned long long f = S.fdeg, m = mu;

@@ -549,6 +549,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         res.sigma_bytes = mode == 1 ? sig_bytes_ : 8;
         res.levels += maxlevel + 1;
         res.bottom_up_levels += h->bu_levels;
+        res.neighbour_visits += (int64_t)h->visits;
         {
             // frontier entries of every level of this batch: foff / hoff hold the level bounds
             std::vector<unsigned long long> fo(maxlevel + 2), ho(maxlevel + 2);

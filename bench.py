@@ -19,7 +19,10 @@ component / time.
           once + 16 B per lane and vertex of lane state per sweep, + 16 B per
           vertex of BC accumulation in the sweep) over its CUDA-event duration,
           against the measured HBM copy bandwidth; traffic from the committed
-          ncu summary.
+          ncu summary (a small-case capture scaled by those bytes);
+          visit_model: the bytes the kernels request (own level row and lane
+          state per frontier entry, the neighbour's level row per neighbour
+          visit, one path count / rho per lane and undirected edge).
   cpu_baseline : the oracle's FP64 Brandes with all host threads on a
           bounded sample of the same sources.
   clocks : SM clocks and throttle reasons sampled during the timed region.
@@ -358,7 +361,37 @@ def ba_section(G, hbm, peak_kind):
             out[job] = {"gteps": round(best["edges_traversed"] / best["kernel_ms"] / 1e6, 3),
                         "ms": round(best["kernel_ms"], 3), "lanes": int(best["lanes"]),
                         "roofline": kernel_roofline(best, csr.n, csr.m, csr.n, job, hbm, peak_kind)}
+        # source order: the library's level-profile grouping (above) against the reference's
+        # shared-BFS pairing (Brandes.c:417-475, each source followed by its first neighbour of
+        # degree != 1 not yet done) and plain id order, both kept as given (source_order = 1)
+        orders = {"pairing": pairing_order(csr), "id": np.arange(csr.n, dtype=np.int32)}
+        for name, order in orders.items():
+            best = None
+            for _ in range(3):
+                g.bc(order, delta_precision=G.DELTA_F64, source_order=1)
+                st = g.stats()
+                best = st["kernel_ms"] if best is None else min(best, st["kernel_ms"])
+            out["bc"]["ms_" + name + "_order"] = round(best, 3)
     return out
+
+
+def pairing_order(csr):
+    """The reference shared-BFS driver's source sequence: in id order, each
+    source not yet done, then its first neighbour of degree != 1 not yet done."""
+    deg = np.diff(csr.row)
+    done = np.zeros(csr.n, bool)
+    out = []
+    for s in range(csr.n):
+        if done[s]:
+            continue
+        done[s] = True
+        out.append(s)
+        for x in csr.col[csr.row[s]:csr.row[s + 1]]:
+            if deg[x] != 1 and not done[x]:
+                done[x] = True
+                out.append(int(x))
+                break
+    return np.array(out, np.int32)
 
 
 def reduction_section(G):
@@ -531,6 +564,8 @@ def main():
     fwd_k = bwd_k = launches = 0
     edges = 0
     group = 32
+    visits = entries = 0
+    sig_bytes = 8
     for i in range(args.warmup, args.warmup + args.steps):
         st = run_step(i)
         group = st.group_lanes
@@ -539,6 +574,9 @@ def main():
         fwd_k += st.fwd_kernels
         bwd_k += st.bwd_kernels
         launches += st.kernel_launches
+        visits += st.neighbour_visits
+        entries += st.frontier_entries
+        sig_bytes = st.sigma_bytes
         edges += int(ce[step_sources(i)].sum())
     e1.record(stream)
     torch.cuda.synchronize()
@@ -569,12 +607,26 @@ def main():
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     tr = load_traffic()
     traffic = None
-    if tr and tr.get("kernel") == dom and tr.get("per_launch_bytes_full_size"):
-        traffic = tr["per_launch_bytes_full_size"]
+    if tr and dom in tr and tr[dom].get("per_launch_bytes_full_size"):
+        traffic = tr[dom]["per_launch_bytes_full_size"]
+    # visit model: what the level kernels request, as opposed to the lane state once per sweep.
+    # Every frontier entry reads its own level row and writes its lanes' state; every neighbour
+    # visit reads the neighbour's level row; each lane reads the path count (forward) or rho
+    # (sweep) of each predecessor / successor, at most once per undirected edge per lane.
+    row_b = group  # 8-bit levels: one byte per lane of a group
+    st_b = sig_bytes if fwd_dom else 4            # FP32 rho in the default FP32-delta sweep
+    vm = (entries * (row_b + group * st_b) + visits * row_b + B * (M // 2) * st_b * args.steps) / max(args.steps, 1)
+    vm_launch = vm * args.steps / max(dom_k, 1)
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 5), "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
             "alg_bytes_per_launch": int(dom_bytes / max(dom_k, 1)),
-            "avg_launch_ms": round(dom_ms / max(dom_k, 1), 4)}
+            "avg_launch_ms": round(dom_ms / max(dom_k, 1), 4),
+            "visit_model": {"bytes_per_launch": int(vm_launch),
+                            "achieved": round(vm_launch / (dom_ms / max(dom_k, 1) * 1e-3) / 1e9, 2),
+                            "frac": round(vm_launch / (dom_ms / max(dom_k, 1) * 1e-3) / 1e9 / hbm, 5),
+                            "neighbour_visits_per_batch": int(visits / max(args.steps, 1)),
+                            "frontier_entries_per_batch": int(entries / max(args.steps, 1)),
+                            "path_count_bytes": sig_bytes}}
 
     out = None
     if rank == 0:

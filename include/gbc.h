@@ -110,6 +110,8 @@ typedef struct {
     int32_t bottom_up_levels; /* closeness levels discovered bottom-up, summed over batches */
     int32_t sigma_bytes;      /* bytes per exact path count in the last batch: 128-lane groups store
                                  them in 2 or 4 bytes while they fit, else 8 */
+    int64_t neighbour_visits; /* adjacency entries scanned by top-down forward tasks (each frontier
+                                 entry's degree), summed over batches; the sweep scans the same */
 } gbc_run_stats;
 
 typedef struct gbc_graph_s* gbc_graph;
