@@ -202,7 +202,10 @@ static gbc_status resolve_options(const gbc_options* opt, gbc_options& o) {
     if (o.sigma_mode < GBC_SIGMA_AUTO || o.sigma_mode > GBC_SIGMA_WIDE) { set_error("bad sigma mode"); return GBC_ERR_ARG; }
     if (o.engine < GBC_ENGINE_AUTO || o.engine > GBC_ENGINE_LANES) { set_error("bad engine"); return GBC_ERR_ARG; }
     if (o.lanes != 0 && (o.lanes < 32 || o.lanes > 1024 || o.lanes % 32)) { set_error("lanes must be 0 or a multiple of 32 in [32,1024]"); return GBC_ERR_ARG; }
-    if (o.group_lanes != 0 && o.group_lanes != 32 && o.group_lanes != 128) { set_error("group_lanes must be 0, 32 or 128"); return GBC_ERR_ARG; }
+    if (o.group_lanes != 0 && o.group_lanes != 1 && o.group_lanes != 32 && o.group_lanes != 128) {
+        set_error("group_lanes must be 0, 1, 32 or 128");
+        return GBC_ERR_ARG;
+    }
     if (o.group_lanes == 128 && o.lanes % 128) { set_error("group_lanes 128 needs lanes = 0 or a multiple of 128"); return GBC_ERR_ARG; }
     if (o.direction != 0 && o.direction != 1) { set_error("direction must be 0 or 1"); return GBC_ERR_ARG; }
     if (o.block_threads != 0 && o.block_threads != 128 && o.block_threads != 256 && o.block_threads != 512) {
@@ -243,13 +246,14 @@ static int32_t group_of(const gbc_graph_s* G, const gbc_options& o) {
 static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested, int32_t group) {
     if (requested) return requested;
     const DevGraph& g = G->g;
-    int32_t lanes = (int32_t)std::min<int64_t>(G->tuned.lanes ? G->tuned.lanes : 1024, ((k + group - 1) / group) * group);
-    lanes = std::max(lanes, group);
+    const int32_t unit = group == 1 ? 32 : group;   // batches stay a multiple of 32 lanes
+    int32_t lanes = (int32_t)std::min<int64_t>(G->tuned.lanes ? G->tuned.lanes : 1024, ((k + unit - 1) / unit) * unit);
+    lanes = std::max(lanes, unit);
     if (G->eng && (G->eng->has_bc() || !bc) && G->eng->lanes() >= lanes && G->eng->group_lanes() == group)
         return G->eng->lanes();
     const size_t fr = dev_free_bytes();
     const size_t budget = (fr + (G->eng ? G->eng->device_bytes() : 0)) / 2;
-    while (lanes > group && LaneEngine::bytes_needed(g.n, lanes, bc) > budget) lanes -= group;
+    while (lanes > unit && LaneEngine::bytes_needed(g.n, lanes, bc, group) > budget) lanes -= unit;
     return lanes;
 }
 
@@ -269,7 +273,8 @@ static Tuning tuning_of(const gbc_graph_s* G, const gbc_options& o) {
 
 static gbc_status get_engine(gbc_graph_s* G, int32_t lanes, bool bc, const gbc_options& o, LaneEngine** out) {
     const Tuning u = tuning_of(G, o);
-    const int32_t group = (lanes % 128 == 0) ? group_of(G, o) : 32;
+    const int32_t gw = group_of(G, o);
+    const int32_t group = (gw == 1 || lanes % 128 == 0) ? gw : 32;
     if (G->eng && G->eng->lanes() == lanes && (G->eng->has_bc() || !bc) && G->eng->group_lanes() == group) {
         G->eng->set_tuning(u.sparse, u.light, u.lpg, u.block, u.share);
         *out = G->eng.get();
@@ -910,17 +915,24 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         return GBC_OK;
     };
     GBC_TRY(timed(lanes, kb, sp0, li0, lp0, gr0, bt0, best));
-    // lanes per group first: 128-lane groups (four lanes per thread) against 32
+    // lanes per group first: 128-lane groups (four lanes per thread) against 32, and on deep graphs
+    // of low degree one lane per task (lanes whose sources lie far apart rarely share a level)
     if (o.group_lanes == 0 && lanes % 128 == 0) {
         double ms = 0;
         GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 128, bt0, ms));   // warm-up of the 128-lane engine
         GBC_TRY(timed(lanes, kb, sp0, li0, lp0, 128, bt0, ms));
         if (ms < best) { best = ms; best_gr = 128; }
     }
+    if (o.group_lanes == 0 && G->key_depth > SMALL_WORLD_DEPTH && G->g.max_degree <= 64 && G->g.n < (1 << 22)) {
+        double ms = 0;
+        GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 1, bt0, ms));   // warm-up of the one-lane engine
+        GBC_TRY(timed(lanes, kb, sp0, li0, lp0, 1, bt0, ms));
+        if (ms < best) { best = ms; best_gr = 1; }
+    }
     // one-thread tasks, then the edge-parallel threshold, then the level-loop graph length
     if (o.light_steps < 0 && best_gr == 32)   // only 32-lane groups have one-thread tasks
         for (int li : {0, 8, 32}) GBC_TRY(consider(best_sp, li, best_lp, best_bt));
-    if (o.sparse_lanes < 0)
+    if (o.sparse_lanes < 0 && best_gr != 1)   // one lane per task has no lane-parallel expansion
         for (int sp : {1, 4}) GBC_TRY(consider(sp, best_li, best_lp, best_bt));
     if (o.levels_per_graph <= 0 && G->eng && G->eng->level_bytes() == 2) GBC_TRY(consider(best_sp, best_li, 64, best_bt));
     // CTA shape of the level kernels
@@ -932,7 +944,7 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         double per_src = best / lanes;
         for (int32_t w = lanes / 2; w >= 32; w /= 2) {
             double ms = 0;
-            const int gw = (w % 128 == 0) ? best_gr : 32;
+            const int gw = (best_gr == 1 || w % 128 == 0) ? best_gr : 32;
             GBC_TRY(tune_batch(G, w, w, o, best_sp, best_li, best_lp, gw, best_bt, ms));   // warm-up of the narrower engine
             GBC_TRY(timed(w, w, best_sp, best_li, best_lp, gw, best_bt, ms));
             if (ms / w >= per_src) break;
@@ -1076,7 +1088,7 @@ gbc_status gbc_sssp(gbc_graph G, const int32_t* sources, int32_t k, const gbc_op
     GBC_TRY(resolve_sources(G, sources, k, hsrc));
     GBC_TRY(upload_sources(G, hsrc));
     const int32_t n = G->g.n;
-    const int32_t grp = group_of(G, o);
+    const int32_t grp = group_of(G, o) == 1 ? 32 : group_of(G, o);   // batches stay a multiple of 32 lanes
     const int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((k + grp - 1) / grp) * grp);
     LaneEngine* E = nullptr;
     GBC_TRY(get_engine(G, lanes, true, o, &E));

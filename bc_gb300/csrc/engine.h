@@ -116,7 +116,8 @@ public:
     LaneEngine(const LaneEngine&) = delete;
     LaneEngine& operator=(const LaneEngine&) = delete;
     // Allocate lane state for `lanes` (multiple of 32, <= 1024) on graph g.
-    // group_lanes: sources per lane group (32: one per warp thread; 128: four per thread).
+    // group_lanes: sources per lane group (32: one per warp thread; 128: four per thread;
+    // 1: one lane per task, lane-major state, for deep graphs whose lanes rarely share a level).
     gbc_status init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
                     cudaStream_t stream, int group_lanes = 32);
     // Expansion tuning (negative = default: 2 / 16 / 16 / 256 threads / 16;
@@ -144,7 +145,7 @@ public:
     const DevGraph* graph() const { return g_; }
     cudaStream_t stream() const { return stream_; }
     size_t device_bytes() const { return bytes_; }
-    static size_t bytes_needed(int32_t n, int32_t lanes, bool need_bc);
+    static size_t bytes_needed(int32_t n, int32_t lanes, bool need_bc, int32_t group = 32);
 
 private:
     friend struct LaneAccess;

@@ -108,6 +108,8 @@ struct LevelKernels {
     void (*backward[2][4])(KArgs);     // [16-bit levels][wide sigma * 2 + FP64 delta]
     void (*expand_q[2][3][3])(KArgs);    // 128-lane groups: [16-bit levels][MODE][path-count width 8/4/2 bytes]
     void (*backward_q[2][4][3])(KArgs);  // [16-bit levels][wide sigma * 2 + FP64 delta][width]
+    void (*expand_s[3])(KArgs);          // one lane per task: [MODE]
+    void (*backward_s[4])(KArgs);        // [wide sigma * 2 + FP64 delta]
 };
 void level_kernels_128(LevelKernels& k);   // lanes_nt128.cu
 void level_kernels_256(LevelKernels& k);   // lanes_nt256.cu
@@ -1920,6 +1922,202 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
 }
 
 
+// ---- one lane per task (group width 1) ---------------------------------------
+// Deep graphs whose sampled sources lie far apart (grids, meshes, roads) give a
+// lane group about one active lane per task, so per-group tasks read a whole
+// level row to find it.  With group width 1 the lane state is lane-major
+// (level / path count / rho [lane][v]), a frontier entry is one (vertex, lane)
+// pair packed v << 10 | lane (n < 2^22), and discovery is a 16-bit
+// compare-and-swap on the neighbour's level, so each (vertex, lane) enters the
+// queue exactly once per batch and no claim array is needed.  Neighbours that
+// are close in id (v +- 1 on a grid) share the cache line of v's own entry.
+// The sweep writes each lane's BC contribution into the lane's path-count slot,
+// which nothing reads after it; lane_bc_reduce_kernel then sums the slots over
+// lanes in lane order, so results stay deterministic.
+constexpr int S_LANE_BITS = 10;
+constexpr uint16_t S_INF = 0xFFFFu;
+
+template <int MODE, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
+    constexpr int WARPS = NT / 32;
+    constexpr int U = LIGHT_U;
+    __shared__ unsigned long long cc_sh[MODE == 0 ? 1024 : 1];
+    __shared__ uint32_t stg[WARPS][STG];
+    if (MODE == 0) {
+        for (int i = threadIdx.x; i < A.ng; i += blockDim.x) cc_sh[i] = 0ULL;
+        __syncthreads();
+    }
+    const int done = *(volatile int*)&A.ctl->done;
+    const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    Stage S{stg[wib], 0};
+    unsigned long long vis = 0;
+    if (!done) {
+        const uint16_t dprev = (uint16_t)(d - 1), dnext = (uint16_t)(d + 1), dl = (uint16_t)d;
+        uint16_t* lv = reinterpret_cast<uint16_t*>(A.lvl);
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            const bool act = base + t < e;
+            const uint32_t ent = act ? A.fq[base + t] : 0u;
+            const int v = (int)(ent >> S_LANE_BITS), a = (int)(ent & ((1u << S_LANE_BITS) - 1u));
+            const long long r0 = act ? A.row[v] : 0, r1 = act ? A.row[v + 1] : 0;
+            const size_t la = (size_t)a * (size_t)A.n;
+            if (act) vis += (unsigned long long)(r1 - r0);
+            if (MODE == 0 && act) {
+                const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
+                atomicAdd(&cc_sh[a], (unsigned long long)c);
+            }
+            const int steps = (int)((r1 - r0 + U - 1) / U);
+            const int maxs = __reduce_max_sync(FULL, steps);
+            long long j = r0;
+            uint64_t acc = 0;
+            bool of = false;
+            int we = WEMPTY;
+            double ws = 0.0;
+            for (int it = 0; it < maxs; it++) {
+                int x[U];
+                uint16_t L[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) x[u] = (j + u < r1) ? A.col[j + u] : -1;
+#pragma unroll
+                for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[la + (size_t)x[u]] : dl;   // dl: neither case below
+                if (MODE != 0 && d > 0) {
+                    uint64_t sv[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) sv[u] = L[u] == dprev ? A.sig[la + (size_t)x[u]] : 0ULL;
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        if (L[u] != dprev) continue;
+                        if (MODE == 1) {
+                            const uint64_t na = acc + sv[u];
+                            of |= (na < acc);
+                            acc = na;
+                        } else {
+                            wadd(ws, we, sv[u]);
+                        }
+                    }
+                }
+                bool has[U];
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    has[u] = L[u] == S_INF && atomicCAS(lv + la + (size_t)x[u], S_INF, dnext) == S_INF;
+                j = min(j + U, r1);
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    warp_append(A, S, has[u], false, ((uint32_t)x[u] << S_LANE_BITS) | (uint32_t)a);
+            }
+            if (act && MODE != 0 && d > 0) {
+                if (MODE == 2) acc = wpack(ws, we, of);
+                A.sig[la + (size_t)v] = acc;
+                if (of) {
+                    atomicOr(&A.ovf[a >> 5], 1u << (a & 31));
+                    A.ctl->any_ovf = 1;
+                }
+            }
+        }
+    }
+    stage_flush(A, S);
+    add_visits(A, vis);
+    if (MODE == 0) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < A.ng; i += blockDim.x)
+            if (cc_sh[i]) atomicAdd(&A.cc[i], cc_sh[i]);
+    }
+    fwd_last_block(A, d, done, Lv<uint16_t>::MAXD);
+}
+
+template <bool WIDE, typename T, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) backward_s_kernel(KArgs A) {
+    constexpr int U = LIGHT_U;
+    const int d = *(volatile int*)&A.ctl->level;
+    const int t = threadIdx.x & 31;
+    const bool refsem = (A.semantics == GBC_BC_REFERENCE);
+    if (d >= 1) {
+        const uint16_t dprev = (uint16_t)(d - 1), dnext = (uint16_t)(d + 1), dl = (uint16_t)d;
+        const uint16_t* lv = reinterpret_cast<const uint16_t*>(A.lvl);
+        const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
+        const unsigned long long e = A.foff[d + 1];
+        for (;;) {
+            unsigned long long base = 0;
+            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
+            base = __shfl_sync(FULL, base, 0);
+            if (base >= e) break;
+            if (base + t < e) {   // the last fetch of a level may leave threads without an entry
+                const uint32_t ent = A.fq[base + t];
+                const int v = (int)(ent >> S_LANE_BITS), a = (int)(ent & ((1u << S_LANE_BITS) - 1u));
+                const long long r0 = A.row[v], r1 = A.row[v + 1];
+                const size_t la = (size_t)a * (size_t)A.n, vi = la + (size_t)v;
+                const uint64_t sw = A.sig[vi];
+                T mv = T(0);
+                int ev = 0;
+                if (WIDE) { mv = wmant<T>(sw); ev = wexp(sw); }
+                Sum<T> acc;
+                int pc = 0;
+                for (long long j = r0; j < r1; j += U) {
+                    int x[U];
+                    uint16_t L[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) x[u] = j + u < r1 ? A.col[j + u] : -1;
+#pragma unroll
+                    for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[la + (size_t)x[u]] : dl;
+                    uint64_t rv[U];
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        rv[u] = 0;
+                        if (L[u] == dnext) {
+                            if (WIDE || sizeof(T) == 8) rv[u] = rw[la + (size_t)x[u]];
+                            else rv[u] = __float_as_uint(reinterpret_cast<const float*>(A.rho)[la + (size_t)x[u]]);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; u++) {
+                        if (L[u] == dnext) {
+                            if (WIDE) acc.add(wterm<T>(mv, ev, rv[u]));
+                            else if (sizeof(T) == 8) acc.add((T)__longlong_as_double((long long)rv[u]));
+                            else acc.add((T)__uint_as_float((unsigned)rv[u]));
+                        } else if (L[u] == dprev) {
+                            pc++;
+                        }
+                    }
+                }
+                const T tw = A.w ? (T)A.w[v] : T(1);
+                T delta;
+                if (WIDE) {
+                    delta = acc.value();
+                    bool of = false;
+                    reinterpret_cast<uint64_t*>(A.rho)[vi] = wpack((T)((tw + delta) / mv), -ev, of);
+                } else {
+                    const T sv = (T)sw;
+                    delta = sv * acc.value();
+                    reinterpret_cast<T*>(A.rho)[vi] = (tw + delta) / sv;
+                }
+                // the lane's contribution replaces its path count, which nothing reads after this
+                const double contrib = (double)delta * (double)A.srcw[a] * (refsem ? (double)pc : 1.0);
+                A.sig[vi] = (uint64_t)__double_as_longlong(contrib);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&A.ctl->blocks, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            A.ctl->blocks = 0;
+            if (d >= 1) {
+                A.ctl->level = d - 1;
+                A.ctl->next = A.foff[d - 1];
+                A.ctl->hnext = A.hoff[d - 1];
+            }
+        }
+    }
+}
+
+
 // 128-lane entry points of one level width; path-count widths 4 and 2 bytes
 // exist for the exact forward and the non-wide sweeps only.
 template <typename LT, int NT>
@@ -1946,6 +2144,13 @@ void fill_q(LevelKernels& K, int lv) {
 // Entry points of every level kernel for NT-thread CTAs.
 template <int NT>
 void fill_level_kernels(LevelKernels& K) {
+    K.expand_s[0] = expand_s_kernel<0, NT>;
+    K.expand_s[1] = expand_s_kernel<1, NT>;
+    K.expand_s[2] = expand_s_kernel<2, NT>;
+    K.backward_s[0] = backward_s_kernel<false, float, NT>;
+    K.backward_s[1] = backward_s_kernel<false, double, NT>;
+    K.backward_s[2] = backward_s_kernel<true, float, NT>;
+    K.backward_s[3] = backward_s_kernel<true, double, NT>;
     K.expand[0][0] = expand_kernel<0, uint8_t, NT>;
     K.expand[0][1] = expand_kernel<1, uint8_t, NT>;
     K.expand[0][2] = expand_kernel<2, uint8_t, NT>;

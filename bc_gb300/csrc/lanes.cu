@@ -35,7 +35,10 @@ __global__ void seed_kernel(KArgs A, const int32_t* __restrict__ src, int kb, in
                 A.sig[i] = WONE;
             }
             A.srcw[l] = A.w ? A.w[s] : 1;
-            if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
+            if (A.gs == 0) {
+                // one lane per task: every lane's source is its own entry
+                A.fq[atomicAdd(&A.ctl->tail, 1ULL)] = ((uint32_t)s << S_LANE_BITS) | (uint32_t)l;
+            } else if (atomicExch(&A.vmark[(size_t)g * A.n + s], 0) != 0) {
                 const uint32_t ent = ((uint32_t)s << 5) | (uint32_t)g;
                 if (is_hub(A, s)) A.hq[atomicAdd(&A.ctl->htail, 1ULL)] = ent;
                 else A.fq[atomicAdd(&A.ctl->tail, 1ULL)] = ent;
@@ -155,6 +158,22 @@ __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, 
 
 constexpr int MAX_LEVEL = Lv<uint16_t>::MAXD;
 
+// One lane per task: bc[v] += the lanes' contributions, which the sweep left in
+// the path-count slots of every (vertex, lane) it processed (levels 1 and
+// deeper), summed in lane order.
+__global__ void lane_bc_reduce_kernel(KArgs A, int lanes) {
+    const uint16_t* lv = reinterpret_cast<const uint16_t*>(A.lvl);
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.n; v += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int a = 0; a < lanes; a++) {
+            const size_t i = (size_t)a * (size_t)A.n + (size_t)v;
+            const uint16_t L = lv[i];
+            if (L != 0 && L != S_INF) s += __longlong_as_double((long long)A.sig[i]);
+        }
+        A.bcg[v] += s;
+    }
+}
+
 // dst[g][v] += bcg[g][v] for every lane group whose destination is set.  One
 // thread per vertex walks the groups in order, so groups that share a
 // destination (one request spanning several groups) never race.
@@ -206,16 +225,21 @@ struct LaneAccess {
     // 10 GB in 12.5 ms, the memsets write 4.4 GB).
     static void reset(LaneEngine& e, const KArgs& A, unsigned long long entries, unsigned long long hentries) {
         const size_t cells = (size_t)e.lanes_ * e.g_->n;
-        if (((entries + hentries) << e.gs_) * 4 < cells) {
+        if (e.gs_ != 0 && ((entries + hentries) << e.gs_) * 4 < cells) {
             cleanup_kernel<<<e.sm_count_ * 4, 256, 0, e.stream_>>>(A, entries, hentries, e.lvl_bytes_);
         } else {
             cudaMemsetAsync(e.lvl_, 0xFF, cells * e.lvl_bytes_, e.stream_);
-            cudaMemsetAsync(e.vmark_, 0xFF, (size_t)e.ng_ * e.g_->n * sizeof(int32_t), e.stream_);
+            if (e.gs_ != 0) cudaMemsetAsync(e.vmark_, 0xFF, e.vmark_sz_, e.stream_);
         }
     }
 };
 
-size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc) {
+size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc, int32_t group) {
+    if (group == 1) {   // 16-bit levels, lane-major state, every (vertex, lane) once in the queue
+        size_t b = (size_t)lanes * n * (2 + 4) + (size_t)(MAX_LEVEL + 2) * 16 + (1 << 20);
+        if (need_bc) b += (size_t)lanes * n * 16 + (size_t)n * 8;
+        return b;
+    }
     const size_t ng = (size_t)lanes / 32;
     size_t b = (size_t)lanes * n * 2 + ng * n * 4 + ng * n * 8 * 4 /*initial queue*/ + (size_t)(MAX_LEVEL + 2) * 8;
     if (need_bc) b += (size_t)lanes * n * 16 + ng * n * 8;
@@ -291,18 +315,23 @@ gbc_status LaneEngine::alloc_queue(unsigned long long cap, unsigned long long hc
 gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int sparse_lanes, int levels_per_graph,
                             cudaStream_t stream, int group_lanes) {
     release();
-    if (group_lanes != 32 && group_lanes != 128) { set_error("lanes per group must be 32 or 128"); return GBC_ERR_ARG; }
-    if (lanes < group_lanes || lanes > 1024 || lanes % group_lanes) {
-        set_error("lanes must be a multiple of %d in [%d,1024]", group_lanes, group_lanes);
+    if (group_lanes != 1 && group_lanes != 32 && group_lanes != 128) { set_error("lanes per group must be 1, 32 or 128"); return GBC_ERR_ARG; }
+    const int32_t unit = group_lanes == 1 ? 32 : group_lanes;
+    if (lanes < unit || lanes > 1024 || lanes % unit) {
+        set_error("lanes must be a multiple of %d in [%d,1024]", unit, unit);
+        return GBC_ERR_ARG;
+    }
+    if (group_lanes == 1 && g->n >= (1 << (32 - S_LANE_BITS))) {
+        set_error("one lane per task supports fewer than 2^%d vertices", 32 - S_LANE_BITS);
         return GBC_ERR_ARG;
     }
     if (g->n >= (1 << 27)) { set_error("lane engine supports fewer than 2^27 vertices"); return GBC_ERR_ARG; }
     g_ = g;
     lanes_ = lanes;
-    gs_ = group_lanes == 128 ? 7 : 5;
+    gs_ = group_lanes == 128 ? 7 : group_lanes == 1 ? 0 : 5;
     ng_ = lanes >> gs_;
     need_bc_ = need_bc;
-    lvl_bytes_ = g->level_bytes_hint == 2 ? 2 : 1;
+    lvl_bytes_ = (g->level_bytes_hint == 2 || group_lanes == 1) ? 2 : 1;   // one lane per task: 16-bit levels (CAS)
     sig_bytes_ = gs_ == 7 ? g->sigma_bytes_hint : 8;
     set_tuning(sparse_lanes, -1, levels_per_graph);
     stream_ = stream;
@@ -313,7 +342,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     const size_t cells = (size_t)lanes * n;
     bool ok = true;
     lvl_sz_ = cells * sizeof(uint16_t);
-    vmark_sz_ = (size_t)ng_ * n * sizeof(int32_t);
+    vmark_sz_ = gs_ ? (size_t)ng_ * n * sizeof(int32_t) : sizeof(int32_t);   // one lane per task claims by level CAS
     ok &= dev_alloc((void**)&lvl_, lvl_sz_) == cudaSuccess;
     ok &= dev_alloc((void**)&vmark_, vmark_sz_) == cudaSuccess;
     ok &= dev_alloc((void**)&foff_, (MAX_LEVEL + 2) * sizeof(unsigned long long)) == cudaSuccess;
@@ -326,7 +355,7 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     if (need_bc) {
         sig_sz_ = cells * sizeof(uint64_t);
         rho_sz_ = cells * sizeof(double);
-        bcg_sz_ = (size_t)ng_ * n * sizeof(double);
+        bcg_sz_ = (gs_ ? (size_t)ng_ : 1) * n * sizeof(double);   // one lane per task: one BC accumulator
         ok &= dev_alloc((void**)&sig_, sig_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&rho_, rho_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&bcg_, bcg_sz_) == cudaSuccess;
@@ -354,13 +383,13 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
         // ids in descending degree order (every device graph of this library): hub <=> id < n_hubs_
         hub_lim_ = unsorted ? -1 : (int)nh;
     }
-    GBC_TRY(alloc_queue((unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
+    GBC_TRY(alloc_queue(gs_ == 0 ? (unsigned long long)lanes * n + (1ULL << 16) : (unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));
     GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, cells * sizeof(uint16_t), stream_));
-    GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * n * sizeof(int32_t), stream_));
+    GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, vmark_sz_, stream_));
     GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
     GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
-    bytes_ = cells * 2 + (size_t)ng_ * n * 4 + (fcap_ + hcap_) * 4 + (need_bc ? cells * 16 + (size_t)ng_ * n * 8 : 0);
+    bytes_ = cells * 2 + vmark_sz_ + (fcap_ + hcap_) * 4 + (need_bc ? cells * 16 + bcg_sz_ : 0);
     return GBC_OK;
 }
 
@@ -394,6 +423,7 @@ gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     const int w = bwd ? (k - 100) / 20 : k / 10;
     const int v = bwd ? ((k - 100) % 20) >> 1 : k % 10;
     void (*fn)(KArgs) = gs_ == 7 ? (bwd ? K.backward_q[lv16][v][w] : K.expand_q[lv16][v][w])
+                      : gs_ == 0 ? (bwd ? K.backward_s[v] : K.expand_s[v])
                                  : (bwd ? K.backward[lv16][v] : K.expand[lv16][v]);
     if (!fn) { set_error("no level kernel for key %d", key); return GBC_ERR_ARG; }
     // one wave: as many CTAs as fit on every SM at once (at most 2048 threads per SM)
@@ -422,17 +452,22 @@ gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
 
 gbc_status LaneEngine::bc_begin() {
     if (!need_bc_) { set_error("engine has no BC state"); return GBC_ERR_ARG; }
-    GBC_CUDA(cudaMemsetAsync(bcg_, 0, (size_t)ng_ * g_->n * sizeof(double), stream_));
+    GBC_CUDA(cudaMemsetAsync(bcg_, 0, bcg_sz_, stream_));
     return GBC_OK;
 }
 
 gbc_status LaneEngine::bc_finish(double* d_bc) {
+    if (gs_ == 0) {
+        GBC_CUDA(cudaMemcpyAsync(d_bc, bcg_, sizeof(double) * g_->n, cudaMemcpyDeviceToDevice, stream_));
+        return GBC_OK;
+    }
     bc_reduce_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(bcg_, ng_, g_->n, d_bc);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
 }
 
 gbc_status LaneEngine::bc_scatter(double* const* d_dst) {
+    if (gs_ == 0) { set_error("per-group BC partials need lane groups of 32 or 128"); return GBC_ERR_ARG; }
     bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, ng_, g_->n, d_dst);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
@@ -510,7 +545,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         if (h->err & 1) {
             // queue overflow: reset the whole lane state, grow the queue, redo the batch
             GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
-            GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
+            GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, vmark_sz_, stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
             // a (vertex, group) task recurs at most once per lane of its group.  Grow 4x: on
             // deep graphs with 128-lane groups a task recurs at up to 128 levels, and the
@@ -529,7 +564,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
                 lvl_bytes_ = 2;
                 g_->level_bytes_hint = 2;
                 GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, (size_t)lanes_ * g_->n * sizeof(uint16_t), stream_));
-                GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, (size_t)ng_ * g_->n * sizeof(int32_t), stream_));
+                GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, vmark_sz_, stream_));
                 GBC_CUDA(cudaStreamSynchronize(stream_));
                 continue;
             }
@@ -621,6 +656,11 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
                 res.bwd_ms += ms;
                 res.bwd_launch_ms.push_back(ms);
             }
+        }
+        if (rq.job == LaneJob::BC && gs_ == 0 && maxlevel >= 1) {
+            lane_bc_reduce_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(A, lanes_);
+            GBC_CUDA(cudaGetLastError());
+            res.kernel_launches++;
         }
         if (mode == 0 && rq.d_cc) {
             GBC_CUDA(cudaMemcpyAsync(rq.d_cc, ccbuf_, rq.kb * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, stream_));

@@ -421,7 +421,8 @@ static gbc_status profile_order(const DevGraph& g, cudaStream_t s, std::vector<i
 static gbc_status block_engine(Reduction& R, const gbc_options& o, bool bc, LaneEngine** out) {
     const int32_t ns = R.bg.n;
     if (R.b_order.empty()) GBC_TRY(profile_order(*R.dg, R.stream, R.b_order, R.b_group));
-    int32_t group = o.group_lanes ? o.group_lanes : R.b_group;
+    // the block graph runs on lane groups (one lane per task is for whole deep graphs)
+    int32_t group = o.group_lanes > 1 ? o.group_lanes : R.b_group;
     if (o.lanes % group) group = 32;
     int32_t lanes = o.lanes ? o.lanes : std::min<int32_t>(1024, ((ns + group - 1) / group) * group);
     const size_t fr = dev_free_bytes() + (R.eng ? R.eng->device_bytes() : 0);

@@ -63,7 +63,7 @@ def main():
     p.add_argument("size", type=int, help="grid side, or R-MAT scale")
     p.add_argument("--sources", type=int, default=1024)
     p.add_argument("--lanes", type=int, default=1024)
-    p.add_argument("--group", type=int, default=0, choices=(0, 32, 128))
+    p.add_argument("--group", type=int, default=0, choices=(0, 1, 32, 128))
     p.add_argument("--block", type=int, default=0, choices=(0, 128, 256, 512))
     p.add_argument("--bins", type=int, default=16)
     a = p.parse_args()

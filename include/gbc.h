@@ -78,7 +78,9 @@ typedef struct {
     int32_t light_steps;      /* a frontier task with (active lanes x degree) <= this is expanded by a
                                  single thread, 32 tasks per warp; 0 = never; -1 = autotune */
     int32_t group_lanes;      /* sources per lane group: 32 (one per warp thread) or 128 (four per
-                                 thread; lanes must then be a multiple of 128); 0 = automatic */
+                                 thread; lanes must then be a multiple of 128), or 1 (one lane per
+                                 task, lane-major state: deep graphs whose lanes rarely share a
+                                 level; fewer than 2^22 vertices); 0 = automatic */
     int32_t direction;        /* closeness with 128-lane groups: 0 = switch between top-down and
                                  bottom-up levels by frontier size (default); 1 = top-down only */
     int32_t block_threads;    /* threads per CTA of the level kernels: 128, 256 or 512; 0 = the
@@ -106,7 +108,8 @@ typedef struct {
     double  bwd_ms;           /* device time of the dependency-sweep level kernels */
     int64_t fwd_kernels;      /* forward level kernels launched (incl. no-op tail launches) */
     int64_t bwd_kernels;      /* dependency-sweep level kernels launched */
-    int32_t group_lanes;      /* lanes per group of the engine that ran (32 or 128; 1 = plain engine) */
+    int32_t group_lanes;      /* lanes per group of the engine that ran (1, 32 or 128; the plain
+                                 engine reports 1 with lanes = 1) */
     int32_t bottom_up_levels; /* closeness levels discovered bottom-up, summed over batches */
     int32_t sigma_bytes;      /* bytes per exact path count in the last batch: 128-lane groups store
                                  them in 2 or 4 bytes while they fit, else 8 */
@@ -178,7 +181,8 @@ gbc_status gbc_bc_device(gbc_graph g, const int32_t* d_sources, int32_t k, const
                          double* d_bc, void* stream);
 
 /* Autotuner: time one betweenness batch of the given sources (k = 0: all
- * vertices) per candidate expansion setting -- lane-group width (32/128),
+ * vertices) per candidate expansion setting -- lane-group width (32/128, and
+ * 1 on deep graphs of degree <= 64),
  * one-thread task threshold (light_steps 0/8/16/32), edge-parallel threshold
  * (sparse_lanes 1/2/4), level kernels per captured graph (16/64, deep graphs),
  * threads per CTA of the level kernels (block_threads 128/256/512) and batch

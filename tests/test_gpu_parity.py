@@ -358,6 +358,49 @@ def test_group128_deep_and_wide(gpu, orc):
         assert relerr(got, ref) < TOL_F64
 
 
+@pytest.mark.parametrize("name", ["grid24", "er2k", "ba4096", "rmat12", "karate", "star+grid"])
+def test_one_lane_per_task(gpu, orc, graphs, name):
+    """One lane per task (group_lanes = 1: lane-major state, (vertex, lane)
+    entries, discovery by compare-and-swap on the level) gives the oracle's
+    betweenness in both semantics and both delta precisions, exact closeness,
+    distances and path counts -- also on graphs with many components and with
+    a 3000-leaf hub, which this mode expands one thread per entry."""
+    csr = graphs[name]
+    og = to_orc(orc, csr)
+    src = sources_of(csr, 200)
+    with gpu.Graph(csr) as G:
+        for sem in (0, 1):
+            ref, novf = orc.bc(og, src, semantics=sem, nthreads=8)
+            assert novf == 0
+            got = G.bc(src, semantics=sem, group_lanes=1, sigma_mode=gpu.SIGMA_EXACT)
+            st = G.stats()
+            assert st["group_lanes"] == 1 and st["lanes"] >= 32
+            assert relerr(got, ref) < TOL_F64
+            got32 = G.bc(src, semantics=sem, group_lanes=1, delta_precision=gpu.DELTA_F32)
+            assert relerr(got32, ref) < TOL_F32
+        assert np.array_equal(G.cc(src, group_lanes=1), orc.cc(og, src, nthreads=8))
+        dist, sig, ovf = G.sssp(src[:6], group_lanes=1)
+    for i in range(6):
+        d0, s0, o0, _ = orc.sssp(og, int(src[i]))
+        assert np.array_equal(dist[i], d0) and not ovf[i] and np.array_equal(sig[i], s0)
+
+
+def test_one_lane_per_task_wide_and_partial_batch(gpu, orc):
+    """One lane per task on a grid whose path counts overflow uint64 (wide
+    form), and with a batch narrower than the engine (unused lanes)."""
+    grid = gpu.gen_grid(80, 80, 0.0, seed=1)
+    og = to_orc(orc, grid)
+    src = np.array([0, 79, 3200, 6399, 17, 4100], dtype=np.int32)
+    ref, novf = orc.bc(og, src, scaled=True)
+    assert novf > 0
+    with gpu.Graph(grid) as G:
+        got = G.bc(src, group_lanes=1, lanes=64)
+        st = G.stats()
+        assert st["sigma_mode_used"] == gpu.SIGMA_WIDE and st["group_lanes"] == 1
+        assert relerr(got, ref) < TOL_F64
+        assert np.array_equal(G.cc(src, group_lanes=1, lanes=64), orc.cc(og, src))
+
+
 def test_group128_grid_queue_growth(gpu, orc):
     """128-lane groups of random sources on a grid: a (vertex, group) task
     recurs at up to 128 levels, far beyond the first frontier queue, which
