@@ -126,17 +126,22 @@ def test_c1_ba4096_all_sources(gpu, orc):
 
 def test_grid1024_256_of_8192_sources_vs_oracle(gpu, orc, grid1024):
     """The deep configuration on 256 of its 8,192 uniformly sampled sources
-    (seed 3, as the bench draws them): betweenness in wide form against the
-    oracle's level-normalised FP64 form, closeness bit-exact."""
+    (seed 3, as the bench draws them), on 32-lane groups and one lane per task:
+    betweenness in wide form against the oracle's level-normalised FP64 form,
+    closeness bit-exact."""
     csr = grid1024
     sample = np.random.default_rng(3).choice(csr.n, 8192, replace=False).astype(np.int32)
     src = sample[:256]
     og = orc.Graph(csr.row, csr.col)
     ref, _ = orc.bc(og, src, semantics=orc.BC_BRANDES, scaled=True, nthreads=16)
+    ref_cc = orc.cc(og, src, nthreads=16)
     with gpu.Graph(csr) as G:
-        b64 = G.bc(src, delta_precision=gpu.DELTA_F64)
-        b32 = G.bc(src, delta_precision=gpu.DELTA_F32)
-        cc = G.cc(src)
-    assert relerr(b64, ref) < TOL_F64
-    assert relerr(b32, ref) < TOL_F32_DEEP
-    assert np.array_equal(cc, orc.cc(og, src, nthreads=16))
+        # 32-lane groups, and one lane per task (what the autotuner picks on this graph)
+        for group in (32, 1):
+            b64 = G.bc(src, delta_precision=gpu.DELTA_F64, group_lanes=group)
+            assert G.stats()["group_lanes"] == group
+            b32 = G.bc(src, delta_precision=gpu.DELTA_F32, group_lanes=group)
+            cc = G.cc(src, group_lanes=group)
+            assert relerr(b64, ref) < TOL_F64, group
+            assert relerr(b32, ref) < TOL_F32_DEEP, group
+            assert np.array_equal(cc, ref_cc), group
