@@ -104,7 +104,7 @@ struct gbc_server_s {
     size_t budget = 0;
     int32_t max_lanes = 1024;
     int32_t max_inflight = 64;
-    int32_t nworkers = 4;
+    int32_t nworkers = 8;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::vector<std::unique_ptr<SGraph>> graphs;
@@ -438,7 +438,9 @@ gbc_status gbc_server_create(const gbc_server_config* cfg, gbc_server* out) {
     S->max_lanes = S->cfg.max_lanes ? S->cfg.max_lanes : 1024;
     S->max_inflight = S->cfg.max_inflight > 0 ? S->cfg.max_inflight : 64;
     if (S->cfg.workers < 0 || S->cfg.workers > 16) { set_error("workers must be in [0,16]"); return GBC_ERR_ARG; }
-    S->nworkers = S->cfg.workers ? S->cfg.workers : 4;
+    // 8 by default: with 4, small queries of a mixed stream waited behind large batches (40 q/s on
+    // the serving mix: p50 / p99 148 / 1754 ms with 4 workers, 61 / 976 ms with 8, the same with 16)
+    S->nworkers = S->cfg.workers ? S->cfg.workers : 8;
     S->budget = S->cfg.hbm_budget_bytes ? S->cfg.hbm_budget_bytes : dev_free_bytes() / 2;
     gbc_server_s* raw = S.get();
     int dev = 0;

@@ -80,6 +80,7 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     p.add_argument("--serve-rates", default="5,10,20,40", help="query arrival rates per second, comma-separated")
     p.add_argument("--serve-burst", type=int, default=96, help="queries submitted at once for the saturation point")
+    p.add_argument("--serve-workers", type=int, default=0, help="server worker threads (0: the library default, 4)")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--no-reduction", action="store_true", help="skip the D1+AP reduction section (R-MAT s18 + pendant trees)")
     p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 8192 sources)")
@@ -214,7 +215,7 @@ def cpu_baseline(csr, sample, n_src, threads):
     return dt
 
 
-def serving(G, seconds, rates, burst=96, seed=11):
+def serving(G, seconds, rates, burst=96, seed=11, workers=0):
     """The serving mix: a Poisson stream of queries over 64 device-resident
     graphs of 1K-2M vertices (BA m=2-8, Erdos-Renyi average degree 4-32,
     square grids, R-MAT scale 10-21; seeded sizes, log-uniform).  Queries:
@@ -243,6 +244,7 @@ def serving(G, seconds, rates, burst=96, seed=11):
             specs.append(("rmat", G.gen_rmat(int(np.clip(round(np.log2(n)), 10, 21)), 16, seed=i)))
     cfg = G.ServerConfig()
     cfg.max_lanes = 1024
+    cfg.workers = workers
     h = C.c_void_p()
     G.check(L.gbc_server_create(C.byref(cfg), C.byref(h)))
     gids = []
@@ -310,7 +312,7 @@ def serving(G, seconds, rates, burst=96, seed=11):
     sat = stream(0.0, count=burst) if burst else None
     L.gbc_server_destroy(h)
     return {"graphs": len(specs), "vertices": [min(c.n for _, c in specs), max(c.n for _, c in specs)],
-            "directed_entries": int(sum(c.m for _, c in specs)), "workers": 4, "points": points,
+            "directed_entries": int(sum(c.m for _, c in specs)), "workers": workers or 8, "points": points,
             "saturation": sat,
             "mix": "uniform over graphs: 15% exact CC (graphs <= 32K vertices), 10% exact BC (<= 16K), "
                    "40% k=64 and 35% k=1024 sampled BC"}
@@ -699,7 +701,8 @@ def main():
                    "sample": f"first {n_cpu} of the {args.k} sampled sources, reference semantics, FP64"}
         serve = None
         if not args.no_serve:
-            serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")], args.serve_burst)
+            serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")], args.serve_burst,
+                            workers=args.serve_workers)
         c1 = None if args.no_ba else ba_section(G, hbm, peak_kind)
         red = None if args.no_reduction else reduction_section(G)
         deep = None if args.no_grid else grid_section(G, hbm, peak_kind, args.grid_sources)

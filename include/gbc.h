@@ -346,7 +346,7 @@ typedef struct {
     size_t  hbm_budget_bytes;   /* engines + result vectors; 0 = 50% of free device memory */
     int32_t max_lanes;          /* lanes per shared batch (multiple of 32), 0 = 1024 */
     int32_t max_inflight;       /* requests admitted at once, 0 = 64 */
-    int32_t workers;            /* lane batches in flight at once, on different graphs; 0 = 4 */
+    int32_t workers;            /* lane batches in flight at once, on different graphs; 0 = 8 */
     int32_t reserved[7];
 } gbc_server_config;
 
