@@ -82,7 +82,7 @@ struct LaneRequest {
     int delta_f64 = 1;
     int semantics = GBC_BC_BRANDES;
     unsigned long long* d_cc = nullptr;  // [kb] per-lane distance sums (CC)
-    double* d_bcg = nullptr;             // [ng][n] per-group BC partials (BC)
+    double* d_bcg = nullptr;             // [lanes/32][n] per-32-lane BC partials (BC)
     int32_t* d_dist = nullptr;           // [kb][n] (SSSP) nullable
     uint64_t* d_sigma = nullptr;         // [kb][n] (SSSP) nullable
     bool abort_on_overflow = false;      // exact sigma: stop before the backward sweep if a lane overflowed

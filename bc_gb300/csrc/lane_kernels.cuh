@@ -315,15 +315,15 @@ __device__ __forceinline__ void warp_append(const KArgs& A, Stage& S, bool has, 
     S.cnt += __popc(m);
 }
 
-// First claim of (x, g) for level lev: a plain read filters repeats before the atomic.
-// Only a thread that saw one of x's active lanes unreached (and wrote d+1
-// there) claims: a lane already at d+1 was written by a thread that claimed,
-// so the claim happens once per discovered (x, g) without a vmark round trip
-// for the (many) later visits of the level.
+// First claim of (x, g) for level lev.  Only a thread that saw one of x's
+// active lanes unreached (and wrote d+1 there) claims: a lane already at d+1
+// was written by a thread that claims, so the claim happens once per
+// discovered (x, g) without a vmark access for the (many) later visits of the
+// level.  Repeats are then rare (two warps that saw the same lane unreached),
+// so the exchange goes straight to the atomic: one round trip, where a plain
+// read to filter repeats first made it two.
 __device__ __forceinline__ bool claim(const KArgs& A, size_t gbase, int x, int lev) {
-    int32_t* p = &A.vmark[gbase + x];
-    if (*(volatile int32_t*)p == lev) return false;
-    return atomicExch(p, lev) != lev;
+    return atomicExch(&A.vmark[gbase + x], lev) != lev;
 }
 
 // Direction of the next closeness level (128-lane groups).  Top-down until
@@ -790,10 +790,19 @@ __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint3
         for (int u = 0; u < U; u++) x[u] = (on && j + u < r1) ? A.col[j + u] : -1;
 #pragma unroll
         for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[((size_t)x[u] << 5) + a] : dl;   // dl: neither case below
-        if (MODE != 0 && d > 0) {
-            uint64_t sv[U];
+        // path-count loads, then the discovery stores and claim atomics, then the sums:
+        // the claims' round trip overlaps the loads' instead of following it
+        uint64_t sv[U];
 #pragma unroll
-            for (int u = 0; u < U; u++) sv[u] = L[u] == dprev ? A.sig[((gbase + (size_t)x[u]) << 5) + a] : 0ULL;
+        for (int u = 0; u < U; u++)
+            sv[u] = (MODE != 0 && d > 0 && L[u] == dprev) ? A.sig[((gbase + (size_t)x[u]) << 5) + a] : 0ULL;
+        bool has[U];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (L[u] == INF) lv[((size_t)x[u] << 5) + a] = dnext;
+#pragma unroll
+        for (int u = 0; u < U; u++) has[u] = L[u] == INF && atomicExch(&A.vmark[gbase + x[u]], d + 1) != d + 1;
+        if (MODE != 0 && d > 0) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (L[u] != dprev) continue;
@@ -806,16 +815,6 @@ __device__ __forceinline__ void fwd_light(const KArgs& A, Stage& S, int d, uint3
                 }
             }
         }
-        // discovery: level stores, then every first-claim check, then the atomics
-        int32_t mk[U];
-        bool has[U];
-#pragma unroll
-        for (int u = 0; u < U; u++)
-            if (L[u] == INF) lv[((size_t)x[u] << 5) + a] = dnext;
-#pragma unroll
-        for (int u = 0; u < U; u++) mk[u] = L[u] == INF ? *(volatile int32_t*)&A.vmark[gbase + x[u]] : d + 1;
-#pragma unroll
-        for (int u = 0; u < U; u++) has[u] = mk[u] != d + 1 && atomicExch(&A.vmark[gbase + x[u]], d + 1) != d + 1;
         if (on) {
             j = min(j + U, r1);
             if (j == r1 && MODE != 0 && d > 0) fwd_store<MODE>(A, g, gbase, v, a, acc, of, we, ws);
@@ -1016,7 +1015,7 @@ __device__ __forceinline__ void bwd_finish(const KArgs& A, int g, size_t gbase, 
     double contrib = act ? bwd_lane<WIDE, T>(A, g, gbase, v, t, mv, ev, acc, pc, refsem) : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(FULL, contrib, o);
-    if (t == 0) A.bcg[gbase + v] += contrib;
+    if (t == 0) atomicAdd(&A.bcg[gbase + v], contrib);   // one writer per (v, g) and level: a fire-and-forget add
 }
 
 // Light entries, one per thread: lanes in order, neighbours in CSR order.
@@ -1074,7 +1073,7 @@ __device__ __forceinline__ void bwd_light(const KArgs& A, int d, uint32_t ent, u
         }
         contrib += bwd_lane<WIDE, T>(A, g, gbase, v, a, mv, ev, acc.value(), pc, refsem);
     }
-    A.bcg[gbase + v] += contrib;
+    atomicAdd(&A.bcg[gbase + v], contrib);   // one writer per (v, g) and level: a fire-and-forget add
 }
 
 template <bool WIDE, typename T, typename LT, int NT>
@@ -1222,6 +1221,15 @@ constexpr int Q_ITER = 8;   // neighbours whose level quads are loaded before an
 constexpr int FETCH_Q = 8;  // regular tasks a warp takes per fetch in 128-lane groups (8: 3% faster than 32 on R-MAT s22)
 constexpr unsigned long long TAIL_Q = 16384;   // fewer regular tasks left than this: take one per fetch
 
+// Column of thread t in the chunk of 32 neighbours starting at jb (0 past r1).
+// The scans load the next chunk's columns while they work on the current one,
+// and a task's first chunk is loaded with its own level row, so a column load
+// is never a round trip of its own.
+__device__ __forceinline__ int q_col(const KArgs& A, long long jb, long long r1) {
+    const long long j = jb + (threadIdx.x & 31);
+    return j < r1 ? A.col[j] : 0;
+}
+
 // Next regular tasks of the level for this warp: FETCH_Q per atomic while
 // many remain, then one at a time, so that no warp is left holding several
 // heavy tasks while the rest of the GPU has finished the level.
@@ -1242,12 +1250,14 @@ __device__ __forceinline__ unsigned long long q_fetch(const KArgs& A, unsigned l
 // level d+1.  Results stay in the thread: acc/ofm (exact) or ws/we (wide).
 template <int MODE, typename LT, int SB>
 __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int g, size_t gbase, LT* lv, unsigned act4,
-                                           long long r0, long long r1, int sub, int nsub, uint64_t (&acc)[4],
+                                           long long r0, long long r1, int sub, int nsub, int xm0, uint64_t (&acc)[4],
                                            unsigned& ofm, int (&we)[4], double (&ws)[4]) {
     const int t = threadIdx.x & 31;
-    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+    int xm = xm0;   // columns of the chunk at r0 + 32*sub
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub, xm = xm0) {
         const int cnt = (int)min(32LL, r1 - jb);
-        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        xm0 = q_col(A, jb + 32LL * nsub, r1);   // the next chunk's columns
+        unsigned want = 0;   // bit k: neighbour jb + k had an active lane unreached (d+1 stored there)
         for (int k0 = 0; k0 < cnt; k0 += Q_ITER) {          // uniform across the warp
             Quad<LT> q[Q_ITER];
             int xs[Q_ITER];
@@ -1299,8 +1309,7 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                     }
                 }
             }
-            // discovery: store d+1 in the unreached active lanes; thread i claims neighbour i
-            unsigned want = 0;
+            // discovery: store d+1 in the unreached active lanes
 #pragma unroll
             for (int i = 0; i < Q_ITER; i++) {
                 const bool inr = k0 + i < cnt;
@@ -1311,13 +1320,14 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                     for (int j = 0; j < 4; j++)
                         if ((un >> j) & 1u) px[j] = (LT)(d + 1);
                 }
-                if (__ballot_sync(FULL, un != 0u)) want |= 1u << i;
+                if (__ballot_sync(FULL, un != 0u)) want |= 1u << (k0 + i);
             }
-            const int xi = __shfl_sync(FULL, xm, (k0 + (t & (Q_ITER - 1))) & 31);
-            const bool has = (t < Q_ITER) && ((want >> t) & 1u) && claim(A, gbase, xi, d + 1);
-            if (MODE == 0 && has) S.fdeg += (unsigned long long)(A.row[xi + 1] - A.row[xi]);
-            warp_append(A, S, has, has && is_hub(A, xi), ((uint32_t)xi << 5) | (uint32_t)g);
         }
+        // claims of the whole 32-neighbour chunk at once: thread k claims its own
+        // column xm, so one claim round trip serves up to 32 neighbours
+        const bool has = ((want >> t) & 1u) && claim(A, gbase, xm, d + 1);
+        if (MODE == 0 && has) S.fdeg += (unsigned long long)(A.row[xm + 1] - A.row[xm]);
+        warp_append(A, S, has, has && is_hub(A, xm), ((uint32_t)xm << 5) | (uint32_t)g);
     }
 }
 
@@ -1595,7 +1605,8 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
             unsigned ofm = 0;
             int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
             double ws[4] = {0.0, 0.0, 0.0, 0.0};
-            if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
+            if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS,
+                                                      q_col(A, A.row[v] + 32LL * wib, A.row[v + 1]), acc, ofm, we, ws);
             else q_fwd_edges<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, A.row[v], A.row[v + 1], wib, WARPS, acc, ofm, we, ws);
             if (MODE != 0) {
 #pragma unroll
@@ -1643,6 +1654,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
                 const size_t gbase = (size_t)g * (size_t)A.n;
                 LT* lv = reinterpret_cast<LT*>(A.lvl) + (gbase << 7);
                 const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+                const int xm0 = q_col(A, r0, r1);   // the first chunk's columns, loaded with the level row
                 const int nact = __reduce_add_sync(FULL, __popc(act4));
                 if (nact == 0) continue;
                 if (t == 0) vis += (unsigned long long)(r1 - r0);
@@ -1651,7 +1663,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
                 unsigned ofm = 0;
                 int we[4] = {WEMPTY, WEMPTY, WEMPTY, WEMPTY};
                 double ws[4] = {0.0, 0.0, 0.0, 0.0};
-                if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
+                if (nact > A.sparse) q_fwd_scan<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, xm0, acc, ofm, we, ws);
                 else q_fwd_edges<MODE, LT, SB>(A, S, d, g, gbase, lv, act4, r0, r1, 0, 1, acc, ofm, we, ws);
                 if (MODE != 0 && d > 0) q_fwd_store<MODE, SB>(A, g, gbase, v, act4, acc, ofm, we, ws);
             }
@@ -1683,11 +1695,12 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) expand_q_kernel(KArgs A) {
 template <bool WIDE, typename T, typename LT>
 __device__ __forceinline__ void q_bwd_scan(const KArgs& A, int d, size_t gbase, const LT* lv, unsigned act4,
                                            const T (&mv)[4], const int (&ev)[4], long long r0, long long r1, int sub,
-                                           int nsub, Sum<T> (&acc)[4], int (&pc)[4]) {
+                                           int nsub, int xm0, Sum<T> (&acc)[4], int (&pc)[4]) {
     const int t = threadIdx.x & 31;
-    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub) {
+    int xm = xm0;   // columns of the chunk at r0 + 32*sub
+    for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub, xm = xm0) {
         const int cnt = (int)min(32LL, r1 - jb);
-        const int xm = (t < cnt) ? A.col[jb + t] : 0;
+        xm0 = q_col(A, jb + 32LL * nsub, r1);   // the next chunk's columns
         for (int k0 = 0; k0 < cnt; k0 += Q_ITER) {
             Quad<LT> q[Q_ITER];
             int xs[Q_ITER];
@@ -1783,7 +1796,9 @@ __device__ __forceinline__ void q_bwd_edges(const KArgs& A, int d, size_t gbase,
 }
 
 // delta, rho and BC contributions of thread t's active lanes of (v, g),
-// warp-summed into bcg.
+// summed per 32-lane quarter of the group (threads 8q..8q+7 hold lanes
+// 32q..32q+31) into bcg row 4g+q: BC partials are kept per 32 lanes for every
+// group width, so a lane batch can carry a different request in each quarter.
 template <bool WIDE, typename T, int SB>
 __device__ __forceinline__ void q_bwd_finish(const KArgs& A, int g, size_t gbase, int v, unsigned act4, const T (&mv)[4],
                                              const int (&ev)[4], const Sum<T> (&acc)[4], const int (&pc)[4], bool refsem) {
@@ -1807,8 +1822,9 @@ __device__ __forceinline__ void q_bwd_finish(const KArgs& A, int g, size_t gbase
         contrib += (double)delta * (double)A.srcw[(g << 7) + 4 * t + j] * (refsem ? (double)pc[j] : 1.0);
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) contrib += __shfl_xor_sync(FULL, contrib, off);
-    if (t == 0) A.bcg[gbase + v] += contrib;
+    for (int off = 4; off > 0; off >>= 1) contrib += __shfl_xor_sync(FULL, contrib, off);
+    // one writer per (v, quarter) and level: a fire-and-forget add
+    if ((t & 7) == 0) atomicAdd(&A.bcg[4 * gbase + (size_t)(t >> 3) * (size_t)A.n + v], contrib);
 }
 
 template <bool WIDE, typename T>
@@ -1854,7 +1870,8 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
             q_sigma_of<WIDE, T>(A, gbase, v, act4, mv, ev);
             Sum<T> acc[4];
             int pc[4] = {0, 0, 0, 0};
-            if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
+            if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, A.row[v], A.row[v + 1], wib, WARPS,
+                                                     q_col(A, A.row[v] + 32LL * wib, A.row[v + 1]), acc, pc);
             else q_bwd_edges<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, A.row[v], A.row[v + 1], wib, WARPS, acc, pc);
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -1892,6 +1909,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
                 const size_t gbase = (size_t)g * (size_t)A.n;
                 const LT* lv = reinterpret_cast<const LT*>(A.lvl) + (gbase << 7);
                 const unsigned act4 = Quad<LT>::load(lv + ((size_t)v << 7), t).eq(d);
+                const int xm0 = q_col(A, r0, r1);   // the first chunk's columns, loaded with the level row
                 const int nact = __reduce_add_sync(FULL, __popc(act4));
                 if (nact == 0) continue;
                 T mv[4];
@@ -1899,7 +1917,7 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_q_kernel(KArgs A) {
                 q_sigma_of<WIDE, T>(A, gbase, v, act4, mv, ev);
                 Sum<T> acc[4];
                 int pc[4] = {0, 0, 0, 0};
-                if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
+                if (nact > A.sparse) q_bwd_scan<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, xm0, acc, pc);
                 else q_bwd_edges<WIDE, T, LT>(A, d, gbase, lv, act4, mv, ev, r0, r1, 0, 1, acc, pc);
                 q_bwd_finish<WIDE, T, SB>(A, g, gbase, v, act4, mv, ev, acc, pc, refsem);
             }
@@ -1985,10 +2003,17 @@ __global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
                 for (int u = 0; u < U; u++) x[u] = (j + u < r1) ? A.col[j + u] : -1;
 #pragma unroll
                 for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[la + (size_t)x[u]] : dl;   // dl: neither case below
-                if (MODE != 0 && d > 0) {
-                    uint64_t sv[U];
+                // path-count loads, then the discovery compare-and-swaps, then the sums:
+                // the swaps' round trip overlaps the loads' instead of following it
+                uint64_t sv[U];
 #pragma unroll
-                    for (int u = 0; u < U; u++) sv[u] = L[u] == dprev ? A.sig[la + (size_t)x[u]] : 0ULL;
+                for (int u = 0; u < U; u++)
+                    sv[u] = (MODE != 0 && d > 0 && L[u] == dprev) ? A.sig[la + (size_t)x[u]] : 0ULL;
+                bool has[U];
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    has[u] = L[u] == S_INF && atomicCAS(lv + la + (size_t)x[u], S_INF, dnext) == S_INF;
+                if (MODE != 0 && d > 0) {
 #pragma unroll
                     for (int u = 0; u < U; u++) {
                         if (L[u] != dprev) continue;
@@ -2001,10 +2026,6 @@ __global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
                         }
                     }
                 }
-                bool has[U];
-#pragma unroll
-                for (int u = 0; u < U; u++)
-                    has[u] = L[u] == S_INF && atomicCAS(lv + la + (size_t)x[u], S_INF, dnext) == S_INF;
                 j = min(j + U, r1);
 #pragma unroll
                 for (int u = 0; u < U; u++)

@@ -147,7 +147,7 @@ __global__ void degree_order_kernel(const int64_t* __restrict__ row, int32_t n, 
         if (row[v + 1] - row[v] > row[v] - row[v - 1]) *out = 1u;
 }
 
-// bc[v] = sum over lane groups of the per-group partials (fixed order).
+// bc[v] = sum of the per-32-lane partials, in lane order.
 __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, double* __restrict__ bc) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         double s = 0.0;
@@ -174,9 +174,9 @@ __global__ void lane_bc_reduce_kernel(KArgs A, int lanes) {
     }
 }
 
-// dst[g][v] += bcg[g][v] for every lane group whose destination is set.  One
-// thread per vertex walks the groups in order, so groups that share a
-// destination (one request spanning several groups) never race.
+// dst[p][v] += bcg[p][v] for every 32-lane partial p whose destination is set.
+// One thread per vertex walks the partials in order, so partials that share a
+// destination (one request spanning several of them) never race.
 __global__ void bc_scatter_kernel(const double* __restrict__ bcg, int ng, int n, double* const* __restrict__ dst) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         for (int g = 0; g < ng; g++) {
@@ -355,7 +355,8 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     if (need_bc) {
         sig_sz_ = cells * sizeof(uint64_t);
         rho_sz_ = cells * sizeof(double);
-        bcg_sz_ = (gs_ ? (size_t)ng_ : 1) * n * sizeof(double);   // one lane per task: one BC accumulator
+        // BC partials per 32 lanes (128-lane groups keep one per quarter); one lane per task: one accumulator
+        bcg_sz_ = (gs_ ? (size_t)(lanes / 32) : 1) * n * sizeof(double);
         ok &= dev_alloc((void**)&sig_, sig_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&rho_, rho_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&bcg_, bcg_sz_) == cudaSuccess;
@@ -461,14 +462,14 @@ gbc_status LaneEngine::bc_finish(double* d_bc) {
         GBC_CUDA(cudaMemcpyAsync(d_bc, bcg_, sizeof(double) * g_->n, cudaMemcpyDeviceToDevice, stream_));
         return GBC_OK;
     }
-    bc_reduce_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(bcg_, ng_, g_->n, d_bc);
+    bc_reduce_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(bcg_, lanes_ / 32, g_->n, d_bc);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
 }
 
 gbc_status LaneEngine::bc_scatter(double* const* d_dst) {
     if (gs_ == 0) { set_error("per-group BC partials need lane groups of 32 or 128"); return GBC_ERR_ARG; }
-    bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, ng_, g_->n, d_dst);
+    bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, lanes_ / 32, g_->n, d_dst);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
 }

@@ -8,10 +8,12 @@
 // launches.  Each registered graph keeps its CSR in HBM and, while it has
 // work, one lane engine sized to its pending sources.  A lane batch is filled
 // from every admitted request on one graph that wants the same kind of sweep
-// (closeness or betweenness), oldest first; a request takes whole lane groups
-// (128 lanes on small-world graphs, else 32, as graph handles choose them), so
-// its betweenness partials stay separate and are added into its own FP64
-// result vector after each batch.  Its sources run in level-profile order.
+// (closeness or betweenness), oldest first, in lane groups of 128 lanes on
+// small-world graphs, else 32, as graph handles choose them.  A request takes
+// whole 32-lane parts: the level kernels keep betweenness partials per 32
+// lanes for both group widths, so one 128-lane group can carry up to four
+// requests, and each request's partials are added into its own FP64 result
+// vector after each batch.  Its sources run in level-profile order.
 // Requests that arrive while a batch runs join the next batch.
 //
 // Device memory is admitted against one budget: a request is admitted, in
@@ -40,6 +42,10 @@
 using namespace gbc;
 
 namespace {
+constexpr int32_t PART = 32;   // lanes of one betweenness partial: a request's unit of a lane batch
+}
+
+namespace {
 
 double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -60,7 +66,11 @@ struct SGraph {
     // level-profile key of every internal id: a request's sources are sorted by
     // it, so that each 32-lane group holds sources whose BFS levels move together
     std::vector<uint32_t> key;
-    std::vector<int32_t> all_sorted;   // every caller id in that order (exact queries)
+    std::vector<int32_t> all_sorted;   // every caller id in that order (exact queries), isolated vertices last
+    size_t n_with_edges = 0;           // leading entries of all_sorted that have edges
+    // A source without edges (an isolated vertex) reaches nothing: it adds
+    // nothing to betweenness and its closeness sum is 0, so it takes no lane.
+    bool isolated(int32_t v) const { return g.comp_edges[g.comp[v]] == 0; }
     int32_t group = 32;          // lanes per lane group: 128 on small-world graphs, as on graph handles
     // device bytes of the narrowest lane engine this graph runs with
     size_t engine_floor() const { return LaneEngine::bytes_needed(g.n, group, true); }
@@ -81,7 +91,8 @@ struct Req {
     int32_t gid = 0;
     int32_t kind = GBC_Q_CC;
     gbc_options opt{};
-    std::vector<int32_t> src;
+    std::vector<int32_t> src;    // the sources, those with edges first (in run order), then any without
+    size_t nlane = 0;            // sources with edges: only these take lanes
     size_t next = 0;             // next source to hand out
     size_t done = 0;             // sources whose lanes finished
     int32_t state = GBC_REQ_QUEUED;
@@ -257,7 +268,7 @@ void gbc_server_s::run() {
                         it = fifo.erase(it);
                         continue;
                     }
-                    if (r->deadline > 0 && t > r->deadline && r->done < r->src.size()) {
+                    if (r->deadline > 0 && t > r->deadline && r->done < r->nlane) {
                         fail(*r, GBC_ERR_TIMEOUT, "deadline passed");
                         cv_done.notify_all();
                         it = fifo.erase(it);
@@ -270,7 +281,7 @@ void gbc_server_s::run() {
                 std::vector<bool> busy(graphs.size(), false);
                 for (int64_t id : fifo) {
                     Req* r = reqs[id].get();
-                    if (r->admitted && r->next < r->src.size()) busy[r->gid] = true;
+                    if (r->admitted && r->next < r->nlane) busy[r->gid] = true;
                 }
                 for (size_t k = 0; k < graphs.size(); k++) {
                     const int32_t cand = (int32_t)((rr + k) % graphs.size());
@@ -282,7 +293,7 @@ void gbc_server_s::run() {
                 int64_t pending = 0;
                 for (int64_t id : fifo) {
                     Req* r = reqs[id].get();
-                    if (r->gid == gi && r->admitted) pending += (int64_t)(r->src.size() - r->next);
+                    if (r->gid == gi && r->admitted) pending += (int64_t)(r->nlane - r->next);
                 }
                 gbc_status st = ensure_engine(this, gi, busy, pending);
                 if (st != GBC_OK) {
@@ -295,24 +306,23 @@ void gbc_server_s::run() {
                     continue;
                 }
                 lanes = graphs[gi]->lanes;
-                const int32_t grp = graphs[gi]->group;
-                // fill the batch: oldest request's kind, whole lane groups per request
+                // fill the batch: oldest request's kind, whole 32-lane parts per request
                 kind = -1;
                 int32_t used = 0;
                 for (int64_t id : fifo) {
                     Req* r = reqs[id].get();
-                    if (r->gid != gi || !r->admitted || r->next >= r->src.size()) continue;
+                    if (r->gid != gi || !r->admitted || r->next >= r->nlane) continue;
                     // requests share a batch only when they need the same sweep
                     const int32_t rk = r->bc() ? 1 + r->opt.semantics * 2 + (r->opt.delta_precision == GBC_DELTA_F64) : 0;
                     if (kind < 0) kind = rk;
                     if (rk != kind) continue;
                     const int32_t room = lanes - used;
-                    if (room < grp) break;
-                    const int32_t take = (int32_t)std::min<size_t>(room, r->src.size() - r->next);
+                    if (room < PART) break;
+                    const int32_t take = (int32_t)std::min<size_t>(room, r->nlane - r->next);
                     slots.push_back({r, r->next, take, used});
                     r->next += take;
                     r->inflight++;
-                    used += ((take + grp - 1) / grp) * grp;
+                    used += ((take + PART - 1) / PART) * PART;
                 }
                 Gp = graphs[gi].get();
                 Gp->running = true;
@@ -324,9 +334,9 @@ void gbc_server_s::run() {
         SGraph& G = *Gp;
         cudaStream_t stream = G.stream;
         const int32_t grp = G.group;
-        const int32_t ng = lanes / grp;
+        const int32_t np = lanes / PART;
         hsrc.assign(lanes, -1);
-        hdst.assign(ng, nullptr);
+        hdst.assign(np, nullptr);
         int32_t kb = 0;
         const bool bc_batch = kind > 0;
         gbc_status st = GBC_OK;
@@ -350,7 +360,7 @@ void gbc_server_s::run() {
         }
         for (auto& sl : slots) {
             for (int32_t i = 0; i < sl.count; i++) hsrc[sl.lane0 + i] = G.h_inv[sl.r->src[sl.first + i]];
-            for (int32_t gg = sl.lane0 / grp; gg < (sl.lane0 + sl.count + grp - 1) / grp; gg++) hdst[gg] = sl.r->d_bc;
+            for (int32_t p = sl.lane0 / PART; p < (sl.lane0 + sl.count + PART - 1) / PART; p++) hdst[p] = sl.r->d_bc;
             kb = std::max(kb, ((sl.lane0 + sl.count + grp - 1) / grp) * grp);
         }
         if (st == GBC_OK &&
@@ -361,7 +371,7 @@ void gbc_server_s::run() {
         }
         LaneResult res;
         if (st == GBC_OK && bc_batch) {
-            if (cudaMemcpyAsync(G.d_dst, hdst.data(), sizeof(double*) * ng, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+            if (cudaMemcpyAsync(G.d_dst, hdst.data(), sizeof(double*) * np, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
                 cudaGetLastError();
                 st = GBC_ERR_CUDA;
             }
@@ -410,7 +420,7 @@ void gbc_server_s::run() {
                     if (!bc_batch) r->cc[v] = (int64_t)hcc[sl.lane0 + i];
                 }
                 r->done += sl.count;
-                if (r->done == r->src.size()) {
+                if (r->done == r->nlane) {
                     r->state = GBC_REQ_DONE;
                     r->t_done = now_ms();
                     completed++;
@@ -490,13 +500,6 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     int32_t depth = 0;
     GBC_TRY(level_profile_key(G->g, G->stream, G->key, depth));
     G->group = (depth > 0 && depth <= SMALL_WORLD_DEPTH && s->max_lanes % 128 == 0) ? 128 : 32;
-    G->all_sorted.resize(n);
-    for (int32_t i = 0; i < n; i++) G->all_sorted[i] = i;
-    {
-        const SGraph* SG = G.get();
-        std::stable_sort(G->all_sorted.begin(), G->all_sorted.end(),
-                         [SG](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
-    }
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
@@ -506,6 +509,17 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     G->g.comp_edges.assign(nc, 0);
     for (int32_t v = 0; v < n; v++) G->g.comp_edges[G->g.comp[v]] += row[v + 1] - row[v];
     for (auto& e : G->g.comp_edges) e /= 2;
+    G->all_sorted.resize(n);
+    for (int32_t i = 0; i < n; i++) G->all_sorted[i] = i;
+    {
+        const SGraph* SG = G.get();
+        std::stable_sort(G->all_sorted.begin(), G->all_sorted.end(), [SG](int32_t a, int32_t b) {
+            const bool ia = SG->isolated(a), ib = SG->isolated(b);
+            return ia != ib ? ib : SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]];
+        });
+        G->n_with_edges = 0;
+        while (G->n_with_edges < (size_t)n && !SG->isolated(G->all_sorted[G->n_with_edges])) G->n_with_edges++;
+    }
     std::lock_guard<std::mutex> lk(s->mu);
     *gid = (int32_t)s->graphs.size();
     s->graphs.push_back(std::move(G));
@@ -536,10 +550,14 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
         Rng rng(seed, 17);
         r->src.resize(k);
         for (int32_t i = 0; i < k; i++) r->src[i] = (int32_t)rng.below((uint64_t)n);
-        std::stable_sort(r->src.begin(), r->src.end(),
-                         [&](int32_t a, int32_t b) { return SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]]; });
+        std::stable_sort(r->src.begin(), r->src.end(), [&](int32_t a, int32_t b) {
+            const bool ia = SG->isolated(a), ib = SG->isolated(b);
+            return ia != ib ? ib : SG->key[SG->h_inv[a]] < SG->key[SG->h_inv[b]];
+        });
+        while (r->nlane < r->src.size() && !SG->isolated(r->src[r->nlane])) r->nlane++;
     } else {
         r->src = SG->all_sorted;
+        r->nlane = SG->n_with_edges;
     }
     if (r->bc()) r->res_bytes = sizeof(double) * (size_t)n;
     else r->cc.assign(n, 0);
@@ -548,6 +566,14 @@ gbc_status gbc_server_submit(gbc_server s, int32_t gid, int32_t kind, int32_t k,
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = s->next_id++;
     *req_id = r->id;
+    if (r->nlane == 0) {   // nothing to run: a zero result, done at once
+        r->state = GBC_REQ_DONE;
+        r->t_done = r->t_submit;
+        s->completed++;
+        s->reqs[r->id] = std::move(r);
+        s->cv_done.notify_all();
+        return GBC_OK;
+    }
     s->fifo.push_back(r->id);
     s->reqs[r->id] = std::move(r);
     s->cv_work.notify_all();
@@ -619,7 +645,9 @@ gbc_status gbc_server_fetch(gbc_server s, int64_t id, double* bc, int64_t* cc, d
         n = s->graphs[r->gid]->g.n;
     }
     if (latency_ms) *latency_ms = r->t_done - r->t_submit;
-    if (r->bc() && bc) {
+    if (r->bc() && bc && !r->d_bc) {   // no source with edges: every value is 0
+        std::memset(bc, 0, sizeof(double) * (size_t)n);
+    } else if (r->bc() && bc) {
         // the result accumulated in internal ids: gather to the caller's, through a scratch vector
         double* tmp = nullptr;
         const size_t bytes = sizeof(double) * (size_t)n;

@@ -26,6 +26,9 @@ component / time.
   cpu_baseline : the oracle's FP64 Brandes with all host threads on a
           bounded sample of the same sources.
   clocks : SM clocks and throttle reasons sampled during the timed region.
+  serving : the serving mix over 64 resident graphs (rates, saturation), and
+          bench_graph: k=1024 / k=64 sampled-BC queries served on the R-MAT
+          s22 graph itself, delivered GTEPS beside the plain engine's.
   ba_all_sources / reduction / deep_grid : the other single-GPU
           configurations in short form -- BA n=4096 m=4 with every vertex a
           source (FP64 delta betweenness and closeness, with rooflines); the
@@ -80,8 +83,12 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     p.add_argument("--serve-rates", default="5,10,20,40", help="query arrival rates per second, comma-separated")
     p.add_argument("--serve-burst", type=int, default=96, help="queries submitted at once for the saturation point")
-    p.add_argument("--serve-workers", type=int, default=0, help="server worker threads (0: the library default, 4)")
+    p.add_argument("--serve-workers", type=int, default=0, help="server worker threads (0: the library default, 8)")
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--serve-graph-rate", type=float, default=6.0,
+                   help="query arrival rate of the serving stream on the benchmark graph itself")
+    p.add_argument("--serve-graph-burst", type=int, default=32,
+                   help="queries submitted at once on the benchmark graph (0: none)")
     p.add_argument("--no-reduction", action="store_true", help="skip the D1+AP reduction section (R-MAT s18 + pendant trees)")
     p.add_argument("--no-grid", action="store_true", help="skip the deep-grid section (1024^2 grid, 8192 sources)")
     p.add_argument("--grid-sources", type=int, default=8192, help="sources of the deep-grid section")
@@ -215,6 +222,49 @@ def cpu_baseline(csr, sample, n_src, threads):
     return dt
 
 
+def server_counters(G, L, h):
+    import ctypes as C
+    v = [C.c_int64() for _ in range(4)] + [C.c_double()]
+    G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
+    return [x.value for x in v]
+
+
+def serve_stream(G, L, h, draw, n_of, rate, seconds, count, rng):
+    """One arrival stream on a server: `count` queries at once (a burst), or
+    Poisson arrivals at `rate` per second for `seconds`.  Every query is waited
+    for and fetched; latencies are the server's submit-to-completion times.
+    draw() submits one query and returns (request id, graph index)."""
+    import ctypes as C
+    c0 = server_counters(G, L, h)
+    t0 = time.perf_counter()
+    t_end = t0 + seconds
+    reqs = [draw() for _ in range(count)] if count else []
+    while not count and time.perf_counter() < t_end:
+        reqs.append(draw())
+        time.sleep(rng.expovariate(rate))
+    lats = []
+    for rid, gi in reqs:
+        st = C.c_int32()
+        G.check(L.gbc_server_wait(h, rid, 600000.0, C.byref(st)))
+        n = n_of(gi)
+        bc = np.zeros(n)
+        cc = np.zeros(n, np.int64)
+        lat = C.c_double()
+        G.check(L.gbc_server_fetch(h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                                   C.byref(lat)))
+        lats.append(lat.value)
+    wall = time.perf_counter() - t0
+    c1 = server_counters(G, L, h)
+    lats = np.array(lats)
+    busy = c1[4] - c0[4]
+    return {"rate_per_s": rate if not count else "burst", "queries": len(lats),
+            "p50_ms": round(float(np.percentile(lats, 50)), 3),
+            "p99_ms": round(float(np.percentile(lats, 99)), 3), "wall_s": round(wall, 3),
+            "lane_batches": c1[1] - c0[1], "shared_batches": c1[2] - c0[2],
+            "gteps_delivered": round((c1[3] - c0[3]) / wall / 1e9, 3),
+            "busy_frac": round(busy * 1e-3 / wall, 3)}
+
+
 def serving(G, seconds, rates, burst=96, seed=11, workers=0):
     """The serving mix: a Poisson stream of queries over 64 device-resident
     graphs of 1K-2M vertices (BA m=2-8, Erdos-Renyi average degree 4-32,
@@ -255,11 +305,6 @@ def serving(G, seconds, rates, burst=96, seed=11, workers=0):
     rng = random.Random(seed)
     o = G.options()
 
-    def counters():
-        v = [C.c_int64() for _ in range(4)] + [C.c_double()]
-        G.check(L.gbc_server_counters(h, *[C.byref(x) for x in v]))
-        return [x.value for x in v]
-
     def draw():
         gi = rng.randrange(len(specs))
         n = specs[gi][1].n
@@ -276,46 +321,57 @@ def serving(G, seconds, rates, burst=96, seed=11, workers=0):
         G.check(L.gbc_server_submit(h, gids[gi], kind, k, rng.randrange(1 << 30), C.byref(o), 0.0, C.byref(rid)))
         return rid.value, gi
 
-    def stream(rate, count=0):
-        reqs = []
-        c0 = counters()
-        t0 = time.perf_counter()
-        t_end = t0 + seconds
-        if count:
-            reqs = [draw() for _ in range(count)]
-        while not count and time.perf_counter() < t_end:
-            reqs.append(draw())
-            time.sleep(rng.expovariate(rate))
-        lats = []
-        for rid, gi in reqs:
-            st = C.c_int32()
-            G.check(L.gbc_server_wait(h, rid, 600000.0, C.byref(st)))
-            n = specs[gi][1].n
-            bc = np.zeros(n)
-            cc = np.zeros(n, np.int64)
-            lat = C.c_double()
-            G.check(L.gbc_server_fetch(h, rid, bc.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
-                                       C.byref(lat)))
-            lats.append(lat.value)
-        wall = time.perf_counter() - t0
-        c1 = counters()
-        lats = np.array(lats)
-        busy = c1[4] - c0[4]
-        return {"rate_per_s": rate if not count else "burst", "queries": len(lats),
-                "p50_ms": round(float(np.percentile(lats, 50)), 3),
-                "p99_ms": round(float(np.percentile(lats, 99)), 3), "wall_s": round(wall, 3),
-                "lane_batches": c1[1] - c0[1], "shared_batches": c1[2] - c0[2],
-                "gteps_delivered": round((c1[3] - c0[3]) / wall / 1e9, 3),
-                "busy_frac": round(busy * 1e-3 / wall, 3)}
+    def n_of(gi):
+        return specs[gi][1].n
 
-    points = [stream(r) for r in rates]
-    sat = stream(0.0, count=burst) if burst else None
+    points = [serve_stream(G, L, h, draw, n_of, r, seconds, 0, rng) for r in rates]
+    sat = serve_stream(G, L, h, draw, n_of, 0.0, seconds, burst, rng) if burst else None
     L.gbc_server_destroy(h)
     return {"graphs": len(specs), "vertices": [min(c.n for _, c in specs), max(c.n for _, c in specs)],
             "directed_entries": int(sum(c.m for _, c in specs)), "workers": workers or 8, "points": points,
             "saturation": sat,
             "mix": "uniform over graphs: 15% exact CC (graphs <= 32K vertices), 10% exact BC (<= 16K), "
                    "40% k=64 and 35% k=1024 sampled BC"}
+
+
+def served_bench_graph(G, csr, seconds, rate, burst, plain_gteps, seed=23, workers=0):
+    """Serving on the benchmark graph itself (R-MAT s22 ef16, resident on a
+    server): sampled-BC queries of k = 1024 and k = 64 sources (half each,
+    drawn by the server uniformly over all vertices with the query's seed;
+    FP32 delta, Brandes semantics), first as a Poisson stream at `rate` per
+    second for `seconds`, then `burst` queries at once.  Delivered GTEPS is
+    the edges of the sources' components over the stream's wall time, set
+    beside the one-source-at-a-time engine's GTEPS on the same graph."""
+    import ctypes as C
+    import random
+    L = G.lib()
+    cfg = G.ServerConfig()
+    cfg.max_lanes = 1024
+    cfg.workers = workers
+    h = C.c_void_p()
+    G.check(L.gbc_server_create(C.byref(cfg), C.byref(h)))
+    gid = C.c_int32()
+    t0 = time.perf_counter()
+    G.check(L.gbc_server_add_graph(h, csr.row, csr.col, csr.n, C.byref(gid)))
+    add_s = time.perf_counter() - t0
+    rng = random.Random(seed)
+    o = G.options(delta_precision=G.DELTA_F32)
+
+    def draw():
+        k = 1024 if rng.random() < 0.5 else 64
+        rid = C.c_int64()
+        G.check(L.gbc_server_submit(h, gid.value, G.Q_BC_SAMPLED, k, rng.randrange(1 << 30), C.byref(o), 0.0,
+                                    C.byref(rid)))
+        return rid.value, 0
+
+    points = [serve_stream(G, L, h, draw, lambda gi: csr.n, rate, seconds, 0, rng)]
+    if burst:
+        points.append(serve_stream(G, L, h, draw, lambda gi: csr.n, 0.0, seconds, burst, rng))
+    L.gbc_server_destroy(h)
+    best = max(p["gteps_delivered"] for p in points)
+    return {"graph": "rmat22_ef16", "add_graph_s": round(add_s, 3), "queries": "50% k=1024, 50% k=64 sampled BC",
+            "points": points, "gteps_delivered_best": best,
+            "speedup_vs_plain": None if not plain_gteps else round(best / plain_gteps, 2)}
 
 
 def kernel_roofline(st, n, M, k, job, hbm, peak_kind):
@@ -703,6 +759,8 @@ def main():
         if not args.no_serve:
             serve = serving(G, args.serve_seconds, [float(x) for x in args.serve_rates.split(",")], args.serve_burst,
                             workers=args.serve_workers)
+            serve["bench_graph"] = served_bench_graph(G, csr, args.serve_seconds, args.serve_graph_rate,
+                                                      args.serve_graph_burst, plain_gteps, workers=args.serve_workers)
         c1 = None if args.no_ba else ba_section(G, hbm, peak_kind)
         red = None if args.no_reduction else reduction_section(G)
         deep = None if args.no_grid else grid_section(G, hbm, peak_kind, args.grid_sources)

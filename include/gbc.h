@@ -226,8 +226,9 @@ gbc_status gbc_sssp(gbc_graph g, const int32_t* sources, int32_t k, const gbc_op
  * device address; make that first call before any stream capture.  Every
  * call first checks the CSR on the device (row[0] == 0, rows non-decreasing,
  * col entries in [0,n)) and refuses a bad one with GBC_ERR_ARG before the BFS
- * touches the array.  Runs on `stream` (a cudaStream_t) and returns when the
- * results are written. */
+ * touches the array.  Runs on `stream` (a cudaStream_t): it waits for
+ * `stream` after the CSR check and after every BFS level, whose frontier size
+ * it reads back, and returns when the results are written. */
 #define GBC_NOALLOC_MAX_VERTICES (1 << 21)
 gbc_status gbc_cc_noalloc(const int64_t* d_row, const int32_t* d_col, int32_t n, const int32_t* d_sources,
                           int32_t k, int64_t* d_cc, void* stream);
@@ -373,8 +374,10 @@ gbc_status gbc_server_fetch(gbc_server s, int64_t req_id, double* bc, int64_t* c
 gbc_status gbc_server_cancel(gbc_server s, int64_t req_id);
 /* The source vertices of a request (the drawn sample for GBC_Q_BC_SAMPLED):
  * *k = count; out (may be NULL) receives them if cap >= count, in the order
- * the server runs them (grouped by BFS level profile, not the draw order).
- * Valid until the request is fetched. */
+ * the server runs them (grouped by BFS level profile, not the draw order),
+ * then the sources without edges: those reach nothing, add nothing to
+ * betweenness, have closeness sum 0, and take no lane.  Valid until the
+ * request is fetched. */
 gbc_status gbc_server_sources(gbc_server s, int64_t req_id, int32_t* out, int32_t cap, int32_t* k);
 /* Aggregate counters: completed requests, lane batches, shared batches
  * (batches that carried sources of more than one request), edges traversed. */

@@ -281,3 +281,93 @@ def test_worker_count(gpu, orc, graphs):
         assert np.array_equal(c8, c1)
     og = orc.Graph(graphs[1].row, graphs[1].col)
     assert np.array_equal(out[8][-1][1], orc.cc(og, np.arange(graphs[1].n)))
+
+
+def spread_over(gpu, csr, extra, seed):
+    """csr's vertices moved to random ids among csr.n + extra; the other ids are isolated."""
+    N = csr.n + extra
+    p = np.random.default_rng(seed).permutation(N)[:csr.n]
+    a = p[np.repeat(np.arange(csr.n), np.diff(csr.row))]
+    b = p[csr.col]
+    order = np.lexsort((b, a))
+    row = np.zeros(N + 1, np.int64)
+    np.add.at(row, a + 1, 1)
+    return gpu.CSR(np.cumsum(row), b[order].astype(np.int32))
+
+
+def test_isolated_sources_take_no_lane(gpu, orc):
+    """Sources without edges reach nothing: they are listed after the others,
+    take no lane, and the results still equal the oracle over every source.
+    A request whose sources are all isolated completes at submission with a
+    zero result."""
+    g = spread_over(gpu, gpu.gen_ba(600, 3, 8), 424, 2)
+    iso = np.nonzero(np.diff(g.row) == 0)[0]
+    assert len(iso) == 424
+    og = orc.Graph(g.row, g.col)
+    S = Server(gpu, max_lanes=128)
+    gid = S.add(g)
+    r_cc = S.submit(gid, gpu.Q_CC)
+    r_bc = S.submit(gid, gpu.Q_BC)
+    r_s = S.submit(gid, gpu.Q_BC_SAMPLED, 300, 5)
+    src = S.sources(r_s)
+    assert len(src) == 300 and len(S.sources(r_bc)) == g.n
+    flag = np.isin(src, iso)
+    k_edge = int((~flag).sum())
+    assert 0 < k_edge < 300 and not flag[:k_edge].any() and flag[k_edge:].all()
+    for r in (r_cc, r_bc, r_s):
+        assert S.wait(r) == gpu.REQ_DONE
+    c = S.counters()
+    # exact requests run the 600 vertices with edges in 128-lane batches (8 each if the 424
+    # isolated ones took lanes), the sample its k_edge sources
+    assert c["batches"] <= 2 * 5 + (k_edge + 127) // 128
+    st, _, cc, _ = S.fetch(r_cc, gid)
+    assert st == 0 and np.array_equal(cc, orc.cc(og, np.arange(g.n)))
+    st, bc, _, _ = S.fetch(r_bc, gid)
+    ref, _ = orc.bc(og, np.arange(g.n), nthreads=8)
+    assert st == 0 and relerr(bc, ref) < TOL
+    st, bs, _, _ = S.fetch(r_s, gid)
+    ref, _ = orc.bc(og, src, nthreads=8)
+    assert st == 0 and relerr(bs, ref) < TOL
+    S.close()
+    # one edge among 1000 vertices: a one-source sample almost surely draws an isolated vertex
+    two = spread_over(gpu, gpu.CSR(np.array([0, 1, 2], np.int64), np.array([1, 0], np.int32)), 998, 3)
+    S = Server(gpu)
+    gid = S.add(two)
+    hit = 0
+    for seed in range(1, 6):
+        r = S.submit(gid, gpu.Q_BC_SAMPLED, 1, seed)
+        if np.diff(two.row)[S.sources(r)[0]] == 0:
+            st = C.c_int32()
+            S.g.check(S.L.gbc_server_poll(S.h, r, C.byref(st)))
+            assert st.value == gpu.REQ_DONE
+            hit += 1
+        assert S.wait(r) == gpu.REQ_DONE
+        st, bc, _, _ = S.fetch(r, gid)
+        assert st == 0 and not bc.any()
+    assert hit > 0
+    assert S.counters()["batches"] == 5 - hit
+    S.close()
+
+
+def test_requests_share_a_lane_group(gpu, orc):
+    """On a small-world graph (128-lane groups) requests take 32-lane parts
+    of a group: eight 32-source requests need two 128-lane batches (eight if
+    each took a whole group), and each result equals a graph handle's
+    betweenness over that request's own sources."""
+    g = gpu.gen_ba(3000, 4, 12)
+    S = Server(gpu, max_lanes=128, workers=1)
+    gid = S.add(g)
+    rids = [S.submit(gid, gpu.Q_BC_SAMPLED, 32, 900 + i) for i in range(8)]
+    for r in rids:
+        assert S.wait(r) == gpu.REQ_DONE
+    c = S.counters()
+    assert c["batches"] <= 4, c
+    srcs = [S.sources(r) for r in rids]
+    res = [S.fetch(r, gid) for r in rids]
+    S.close()
+    with gpu.Graph(g) as h:
+        for src, (st, bc, _, _) in zip(srcs, res):
+            assert st == 0 and len(src) == 32
+            assert relerr(bc, h.bc(src)) < TOL
+    ref, _ = orc.bc(orc.Graph(g.row, g.col), srcs[3], nthreads=8)
+    assert relerr(res[3][1], ref) < TOL
