@@ -396,9 +396,10 @@ static void map_sources(const gbc_graph_s* G, std::vector<int32_t>& hsrc) {
     for (auto& x : hsrc) x = G->h_inv[x];
 }
 
-// After the CSR is on the device: degree relabelling and the id maps.
+// After the CSR is on the device: relabelling (degree order, or Cuthill-McKee
+// on deep graphs of low degree) and the id maps.
 static gbc_status finish_graph(gbc_graph_s* G) {
-    GBC_TRY(relabel_by_degree(G->g, G->stream, &G->d_order, &G->d_inv));
+    GBC_TRY(relabel_graph(G->g, G->stream, &G->d_order, &G->d_inv, nullptr));
     G->h_inv.resize(G->g.n);
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * G->g.n, cudaMemcpyDeviceToHost));
     return GBC_OK;

@@ -381,8 +381,8 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
         GBC_CUDA(cudaMemcpyAsync(&unsorted, ovf_ + 1, sizeof unsorted, cudaMemcpyDeviceToHost, stream_));
         GBC_CUDA(cudaStreamSynchronize(stream_));
         n_hubs_ = nh;
-        // ids in descending degree order (every device graph of this library): hub <=> id < n_hubs_
-        hub_lim_ = unsorted ? -1 : (int)nh;
+        // ids in descending degree order (graphs with hubs): hub <=> id < n_hubs_; no hubs: none
+        hub_lim_ = (unsorted && nh > 0) ? -1 : (int)nh;
     }
     GBC_TRY(alloc_queue(gs_ == 0 ? (unsigned long long)lanes * n + (1ULL << 16) : (unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));

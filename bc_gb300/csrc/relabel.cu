@@ -10,7 +10,20 @@
 // frontier work (the neighbour tie-break adds about 3%).  The caller keeps
 // original ids: the library maps sources in and per-vertex results out
 // (order[] / inv[]).
+//
+// Deep graphs of low degree (meshes, grids, road-like graphs: maximum degree
+// at most 64, a BFS deeper than 32 levels) have no hubs to gather; there the
+// ids follow a Cuthill-McKee order instead (relabel_graph): per component a
+// BFS from a far vertex, so that a vertex's neighbours sit in the BFS levels
+// next to its own and a BFS wavefront of one source walks along consecutive
+// ids.  A lane's level / path-count row then shares its cache lines between
+// neighbouring frontier entries: on the 1024^2 grid with 1024 one-lane tasks
+// a batch took 181 + 149 ms (forward + sweep) against 207 + 192 ms in degree
+// order, and the cache-line footprint of a level fits L2 better.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
 
 #include <cub/cub.cuh>
 
@@ -172,6 +185,167 @@ gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order_out,
     *d_order_out = order;
     *d_inv_out = inv;
     cleanup(true);
+    return GBC_OK;
+}
+
+namespace {
+
+// inv[order[i]] = i; ndeg[i] = degree of new vertex i (from the old rows)
+__global__ void inverse_row_kernel(const int64_t* __restrict__ row, const int32_t* __restrict__ order, int32_t n,
+                                   int32_t* __restrict__ inv, int32_t* __restrict__ ndeg) {
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int32_t o = order[i];
+        inv[o] = i;
+        ndeg[i] = (int32_t)(row[o + 1] - row[o]);
+    }
+}
+
+// Cuthill-McKee order of a host CSR: components in order of their smallest
+// vertex; in each, a BFS from the vertex a BFS from that smallest vertex
+// reached last (a far, pseudo-peripheral vertex), neighbours in row order.
+// order[new] = old.  Returns the most levels any of these BFS had.
+int32_t cuthill_mckee(const std::vector<int64_t>& row, const std::vector<int32_t>& col, int32_t n,
+                      std::vector<int32_t>& order) {
+    std::vector<int32_t> lev(n, -1), probe(n, -1), q(n);
+    order.clear();
+    order.reserve(n);
+    int32_t depth = 0;
+    for (int32_t s0 = 0; s0 < n; s0++) {
+        if (lev[s0] >= 0) continue;
+        // probe BFS from s0: its last vertex is the start
+        int32_t head = 0, tail = 0;
+        q[tail++] = s0;
+        probe[s0] = s0;
+        while (head < tail) {
+            const int32_t v = q[head++];
+            for (int64_t j = row[v]; j < row[v + 1]; j++) {
+                const int32_t x = col[j];
+                if (probe[x] != s0) { probe[x] = s0; q[tail++] = x; }
+            }
+        }
+        const int32_t a = q[tail - 1];
+        head = 0;
+        tail = 0;
+        q[tail++] = a;
+        lev[a] = 0;
+        while (head < tail) {
+            const int32_t v = q[head++];
+            order.push_back(v);
+            depth = std::max(depth, lev[v] + 1);
+            for (int64_t j = row[v]; j < row[v + 1]; j++) {
+                const int32_t x = col[j];
+                if (lev[x] < 0) { lev[x] = lev[v] + 1; q[tail++] = x; }
+            }
+        }
+    }
+    return depth;
+}
+
+}  // namespace
+
+// Rewrite g's rows in the ids of `order` (device, order[new] = old; the
+// function takes it over and hands it back as *d_order_out).
+static gbc_status apply_order(DevGraph& g, cudaStream_t s, int32_t* order, int32_t** d_order_out, int32_t** d_inv_out) {
+    const int32_t n = g.n;
+    const int64_t M = g.m;
+    int32_t *inv = nullptr, *ndeg = nullptr, *off32 = nullptr, *ncol = nullptr, *ncol2 = nullptr;
+    int64_t* nrow = nullptr;
+    void* tmp = nullptr;
+    const size_t sn = sizeof(int32_t) * (size_t)n, srow = sizeof(int64_t) * ((size_t)n + 1),
+                 scol = sizeof(int32_t) * std::max<int64_t>(M, 1);
+    size_t stmp = 0;
+    auto cleanup = [&](bool keep) {
+        cudaStreamSynchronize(s);
+        dev_release(ndeg, sn); dev_release(off32, sn); dev_release(tmp, stmp);
+        if (!keep) {
+            dev_release(order, sn); dev_release(inv, sn); dev_release(nrow, srow);
+            dev_release(ncol, scol); dev_release(ncol2, scol);
+        }
+    };
+    bool ok = true;
+    ok &= dev_alloc((void**)&inv, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&ndeg, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&off32, sn) == cudaSuccess;
+    ok &= dev_alloc((void**)&nrow, srow) == cudaSuccess;
+    ok &= dev_alloc((void**)&ncol, scol) == cudaSuccess;
+    ok &= dev_alloc((void**)&ncol2, scol) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cleanup(false);
+        set_error("relabel buffers (n=%d, m=%lld)", n, (long long)M);
+        return GBC_ERR_NOMEM;
+    }
+    int dev = 0, sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    size_t tb2 = 0, tb3 = 0;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, tb2, ndeg, off32, n, s);
+    if (e == cudaSuccess) e = cub::DeviceSegmentedSort::SortKeys(nullptr, tb3, ncol, ncol2, M, n, nrow, nrow + 1, s);
+    stmp = std::max(tb2, tb3) + 16;
+    if (e == cudaSuccess) e = dev_alloc(&tmp, stmp);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cleanup(false);
+        set_error("relabel workspace: %s", cudaGetErrorString(e));
+        return GBC_ERR_NOMEM;
+    }
+    const int grid = sm * 8;
+    inverse_row_kernel<<<grid, 256, 0, s>>>(g.row, order, n, inv, ndeg);
+    e = cub::DeviceScan::ExclusiveSum(tmp, tb2, ndeg, off32, n, s);
+    if (e == cudaSuccess) {
+        widen_kernel<<<grid, 256, 0, s>>>(off32, n, M, nrow);
+        fill_kernel<<<grid, 256, 0, s>>>(g.row, g.col, order, inv, nrow, n, ncol);
+        if (M > 0) e = cub::DeviceSegmentedSort::SortKeys(tmp, tb3, ncol, ncol2, M, n, nrow, nrow + 1, s);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cleanup(false);
+        set_error("relabel failed: %s", cudaGetErrorString(e));
+        return GBC_ERR_CUDA;
+    }
+    dev_release(g.row, srow);
+    dev_release(g.col, scol);
+    dev_release(ncol, scol);
+    ncol = nullptr;
+    g.row = nrow;
+    g.col = ncol2;
+    *d_order_out = order;
+    *d_inv_out = inv;
+    cleanup(true);
+    return GBC_OK;
+}
+
+gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order_out, int32_t** d_inv_out, bool* locality) {
+    if (locality) *locality = false;
+    const int32_t n = g.n;
+    if (n >= LOCALITY_MAX_N || g.m == 0) return relabel_by_degree(g, s, d_order_out, d_inv_out);
+    std::vector<int64_t> row((size_t)n + 1);
+    GBC_CUDA(cudaMemcpyAsync(row.data(), g.row, sizeof(int64_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    int64_t md = 0;
+    for (int32_t v = 0; v < n; v++) md = std::max<int64_t>(md, row[v + 1] - row[v]);
+    if (md > LOCALITY_MAX_DEGREE) return relabel_by_degree(g, s, d_order_out, d_inv_out);
+    std::vector<int32_t> col((size_t)g.m), order;
+    GBC_CUDA(cudaMemcpyAsync(col.data(), g.col, sizeof(int32_t) * (size_t)g.m, cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    if (cuthill_mckee(row, col, n, order) <= LOCALITY_MIN_DEPTH) return relabel_by_degree(g, s, d_order_out, d_inv_out);
+    int32_t* d_order = nullptr;
+    if (dev_alloc((void**)&d_order, sizeof(int32_t) * (size_t)n) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("relabel order buffer");
+        return GBC_ERR_NOMEM;
+    }
+    if (cudaMemcpyAsync(d_order, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        dev_release(d_order, sizeof(int32_t) * (size_t)n);
+        set_error("relabel order upload failed");
+        return GBC_ERR_CUDA;
+    }
+    GBC_TRY(apply_order(g, s, d_order, d_order_out, d_inv_out));
+    if (locality) *locality = true;
     return GBC_OK;
 }
 
