@@ -285,6 +285,23 @@ __device__ __forceinline__ void stage_flush(const KArgs& A, Stage& S) {
     S.cnt = 0;
 }
 
+// Start of the next FETCH regular entries of level d for this warp (e: the
+// level's end).  The first round is assigned statically -- warp w of the grid
+// takes the entries at foff[d] + w*FETCH -- so a level with fewer entries than
+// the grid has threads costs no atomic on the level counter, and a large one
+// one atomic fewer per warp; later rounds take FETCH at a time from the
+// counter (which starts at foff[d]) past that static region.
+__device__ __forceinline__ unsigned long long warp_fetch(const KArgs& A, int d, bool& first) {
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    if (first) {
+        first = false;
+        return A.foff[d] + ((unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * FETCH;
+    }
+    unsigned long long base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH) + warps * FETCH;
+    return __shfl_sync(FULL, base, 0);
+}
+
 // Neighbour visits counted by the threads of a warp, added to the control block.
 __device__ __forceinline__ void add_visits(const KArgs& A, unsigned long long vis) {
 #pragma unroll
@@ -894,10 +911,9 @@ __global__ void __launch_bounds__(NT, (MINB<LT, MODE == 2, NT>)) expand_kernel(K
         // regular entries: a warp takes FETCH per fetch; light ones are expanded
         // one per thread, the others by the whole warp in turn
         const unsigned long long e = A.foff[d + 1];
+        bool first = true;
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
-            base = __shfl_sync(FULL, base, 0);
+            const unsigned long long base = warp_fetch(A, d, first);
             if (base >= e) break;
             uint32_t ent;
             unsigned am;
@@ -1120,10 +1136,9 @@ __global__ void __launch_bounds__(NT, 4 * 256 / NT) backward_kernel(KArgs A) {
             __syncthreads();
         }
         const unsigned long long e = A.foff[d + 1];
+        bool first = true;
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
-            base = __shfl_sync(FULL, base, 0);
+            const unsigned long long base = warp_fetch(A, d, first);
             if (base >= e) break;
             uint32_t ent;
             unsigned am;
@@ -1974,10 +1989,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
         const uint16_t dprev = (uint16_t)(d - 1), dnext = (uint16_t)(d + 1), dl = (uint16_t)d;
         uint16_t* lv = reinterpret_cast<uint16_t*>(A.lvl);
         const unsigned long long e = A.foff[d + 1];
+        bool first = true;
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
-            base = __shfl_sync(FULL, base, 0);
+            const unsigned long long base = warp_fetch(A, d, first);
             if (base >= e) break;
             const bool act = base + t < e;
             const uint32_t ent = act ? A.fq[base + t] : 0u;
@@ -2062,10 +2076,9 @@ __global__ void __launch_bounds__(NT, 1024 / NT) backward_s_kernel(KArgs A) {
         const uint16_t* lv = reinterpret_cast<const uint16_t*>(A.lvl);
         const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
         const unsigned long long e = A.foff[d + 1];
+        bool first = true;
         for (;;) {
-            unsigned long long base = 0;
-            if (t == 0) base = atomicAdd(&A.ctl->next, (unsigned long long)FETCH);
-            base = __shfl_sync(FULL, base, 0);
+            const unsigned long long base = warp_fetch(A, d, first);
             if (base >= e) break;
             if (base + t < e) {   // the last fetch of a level may leave threads without an entry
                 const uint32_t ent = A.fq[base + t];
