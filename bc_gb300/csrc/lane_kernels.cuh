@@ -1324,7 +1324,8 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                     }
                 }
             }
-            // discovery: store d+1 in the unreached active lanes
+            // discovery: store d+1 in the unreached active lanes; bit i of mine: neighbour k0+i had one
+            unsigned mine = 0;
 #pragma unroll
             for (int i = 0; i < Q_ITER; i++) {
                 const bool inr = k0 + i < cnt;
@@ -1334,9 +1335,10 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
 #pragma unroll
                     for (int j = 0; j < 4; j++)
                         if ((un >> j) & 1u) px[j] = (LT)(d + 1);
+                    mine |= 1u << i;
                 }
-                if (__ballot_sync(FULL, un != 0u)) want |= 1u << (k0 + i);
             }
+            want |= __reduce_or_sync(FULL, mine) << k0;
         }
         // claims of the whole 32-neighbour chunk at once: thread k claims its own
         // column xm, so one claim round trip serves up to 32 neighbours
@@ -1712,6 +1714,7 @@ __device__ __forceinline__ void q_bwd_scan(const KArgs& A, int d, size_t gbase, 
                                            const T (&mv)[4], const int (&ev)[4], long long r0, long long r1, int sub,
                                            int nsub, int xm0, Sum<T> (&acc)[4], int (&pc)[4]) {
     const int t = threadIdx.x & 31;
+    const bool refsem = A.semantics == GBC_BC_REFERENCE;   // predecessor counts: the reference semantics only
     int xm = xm0;   // columns of the chunk at r0 + 32*sub
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub, xm = xm0) {
         const int cnt = (int)min(32LL, r1 - jb);
@@ -1728,9 +1731,11 @@ __device__ __forceinline__ void q_bwd_scan(const KArgs& A, int d, size_t gbase, 
             for (int i = 0; i < Q_ITER; i++) {
                 if (k0 + i >= cnt) continue;
                 const unsigned sm = q[i].eq(d + 1) & act4;
-                const unsigned pm = q[i].eq(d - 1) & act4;
+                if (refsem) {
+                    const unsigned pm = q[i].eq(d - 1) & act4;
 #pragma unroll
-                for (int j = 0; j < 4; j++) pc[j] += (pm >> j) & 1u;
+                    for (int j = 0; j < 4; j++) pc[j] += (pm >> j) & 1u;
+                }
                 if (!sm) continue;
                 const size_t xo = ((gbase + (size_t)xs[i]) << 7) + 4 * t;
                 if (WIDE) {
@@ -1769,6 +1774,7 @@ __device__ __forceinline__ void q_bwd_edges(const KArgs& A, int d, size_t gbase,
                                             const T (&mv)[4], const int (&ev)[4], long long r0, long long r1, int sub,
                                             int nsub, Sum<T> (&acc)[4], int (&pc)[4]) {
     const int t = threadIdx.x & 31;
+    const bool refsem = A.semantics == GBC_BC_REFERENCE;
     const LT dprev = (LT)(d - 1), dnext = (LT)(d + 1);
     const T* rho = reinterpret_cast<const T*>(A.rho);
     const uint64_t* rw = reinterpret_cast<const uint64_t*>(A.rho);
@@ -1800,7 +1806,7 @@ __device__ __forceinline__ void q_bwd_edges(const KArgs& A, int d, size_t gbase,
             for (int off = 16; off > 0; off >>= 1) {
                 const T s2 = __shfl_xor_sync(FULL, ps.s, off), c2 = __shfl_xor_sync(FULL, ps.c, off);
                 ps.merge(s2, c2);
-                ppc += __shfl_xor_sync(FULL, ppc, off);
+                if (refsem) ppc += __shfl_xor_sync(FULL, ppc, off);
             }
             if (t == o) {
                 acc[j].merge(ps.s, ps.c);
