@@ -236,16 +236,21 @@ __device__ __forceinline__ T wterm(T mv, int ev, uint64_t r) {
     return pow2s(mv * wmant<T>(r), ev + wexp(r));
 }
 
-// Running sum of the dependency sweep: compensated (Neumaier) in FP32, so a
+// Running sum of the dependency sweep: compensated (Kahan) in FP32, so a
 // hub's sum over thousands of successor terms keeps FP32-ulp accuracy instead
-// of losing ~sqrt(terms) ulps; plain in FP64.
+// of losing ~sqrt(terms) ulps; plain in FP64.  The terms are non-negative, and
+// Kahan's recurrence bounds the error by (2u + O(n u^2)) times the sum of the
+// terms' magnitudes in any order, so it needs no magnitude test (Neumaier's
+// variant, which also handles cancelling terms, costs twice the instructions
+// per term).  c holds the part of the sum not yet in s: the value is s + c.
 template <typename T>
 struct Sum {
     T s = T(0), c = T(0);
     __device__ __forceinline__ void add(T x) {
         if (sizeof(T) == 4) {
-            const T t = s + x;
-            c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+            const T y = x + c;
+            const T t = s + y;
+            c = y - (t - s);
             s = t;
         } else {
             s += x;
@@ -620,9 +625,11 @@ __device__ __forceinline__ void bwd_lanes(const KArgs& A, int d, size_t gbase, c
         for (int k = 0; k < ITER; k++) {
             if (k >= kmax) break;
             const unsigned sm = Sd::eq(Lw[k], dn4) & act4;
-            const unsigned pm = Sd::eq(Lw[k], dp4) & act4;
+            if (A.semantics == GBC_BC_REFERENCE) {   // predecessor counts: the reference semantics only
+                const unsigned pm = Sd::eq(Lw[k], dp4) & act4;
 #pragma unroll
-            for (int j = 0; j < LPW; j++) pcs[j] += Sd::has(pm, j);
+                for (int j = 0; j < LPW; j++) pcs[j] += Sd::has(pm, j);
+            }
             if (!sm) continue;
             const size_t xo = (size_t)xs[k] << 5;
             if (!WIDE && sizeof(T) == 4 && LPW == 4) {
