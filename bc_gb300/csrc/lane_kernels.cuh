@@ -1207,9 +1207,16 @@ template <> struct Quad<uint8_t> {
     }
     __device__ static __forceinline__ Quad none() { return {0xFFFFFFFFu}; }
     __device__ static __forceinline__ unsigned bits(unsigned m) { return ((m & 0x80808080u) * 0x00204081u) >> 28; }
-    __device__ __forceinline__ unsigned eq(int d) const { return bits(__vcmpeq4(w, Simd<uint8_t>::bc(d))); }
+    // 0x80 in every zero byte of x, 0 elsewhere: the masked add cannot carry
+    // across bytes, so each byte's result is exact
+    __device__ static __forceinline__ unsigned zero_bytes(unsigned x) {
+        return ~(((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x) & 0x80808080u;
+    }
+    __device__ __forceinline__ unsigned eq(int d) const {
+        return (zero_bytes(w ^ Simd<uint8_t>::bc(d)) * 0x00204081u) >> 28;
+    }
     __device__ __forceinline__ unsigned gt(int d) const { return bits(__vcmpgtu4(w, Simd<uint8_t>::bc(d))); }
-    __device__ __forceinline__ unsigned unreached() const { return bits(__vcmpeq4(w, 0xFFFFFFFFu)); }
+    __device__ __forceinline__ unsigned unreached() const { return (zero_bytes(~w) * 0x00204081u) >> 28; }
 };
 template <> struct Quad<uint16_t> {
     uint2 w;

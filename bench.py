@@ -396,7 +396,8 @@ def kernel_roofline(st, n, M, k, job, hbm, peak_kind):
     return {"bound": "hbm", "levels": name, "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
             "frac": round(ach / hbm, 5), "traffic": None, "peak_kind": peak_kind,
             "alg_bytes_per_launch": int(nb / max(launches, 1)), "avg_launch_ms": round(ms / max(launches, 1), 4),
-            "kernel": ("expand" if name == "forward" else "backward") + ("_q" if st["group_lanes"] == 128 else "") + "_kernel"}
+            "kernel": ("expand" if name == "forward" else "backward")
+                      + {128: "_q", 1: "_s"}.get(int(st["group_lanes"]), "") + "_kernel"}
 
 
 def ba_section(G, hbm, peak_kind):
@@ -658,7 +659,7 @@ def main():
     fwd_bytes = (adj + 16 * B * n) * args.steps
     bwd_bytes = (adj + 16 * B * n + 16 * n) * args.steps
     fwd_dom = fwd_ms >= bwd_ms
-    q = "_q" if group == 128 else ""   # the 128-lane-group kernels
+    q = {128: "_q", 1: "_s"}.get(int(group), "")   # the 128-lane-group / one-lane kernels
     dom = ("expand" if fwd_dom else "backward") + q + "_kernel"
     dom_ms, dom_bytes, dom_k = (fwd_ms, fwd_bytes, fwd_k) if fwd_dom else (bwd_ms, bwd_bytes, bwd_k)
     hbm, peak_kind = peaks()
