@@ -234,13 +234,18 @@ static gbc_status check_weighted(const gbc_graph_s* G, const gbc_options& o, boo
 // Lanes per group of a call: the option, else the tuned value, else 128 on
 // small-world graphs (the source-ordering BFS from the hubs ended within 32
 // levels: sources grouped by level profile keep many lanes active per task;
-// R-MAT scale 22 BC 103 -> 126 GTEPS, closeness 258 -> 490 GTEPS) and 32
-// otherwise, where a task usually has one active lane and the one-thread light
-// path of 32-lane groups matters (grids, meshes, roads).
+// R-MAT scale 22 BC 103 -> 126 GTEPS, closeness 258 -> 490 GTEPS), one lane per
+// task on deeper graphs of degree at most 64 (grids, meshes, roads: a lane
+// group's sampled sources rarely share a level; 1024^2 grid BC 3.9 -> 5.2
+// GTEPS), and 32 on other deep graphs.  The max degree is known from graph
+// creation for graphs of fewer than 2^22 vertices.
 static int32_t group_of(const gbc_graph_s* G, const gbc_options& o) {
     if (o.group_lanes) return o.group_lanes;
     if (G->tuned.done && G->tuned.group) return G->tuned.group;
-    return (G->key_depth > 0 && G->key_depth <= SMALL_WORLD_DEPTH) ? 128 : 32;
+    if (G->key_depth > 0 && G->key_depth <= SMALL_WORLD_DEPTH) return 128;
+    if (G->key_depth > SMALL_WORLD_DEPTH && G->g.max_degree <= ONE_LANE_MAX_DEGREE && G->g.n < ONE_LANE_MAX_N)
+        return 1;
+    return 32;
 }
 
 static int32_t pick_lanes(const gbc_graph_s* G, int64_t k, bool bc, int32_t requested, int32_t group) {
@@ -924,7 +929,8 @@ gbc_status gbc_autotune(gbc_graph G, const int32_t* sources, int32_t k, const gb
         GBC_TRY(timed(lanes, kb, sp0, li0, lp0, 128, bt0, ms));
         if (ms < best) { best = ms; best_gr = 128; }
     }
-    if (o.group_lanes == 0 && G->key_depth > SMALL_WORLD_DEPTH && G->g.max_degree <= 64 && G->g.n < (1 << 22)) {
+    if (o.group_lanes == 0 && G->key_depth > SMALL_WORLD_DEPTH && G->g.max_degree <= ONE_LANE_MAX_DEGREE &&
+        G->g.n < ONE_LANE_MAX_N) {
         double ms = 0;
         GBC_TRY(tune_batch(G, lanes, kb, o, sp0, li0, lp0, 1, bt0, ms));   // warm-up of the one-lane engine
         GBC_TRY(timed(lanes, kb, sp0, li0, lp0, 1, bt0, ms));

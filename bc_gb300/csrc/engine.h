@@ -212,6 +212,9 @@ private:
 // SMALL_WORLD_DEPTH run on 128-lane groups.
 gbc_status level_profile_key(const DevGraph& g, cudaStream_t stream, std::vector<uint32_t>& key, int32_t& depth);
 constexpr int32_t SMALL_WORLD_DEPTH = 32;
+// Graphs deeper than SMALL_WORLD_DEPTH with at most this degree and fewer vertices run one lane per
+// task by default (the entry packing v << 10 | lane needs n < 2^22).
+constexpr int32_t ONE_LANE_MAX_DEGREE = 64, ONE_LANE_MAX_N = 1 << 22;
 
 // Plain engine: one source at a time, int32 distances, uint64 sigma, the
 // level loop driven from the host with one device->host read per level.

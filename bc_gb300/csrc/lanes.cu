@@ -158,19 +158,22 @@ __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, 
 
 constexpr int MAX_LEVEL = Lv<uint16_t>::MAXD;
 
-// One lane per task: bc[v] += the lanes' contributions, which the sweep left in
-// the path-count slots of every (vertex, lane) it processed (levels 1 and
-// deeper), summed in lane order.
+// One lane per task: bcg[p][v] += the contributions of the lanes of 32-lane
+// part p, which the sweep left in the path-count slots of every (vertex, lane)
+// it processed (levels 1 and deeper), summed in lane order.  The partials are
+// kept per 32 lanes as for lane groups, so served requests can share a batch.
 __global__ void lane_bc_reduce_kernel(KArgs A, int lanes) {
     const uint16_t* lv = reinterpret_cast<const uint16_t*>(A.lvl);
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.n; v += gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int a = 0; a < lanes; a++) {
-            const size_t i = (size_t)a * (size_t)A.n + (size_t)v;
-            const uint16_t L = lv[i];
-            if (L != 0 && L != S_INF) s += __longlong_as_double((long long)A.sig[i]);
+        for (int p = 0; p * 32 < lanes; p++) {
+            double s = 0.0;
+            for (int a = 32 * p; a < min(lanes, 32 * p + 32); a++) {
+                const size_t i = (size_t)a * (size_t)A.n + (size_t)v;
+                const uint16_t L = lv[i];
+                if (L != 0 && L != S_INF) s += __longlong_as_double((long long)A.sig[i]);
+            }
+            A.bcg[(size_t)p * (size_t)A.n + v] += s;
         }
-        A.bcg[v] += s;
     }
 }
 
@@ -237,7 +240,7 @@ struct LaneAccess {
 size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc, int32_t group) {
     if (group == 1) {   // 16-bit levels, lane-major state, every (vertex, lane) once in the queue
         size_t b = (size_t)lanes * n * (2 + 4) + (size_t)(MAX_LEVEL + 2) * 16 + (1 << 20);
-        if (need_bc) b += (size_t)lanes * n * 16 + (size_t)n * 8;
+        if (need_bc) b += (size_t)lanes * n * 16 + (size_t)((lanes + 31) / 32) * n * 8;
         return b;
     }
     const size_t ng = (size_t)lanes / 32;
@@ -355,8 +358,8 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     if (need_bc) {
         sig_sz_ = cells * sizeof(uint64_t);
         rho_sz_ = cells * sizeof(double);
-        // BC partials per 32 lanes (128-lane groups keep one per quarter); one lane per task: one accumulator
-        bcg_sz_ = (gs_ ? (size_t)(lanes / 32) : 1) * n * sizeof(double);
+        // BC partials per 32 lanes, for every group width (128-lane groups keep one per quarter)
+        bcg_sz_ = (size_t)((lanes + 31) / 32) * n * sizeof(double);
         ok &= dev_alloc((void**)&sig_, sig_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&rho_, rho_sz_) == cudaSuccess;
         ok &= dev_alloc((void**)&bcg_, bcg_sz_) == cudaSuccess;
@@ -458,18 +461,13 @@ gbc_status LaneEngine::bc_begin() {
 }
 
 gbc_status LaneEngine::bc_finish(double* d_bc) {
-    if (gs_ == 0) {
-        GBC_CUDA(cudaMemcpyAsync(d_bc, bcg_, sizeof(double) * g_->n, cudaMemcpyDeviceToDevice, stream_));
-        return GBC_OK;
-    }
-    bc_reduce_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(bcg_, lanes_ / 32, g_->n, d_bc);
+    bc_reduce_kernel<<<sm_count_ * 4, 256, 0, stream_>>>(bcg_, (lanes_ + 31) / 32, g_->n, d_bc);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
 }
 
 gbc_status LaneEngine::bc_scatter(double* const* d_dst) {
-    if (gs_ == 0) { set_error("per-group BC partials need lane groups of 32 or 128"); return GBC_ERR_ARG; }
-    bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, lanes_ / 32, g_->n, d_dst);
+    bc_scatter_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(bcg_, (lanes_ + 31) / 32, g_->n, d_dst);
     GBC_CUDA(cudaGetLastError());
     return GBC_OK;
 }

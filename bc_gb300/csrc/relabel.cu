@@ -326,6 +326,7 @@ gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order_out, int
     GBC_CUDA(cudaStreamSynchronize(s));
     int64_t md = 0;
     for (int32_t v = 0; v < n; v++) md = std::max<int64_t>(md, row[v + 1] - row[v]);
+    g.max_degree = (int32_t)md;
     if (md > LOCALITY_MAX_DEGREE) return relabel_by_degree(g, s, d_order_out, d_inv_out);
     std::vector<int32_t> col((size_t)g.m), order;
     GBC_CUDA(cudaMemcpyAsync(col.data(), g.col, sizeof(int32_t) * (size_t)g.m, cudaMemcpyDeviceToHost, s));

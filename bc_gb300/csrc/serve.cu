@@ -73,7 +73,8 @@ struct SGraph {
     bool isolated(int32_t v) const { return g.comp_edges[g.comp[v]] == 0; }
     int32_t group = 32;          // lanes per lane group: 128 on small-world graphs, as on graph handles
     // device bytes of the narrowest lane engine this graph runs with
-    size_t engine_floor() const { return LaneEngine::bytes_needed(g.n, group, true); }
+    int32_t unit() const { return group == 1 ? 32 : group; }   // lanes an engine grows by
+    size_t engine_floor() const { return LaneEngine::bytes_needed(g.n, unit(), true, group); }
     ~SGraph() {
         eng.reset();
         cudaFree(g.row);
@@ -160,7 +161,7 @@ namespace {
 // wider one that fits; its buffers go to the cache.
 gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& graph_busy, int64_t pending) {
     SGraph& G = *S->graphs[gi];
-    const int32_t gr = G.group;
+    const int32_t gr = G.unit();
     const int32_t cap = S->max_lanes / gr * gr;
     const int32_t want = (int32_t)std::min<int64_t>(cap, std::max<int64_t>(gr, (pending + gr - 1) / gr * gr));
     if (G.eng && (G.eng->lanes() >= want || G.eng->lanes() >= cap)) return GBC_OK;
@@ -169,9 +170,9 @@ gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& g
     for (size_t j = 0; j < S->graphs.size(); j++)
         if ((int32_t)j != gi && S->graphs[j]->eng && graph_busy[j]) held += S->graphs[j]->eng->device_bytes();
     int32_t lanes = want;
-    while (lanes > gr && held + LaneEngine::bytes_needed(G.g.n, lanes, true) > S->budget)
+    while (lanes > gr && held + LaneEngine::bytes_needed(G.g.n, lanes, true, G.group) > S->budget)
         lanes = std::max(gr, lanes / 2 / gr * gr);
-    if (held + LaneEngine::bytes_needed(G.g.n, lanes, true) > S->budget) {
+    if (held + LaneEngine::bytes_needed(G.g.n, lanes, true, G.group) > S->budget) {
         if (G.eng) return GBC_OK;   // keep the engine it has
         set_error("graph does not fit the HBM budget");
         return GBC_ERR_BUSY;
@@ -179,14 +180,14 @@ gbc_status ensure_engine(gbc_server_s* S, int32_t gi, const std::vector<bool>& g
     if (G.eng && G.eng->lanes() >= lanes) return GBC_OK;   // nothing wider fits
     G.eng.reset();
     size_t used = S->engines_bytes() + S->results_bytes();
-    const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true);
+    const size_t need = LaneEngine::bytes_needed(G.g.n, lanes, true, G.group);
     for (size_t j = 0; j < S->graphs.size() && used + need > S->budget; j++) {
         if ((int32_t)j == gi || !S->graphs[j]->eng || graph_busy[j]) continue;
         used -= S->graphs[j]->eng->device_bytes();
         S->graphs[j]->eng.reset();
     }
     auto e = std::make_unique<LaneEngine>();
-    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream, gr));
+    GBC_TRY(e->init(&G.g, lanes, true, -1, 0, G.stream, G.group));
     if (G.lanes != lanes) {
         cudaFree(G.d_src);
         cudaFree(G.d_dst);
@@ -499,7 +500,13 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     int32_t depth = 0;
     GBC_TRY(level_profile_key(G->g, G->stream, G->key, depth));
-    G->group = (depth > 0 && depth <= SMALL_WORLD_DEPTH && s->max_lanes % 128 == 0) ? 128 : 32;
+    // 128-lane groups on small-world graphs; one lane per task on deep graphs of low degree, whose
+    // sampled sources rarely share a level (as graph handles choose them); 32-lane groups otherwise
+    int64_t maxdeg = 0;
+    for (int32_t v = 0; v < n; v++) maxdeg = std::max<int64_t>(maxdeg, row[v + 1] - row[v]);
+    if (depth > 0 && depth <= SMALL_WORLD_DEPTH && s->max_lanes % 128 == 0) G->group = 128;
+    else if (depth > SMALL_WORLD_DEPTH && maxdeg <= ONE_LANE_MAX_DEGREE && n < ONE_LANE_MAX_N) G->group = 1;
+    else G->group = 32;
     HostCSR h;
     h.n = n;
     h.row.assign(row, row + n + 1);
