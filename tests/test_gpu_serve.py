@@ -371,3 +371,34 @@ def test_requests_share_a_lane_group(gpu, orc):
             assert relerr(bc, h.bc(src)) < TOL
     ref, _ = orc.bc(orc.Graph(g.row, g.col), srcs[3], nthreads=8)
     assert relerr(res[3][1], ref) < TOL
+
+
+def test_deep_graph_serving_one_lane(gpu, orc):
+    """A deep grid of low degree runs one lane per task by default, on a graph
+    handle and on the server: requests that share a batch there (32-lane
+    parts of one-lane engines) each equal the oracle over their own sources."""
+    g = gpu.gen_grid(60, 60, 0.05, seed=7)
+    og = orc.Graph(g.row, g.col)
+    with gpu.Graph(g) as h:
+        src = np.arange(0, g.n, 37, dtype=np.int32)
+        bc = h.bc(src)
+        assert h.stats()["group_lanes"] == 1
+    # path counts on this grid pass 2^64: the oracle's level-scaled FP64 form is the reference
+    ref, _ = orc.bc(og, src, scaled=True, nthreads=8)
+    assert relerr(bc, ref) < TOL
+    S = Server(gpu, max_lanes=256)
+    gid = S.add(g)
+    rids = [S.submit(gid, gpu.Q_BC_SAMPLED, 40 + 10 * i, 70 + i) for i in range(5)]
+    rcc = S.submit(gid, gpu.Q_CC)
+    for r in rids + [rcc]:
+        assert S.wait(r) == gpu.REQ_DONE
+    srcs = [S.sources(r) for r in rids]
+    res = [S.fetch(r, gid) for r in rids]
+    st, _, cc, _ = S.fetch(rcc, gid)
+    c = S.counters()
+    S.close()
+    assert st == 0 and np.array_equal(cc, orc.cc(og, np.arange(g.n)))
+    assert c["shared"] > 0
+    for s, (st, b, _, _) in zip(srcs, res):
+        ref, _ = orc.bc(og, s, scaled=True, nthreads=8)
+        assert st == 0 and relerr(b, ref) < TOL
