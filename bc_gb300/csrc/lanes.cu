@@ -401,7 +401,9 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
 void LaneEngine::set_tuning(int sparse_lanes, int light_steps, int levels_per_graph, int block_threads, int bu_share) {
     const int sp = sparse_lanes < 0 ? 2 : sparse_lanes;
     const int li = light_steps < 0 ? 16 : light_steps;
-    const int lp = levels_per_graph > 0 ? levels_per_graph : 16;
+    // level kernels per captured graph: 16, or 64 on deep graphs (16-bit levels), whose thousands of
+    // levels would otherwise cost a graph launch and a host check every 16
+    const int lp = levels_per_graph > 0 ? levels_per_graph : (lvl_bytes_ == 2 ? 64 : 16);
     const int bt = (block_threads == 128 || block_threads == 512) ? block_threads : 256;
     const int bs = bu_share < 0 ? 16 : bu_share;
     if (sp == sparse_ && li == light_ && lp == lpg_ && bt == block_ && bs == bu_share_) return;
