@@ -404,7 +404,7 @@ static void map_sources(const gbc_graph_s* G, std::vector<int32_t>& hsrc) {
 // After the CSR is on the device: relabelling (degree order, or Cuthill-McKee
 // on deep graphs of low degree) and the id maps.
 static gbc_status finish_graph(gbc_graph_s* G) {
-    GBC_TRY(relabel_graph(G->g, G->stream, &G->d_order, &G->d_inv, nullptr));
+    GBC_TRY(relabel_graph(G->g, G->stream, &G->d_order, &G->d_inv));
     G->h_inv.resize(G->g.n);
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * G->g.n, cudaMemcpyDeviceToHost));
     return GBC_OK;

@@ -50,10 +50,10 @@ struct DevGraph;
 gbc_status relabel_by_degree(DevGraph& g, cudaStream_t s, int32_t** d_order, int32_t** d_inv);
 // The id order of graph handles and served graphs: Cuthill-McKee on deep graphs
 // of low degree (fewer than LOCALITY_MAX_N vertices, maximum degree at most
-// LOCALITY_MAX_DEGREE, a BFS deeper than LOCALITY_MIN_DEPTH levels; *locality
-// = true), descending degree on all others (relabel.cu).
+// LOCALITY_MAX_DEGREE, a BFS deeper than LOCALITY_MIN_DEPTH levels),
+// descending degree on all others (relabel.cu).
 constexpr int32_t LOCALITY_MAX_N = 1 << 22, LOCALITY_MAX_DEGREE = 64, LOCALITY_MIN_DEPTH = 32;
-gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order, int32_t** d_inv, bool* locality);
+gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order, int32_t** d_inv);
 // out[r*n + v] = in[r*n + inv[v]], r < rows.
 template <typename T>
 gbc_status gather_to_caller(const T* d_in, const int32_t* d_inv, int32_t n, int64_t rows, T* d_out, cudaStream_t s);

@@ -317,8 +317,7 @@ static gbc_status apply_order(DevGraph& g, cudaStream_t s, int32_t* order, int32
     return GBC_OK;
 }
 
-gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order_out, int32_t** d_inv_out, bool* locality) {
-    if (locality) *locality = false;
+gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order_out, int32_t** d_inv_out) {
     const int32_t n = g.n;
     if (n >= LOCALITY_MAX_N || g.m == 0) return relabel_by_degree(g, s, d_order_out, d_inv_out);
     std::vector<int64_t> row((size_t)n + 1);
@@ -345,9 +344,7 @@ gbc_status relabel_graph(DevGraph& g, cudaStream_t s, int32_t** d_order_out, int
         set_error("relabel order upload failed");
         return GBC_ERR_CUDA;
     }
-    GBC_TRY(apply_order(g, s, d_order, d_order_out, d_inv_out));
-    if (locality) *locality = true;
-    return GBC_OK;
+    return apply_order(g, s, d_order, d_order_out, d_inv_out);
 }
 
 // out[r*n + v] = in[r*n + inv[v]] for r < rows: per-vertex results back to the

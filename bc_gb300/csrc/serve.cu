@@ -495,7 +495,7 @@ gbc_status gbc_server_add_graph(gbc_server s, const int64_t* row, const int32_t*
     }
     GBC_CUDA(cudaMemcpy(G->g.row, row, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     if (row[n]) GBC_CUDA(cudaMemcpy(G->g.col, col, sizeof(int32_t) * row[n], cudaMemcpyHostToDevice));
-    GBC_TRY(relabel_graph(G->g, G->stream, &G->d_order, &G->d_inv, nullptr));
+    GBC_TRY(relabel_graph(G->g, G->stream, &G->d_order, &G->d_inv));
     G->h_inv.resize(n);
     GBC_CUDA(cudaMemcpy(G->h_inv.data(), G->d_inv, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
     int32_t depth = 0;
