@@ -1282,6 +1282,9 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                                            long long r0, long long r1, int sub, int nsub, int xm0, uint64_t (&acc)[4],
                                            unsigned& ofm, int (&we)[4], double (&ws)[4]) {
     const int t = threadIdx.x & 31;
+    // 2-byte counts: 32-bit sums, clamped to 2^16 after every chunk of 32 neighbours (a lane past
+    // 2^16 - 1 is over the width, so its batch is redone wider), so that they never wrap
+    unsigned a32[4] = {0u, 0u, 0u, 0u};
     int xm = xm0;   // columns of the chunk at r0 + 32*sub
     for (long long jb = r0 + 32LL * sub; jb < r1; jb += 32LL * nsub, xm = xm0) {
         const int cnt = (int)min(32LL, r1 - jb);
@@ -1313,8 +1316,11 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
                             w4[0] = w.x & 0xFFFFu; w4[1] = w.x >> 16; w4[2] = w.y & 0xFFFFu; w4[3] = w.y >> 16;
                         }
 #pragma unroll
-                        for (int j = 0; j < 4; j++)
-                            if ((pm >> j) & 1u) acc[j] += w4[j];
+                        for (int j = 0; j < 4; j++) {
+                            if (!((pm >> j) & 1u)) continue;
+                            if (SB == 2) a32[j] += w4[j];
+                            else acc[j] += w4[j];
+                        }
                         continue;
                     }
                     const uint64_t* sg = A.sig + ((gbase + (size_t)xs[i]) << 7) + 4 * t;
@@ -1359,6 +1365,14 @@ __device__ __forceinline__ void q_fwd_scan(const KArgs& A, Stage& S, int d, int 
         const bool has = ((want >> t) & 1u) && claim(A, gbase, xm, d + 1);
         if (MODE == 0 && has) S.fdeg += (unsigned long long)(A.row[xm + 1] - A.row[xm]);
         warp_append(A, S, has, has && is_hub(A, xm), ((uint32_t)xm << 5) | (uint32_t)g);
+        if (MODE == 1 && SB == 2) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) a32[j] = min(a32[j], 0x10000u);
+        }
+    }
+    if (MODE == 1 && SB == 2) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[j] += a32[j];
     }
 }
 
