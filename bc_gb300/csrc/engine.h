@@ -193,6 +193,9 @@ private:
     double* bcg_ = nullptr;
     unsigned long long* ccbuf_ = nullptr;
     int32_t* srcw_ = nullptr;             // per-lane source weights of the running batch
+    int4* ell_ = nullptr;                 // one lane per task, degree <= 8: padded neighbour table
+    int ell_q_ = 0;                       // int4 slots per vertex of ell_ (0: no table)
+    size_t ell_sz_ = 0;                   // bytes of ell_
     // bottom-up closeness levels (128-lane groups), set up on the first closeness batch
     int32_t* vcomp_ = nullptr;            // component label of every vertex
     int32_t* lcomp_ = nullptr;            // component label of every lane's source

@@ -100,6 +100,10 @@ struct KArgs {
     unsigned long long bu_share;
     // bytes per exact path count (128-lane groups: 2 or 4 while every count fits, else 8)
     int sig_bytes;
+    // one lane per task on graphs of degree <= 8: every vertex's neighbours in ell_q int4 slots
+    // (ell[v * ell_q + q], -1 past the degree), read in place of row offsets and columns; 0: none
+    const int4* ell;
+    int ell_q;
 };
 
 // Entry points of the level kernels of one CTA shape.
@@ -2030,15 +2034,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
             const bool act = base + t < e;
             const uint32_t ent = act ? A.fq[base + t] : 0u;
             const int v = (int)(ent >> S_LANE_BITS), a = (int)(ent & ((1u << S_LANE_BITS) - 1u));
-            const long long r0 = act ? A.row[v] : 0, r1 = act ? A.row[v + 1] : 0;
+            // neighbours from the padded table (no row-offset round trip) or from the CSR
+            const long long r0 = (act && !A.ell_q) ? A.row[v] : 0, r1 = (act && !A.ell_q) ? A.row[v + 1] : 0;
             const size_t la = (size_t)a * (size_t)A.n;
             if (act) vis += (unsigned long long)(r1 - r0);
             if (MODE == 0 && act) {
                 const long long c = (A.w ? (long long)d * (long long)A.w[v] : (long long)d) + (A.ff ? A.ff[v] : 0LL);
                 atomicAdd(&cc_sh[a], (unsigned long long)c);
             }
-            const int steps = (int)((r1 - r0 + U - 1) / U);
-            const int maxs = __reduce_max_sync(FULL, steps);
+            const int maxs = A.ell_q ? A.ell_q : __reduce_max_sync(FULL, (int)((r1 - r0 + U - 1) / U));
             long long j = r0;
             uint64_t acc = 0;
             bool of = false;
@@ -2047,8 +2051,15 @@ __global__ void __launch_bounds__(NT, 1024 / NT) expand_s_kernel(KArgs A) {
             for (int it = 0; it < maxs; it++) {
                 int x[U];
                 uint16_t L[U];
+                if (A.ell_q) {
+                    const int4 nb = act ? A.ell[(size_t)v * A.ell_q + it] : make_int4(-1, -1, -1, -1);
+                    x[0] = nb.x; x[1] = nb.y; x[2] = nb.z; x[3] = nb.w;
 #pragma unroll
-                for (int u = 0; u < U; u++) x[u] = (j + u < r1) ? A.col[j + u] : -1;
+                    for (int u = 0; u < U; u++) vis += x[u] >= 0;
+                } else {
+#pragma unroll
+                    for (int u = 0; u < U; u++) x[u] = (j + u < r1) ? A.col[j + u] : -1;
+                }
 #pragma unroll
                 for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[la + (size_t)x[u]] : dl;   // dl: neither case below
                 // path-count loads, then the discovery compare-and-swaps, then the sums:
@@ -2117,7 +2128,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) backward_s_kernel(KArgs A) {
             if (base + t < e) {   // the last fetch of a level may leave threads without an entry
                 const uint32_t ent = A.fq[base + t];
                 const int v = (int)(ent >> S_LANE_BITS), a = (int)(ent & ((1u << S_LANE_BITS) - 1u));
-                const long long r0 = A.row[v], r1 = A.row[v + 1];
+                // neighbours from the padded table (no row-offset round trip) or from the CSR
+                const long long r0 = A.ell_q ? 0 : A.row[v], r1 = A.ell_q ? (long long)U * A.ell_q : A.row[v + 1];
                 const size_t la = (size_t)a * (size_t)A.n, vi = la + (size_t)v;
                 const uint64_t sw = A.sig[vi];
                 T mv = T(0);
@@ -2128,8 +2140,13 @@ __global__ void __launch_bounds__(NT, 1024 / NT) backward_s_kernel(KArgs A) {
                 for (long long j = r0; j < r1; j += U) {
                     int x[U];
                     uint16_t L[U];
+                    if (A.ell_q) {
+                        const int4 nb = A.ell[(size_t)v * A.ell_q + (int)(j / U)];
+                        x[0] = nb.x; x[1] = nb.y; x[2] = nb.z; x[3] = nb.w;
+                    } else {
 #pragma unroll
-                    for (int u = 0; u < U; u++) x[u] = j + u < r1 ? A.col[j + u] : -1;
+                        for (int u = 0; u < U; u++) x[u] = j + u < r1 ? A.col[j + u] : -1;
+                    }
 #pragma unroll
                     for (int u = 0; u < U; u++) L[u] = x[u] >= 0 ? lv[la + (size_t)x[u]] : dl;
                     uint64_t rv[U];

@@ -147,6 +147,18 @@ __global__ void degree_order_kernel(const int64_t* __restrict__ row, int32_t n, 
         if (row[v + 1] - row[v] > row[v] - row[v - 1]) *out = 1u;
 }
 
+// ell[v * q + k / 4] component k % 4 = the k-th neighbour of v, -1 past its degree
+// (the one-lane kernels read a vertex's neighbours with q 16-byte loads).
+__global__ void ell_build_kernel(const int64_t* __restrict__ row, const int32_t* __restrict__ col, int32_t n, int q,
+                                 int32_t* __restrict__ ell) {
+    const int w = 4 * q;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * w; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = i / w, k = i - v * w;
+        const int64_t r0 = row[v], deg = row[v + 1] - r0;
+        ell[i] = k < deg ? col[r0 + k] : -1;
+    }
+}
+
 // bc[v] = sum of the per-32-lane partials, in lane order.
 __global__ void bc_reduce_kernel(const double* __restrict__ bcg, int ng, int n, double* __restrict__ bc) {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -220,6 +232,8 @@ struct LaneAccess {
         A.hub_lim = e.hub_lim_;
         A.bu_share = (unsigned long long)e.bu_share_;
         A.sig_bytes = e.sig_bytes_;
+        A.ell = e.ell_;
+        A.ell_q = e.ell_q_;
         return A;
     }
     // Reset the lane state a batch touched: per task when few were touched,
@@ -239,7 +253,7 @@ struct LaneAccess {
 
 size_t LaneEngine::bytes_needed(int32_t n, int32_t lanes, bool need_bc, int32_t group) {
     if (group == 1) {   // 16-bit levels, lane-major state, every (vertex, lane) once in the queue
-        size_t b = (size_t)lanes * n * (2 + 4) + (size_t)(MAX_LEVEL + 2) * 16 + (1 << 20);
+        size_t b = (size_t)lanes * n * (2 + 4) + (size_t)(MAX_LEVEL + 2) * 16 + (1 << 20) + (size_t)n * 32;   // + neighbour table
         if (need_bc) b += (size_t)lanes * n * 16 + (size_t)((lanes + 31) / 32) * n * 8;
         return b;
     }
@@ -271,6 +285,10 @@ void LaneEngine::release() {
     dev_release(ccbuf_, 1024 * sizeof(unsigned long long));
     dev_release(srcw_, 1024 * sizeof(int32_t));
     srcw_ = nullptr;
+    dev_release(ell_, ell_sz_);
+    ell_ = nullptr;
+    ell_q_ = 0;
+    ell_sz_ = 0;
     cudaFree(vcomp_);
     cudaFree(lcomp_);
     cudaFree(done_);
@@ -354,6 +372,13 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
     ok &= dev_alloc((void**)&ovf_, 32 * sizeof(uint32_t)) == cudaSuccess;
     ok &= dev_alloc((void**)&ccbuf_, 1024 * sizeof(unsigned long long)) == cudaSuccess;
     ok &= dev_alloc((void**)&srcw_, 1024 * sizeof(int32_t)) == cudaSuccess;
+    // one lane per task on a graph of degree <= 8: a padded neighbour table, so a frontier entry
+    // reads its neighbours with one or two 16-byte loads instead of row offsets, then columns
+    if (gs_ == 0 && g->max_degree > 0 && g->max_degree <= 8) {
+        ell_q_ = g->max_degree <= 4 ? 1 : 2;
+        ell_sz_ = (size_t)ell_q_ * n * sizeof(int4);
+        ok &= dev_alloc((void**)&ell_, ell_sz_) == cudaSuccess;
+    }
     ok &= cudaMallocHost(&ctl_host_, sizeof(Ctl)) == cudaSuccess;
     if (need_bc) {
         sig_sz_ = cells * sizeof(uint64_t);
@@ -387,13 +412,17 @@ gbc_status LaneEngine::init(const DevGraph* g, int32_t lanes, bool need_bc, int 
         // ids in descending degree order (graphs with hubs): hub <=> id < n_hubs_; no hubs: none
         hub_lim_ = (unsorted && nh > 0) ? -1 : (int)nh;
     }
+    if (ell_) {
+        ell_build_kernel<<<sm_count_ * 8, 256, 0, stream_>>>(g->row, g->col, g->n, ell_q_, reinterpret_cast<int32_t*>(ell_));
+        GBC_CUDA(cudaGetLastError());
+    }
     GBC_TRY(alloc_queue(gs_ == 0 ? (unsigned long long)lanes * n + (1ULL << 16) : (unsigned long long)ng_ * n * 8ULL + (1ULL << 16),
                         (unsigned long long)ng_ * n_hubs_ * 8ULL + (1ULL << 12)));
     GBC_CUDA(cudaMemsetAsync(lvl_, 0xFF, cells * sizeof(uint16_t), stream_));
     GBC_CUDA(cudaMemsetAsync(vmark_, 0xFF, vmark_sz_, stream_));
     GBC_CUDA(cudaMemsetAsync(ctl_, 0, sizeof(Ctl), stream_));
     GBC_CUDA(cudaMemsetAsync(ovf_, 0, 32 * sizeof(uint32_t), stream_));
-    bytes_ = cells * 2 + vmark_sz_ + (fcap_ + hcap_) * 4 + (need_bc ? cells * 16 + bcg_sz_ : 0);
+    bytes_ = cells * 2 + vmark_sz_ + (fcap_ + hcap_) * 4 + ell_sz_ + (need_bc ? cells * 16 + bcg_sz_ : 0);
     return GBC_OK;
 }
 

@@ -452,3 +452,47 @@ def test_group128_hub_with_wide_sigma(gpu, orc):
             assert G.stats()["sigma_mode_used"] == gpu.SIGMA_WIDE
             assert relerr(got, ref) < (TOL_F64 if dp == gpu.DELTA_F64 else TOL_F32)
         assert np.array_equal(G.cc(src, group_lanes=128), orc.cc(og, src))
+
+
+def king_graph(gpu, side, drop, seed):
+    """A side x side grid with diagonals (degree up to 8), a fraction of the edges dropped."""
+    r, c = np.divmod(np.arange(side * side), side)
+    u, v = [], []
+    for dr, dc in ((0, 1), (1, -1), (1, 0), (1, 1)):
+        ok = (r + dr < side) & (c + dc >= 0) & (c + dc < side)
+        u.append(np.nonzero(ok)[0])
+        v.append(np.nonzero(ok)[0] + dr * side + dc)
+    u, v = np.concatenate(u), np.concatenate(v)
+    keep = np.random.default_rng(seed).random(len(u)) >= drop
+    u, v = u[keep], v[keep]
+    a, b = np.concatenate([u, v]), np.concatenate([v, u])
+    o = np.lexsort((b, a))
+    row = np.zeros(side * side + 1, np.int64)
+    np.add.at(row, a + 1, 1)
+    return gpu.CSR(np.cumsum(row), b[o].astype(np.int32))
+
+
+@pytest.mark.parametrize("kind", ["grid", "king"])
+def test_one_lane_neighbour_table(gpu, orc, kind):
+    """Deep graphs of degree <= 4 and <= 8 run one lane per task by default and
+    read neighbours from the padded table (one or two 16-byte slots per vertex):
+    betweenness in both semantics, closeness, distances and path counts against
+    the oracle (level-scaled where path counts pass 2^64)."""
+    csr = gpu.gen_grid(70, 70, 0.05, seed=9) if kind == "grid" else king_graph(gpu, 64, 0.3, 2)
+    deg = np.diff(csr.row)
+    assert deg.max() <= (4 if kind == "grid" else 8) and (kind == "grid" or deg.max() > 4)
+    og = to_orc(orc, csr)
+    src = sources_of(csr, 150)
+    with gpu.Graph(csr) as G:
+        for sem in (0, 1):
+            ref, _ = orc.bc(og, src, semantics=sem, scaled=True, nthreads=8)
+            got = G.bc(src, semantics=sem)
+            assert G.stats()["group_lanes"] == 1
+            assert relerr(got, ref) < TOL_F64
+        assert np.array_equal(G.cc(src), orc.cc(og, src, nthreads=8))
+        dist, sig, ovf = G.sssp(src[:4])
+    for i in range(4):
+        d0, s0, o0, _ = orc.sssp(og, int(src[i]))
+        assert np.array_equal(dist[i], d0)
+        if not ovf[i] and not o0.any():
+            assert np.array_equal(sig[i], s0)
