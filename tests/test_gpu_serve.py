@@ -120,9 +120,15 @@ def test_mixed_stream_equals_alone(gpu, orc, graphs):
     for j, rid in enumerate(rids):
         assert S.wait(rid) == gpu.REQ_DONE
         results.append(S.fetch(rid, gids[plan[j][0]]))
+    # whether the stream above shares batches depends on its timing; four requests submitted
+    # back to back on one graph share at least the batch after the first one's
+    burst = [S.submit(gids[0], gpu.Q_BC_SAMPLED, 64, 900 + i) for i in range(4)]
+    for r in burst:
+        assert S.wait(r) == gpu.REQ_DONE
+        assert S.fetch(r, gids[0])[0] == 0
     c = S.counters()
     S.close()
-    assert c["completed"] == len(plan)
+    assert c["completed"] == len(plan) + len(burst)
     assert c["shared"] > 0, "no lane batch carried more than one request"
     lats = [r[3] for r in results]
     assert all(l > 0 for l in lats)
