@@ -155,7 +155,8 @@ public:
 
 private:
     friend struct LaneAccess;
-    gbc_status get_graph(int key, cudaGraphExec_t* out);
+    // the captured level loop of `count` level kernels for a kernel key
+    gbc_status get_graph(int key, int count, cudaGraphExec_t* out);
     gbc_status alloc_queue(unsigned long long cap, unsigned long long hcap);
     gbc_status ensure_events(size_t count);
     void release();
@@ -203,6 +204,7 @@ private:
     size_t done_sz_ = 0;
     struct Captured { int key = -1; cudaGraphExec_t exec = nullptr; };
     std::vector<Captured> graphs_;
+    int depth_hint_ = 0;                  // levels of the engine's last batch: the first forward graph's length
     int sm_count_ = 0;
     std::vector<cudaEvent_t> ev_;       // timing events, two per graph launch
 };

@@ -449,8 +449,9 @@ void LaneEngine::set_tuning(int sparse_lanes, int light_steps, int levels_per_gr
 // w = path-count width (0: 8 bytes, 1: 4, 2: 2; 128-lane groups only); +1000 with 16-bit levels.
 int LaneEngine::width_index() const { return sig_bytes_ == 2 ? 2 : sig_bytes_ == 4 ? 1 : 0; }
 
-gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
-    for (auto& c : graphs_) if (c.key == key) { *out = c.exec; return GBC_OK; }
+gbc_status LaneEngine::get_graph(int key, int count, cudaGraphExec_t* out) {
+    const int full = key + 100000 * count;
+    for (auto& c : graphs_) if (c.key == full) { *out = c.exec; return GBC_OK; }
     const int lv16 = key >= 1000 ? 1 : 0, k = key % 1000;
     const bool bwd = k >= 100;
     KArgs A = LaneAccess::args(*this, (bwd && ((k - 100) & 1)) ? GBC_BC_REFERENCE : GBC_BC_BRANDES);
@@ -469,7 +470,7 @@ gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     GBC_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t graph;
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    for (int i = 0; i < lpg_ && e == cudaSuccess; i++) {
+    for (int i = 0; i < count && e == cudaSuccess; i++) {
         fn<<<grid, block_, 0, cs>>>(A);
         e = cudaGetLastError();
     }
@@ -480,10 +481,18 @@ gbc_status LaneEngine::get_graph(int key, cudaGraphExec_t* out) {
     if (e2 == cudaSuccess) cudaGraphDestroy(graph);
     cudaStreamDestroy(cs);
     if (e != cudaSuccess) { set_error("level-loop graph capture failed: %s", cudaGetErrorString(e)); return GBC_ERR_CUDA; }
-    graphs_.push_back({key, exec});
+    graphs_.push_back({full, exec});
     *out = exec;
     return GBC_OK;
 }
+
+namespace {
+int pow2_at_least(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+}  // namespace
 
 gbc_status LaneEngine::bc_begin() {
     if (!need_bc_) { set_error("engine has no BC state"); return GBC_ERR_ARG; }
@@ -547,18 +556,23 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         cudaGraphExec_t fwd;
         const int lv16 = (lvl_bytes_ == 2) ? 1000 : 0;
         const int wi = mode == 1 ? width_index() : 0;
-        GBC_TRY(get_graph(lv16 + mode + 10 * wi, &fwd));
+        // the first graph as long as the last batch needed (levels + the launch that finds the
+        // next frontier empty), so shallow graphs launch few level kernels past their depth;
+        // later graphs lpg_ long
+        int count = depth_hint_ > 0 ? std::min(lpg_, pow2_at_least(depth_hint_ + 1)) : lpg_;
         Ctl* h = (Ctl*)ctl_host_;
         int64_t launched = 0;
         GBC_TRY(ensure_events(2));
         for (;;) {
+            GBC_TRY(get_graph(lv16 + mode + 10 * wi, count, &fwd));
             GBC_CUDA(cudaEventRecord(ev_[0], stream_));
             GBC_CUDA(cudaGraphLaunch(fwd, stream_));
             GBC_CUDA(cudaEventRecord(ev_[1], stream_));
             res.graph_launches++;
-            res.kernel_launches += lpg_;
-            res.fwd_kernels += lpg_;
-            launched += lpg_;
+            res.kernel_launches += count;
+            res.fwd_kernels += count;
+            launched += count;
+            count = lpg_;
             GBC_CUDA(cudaMemcpyAsync(h, ctl_, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_));
             GBC_CUDA(cudaStreamSynchronize(stream_));
             float ms = 0;
@@ -570,6 +584,7 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
             if (launched > (int64_t)MAX_LEVEL + 2 * lpg_) { set_error("forward level loop did not terminate"); return GBC_ERR_LIMIT; }
         }
         const int maxlevel = h->maxlevel;
+        depth_hint_ = maxlevel;
         const unsigned long long entries = std::min<unsigned long long>(h->tail, fcap_);
         const unsigned long long hentries = std::min<unsigned long long>(h->htail, hcap_);
         if (h->err & 1) {
@@ -665,19 +680,25 @@ gbc_status LaneEngine::run(const LaneRequest& rq, LaneResult& res) {
         if (rq.job == LaneJob::BC && maxlevel >= 1) {
             const int key = lv16 + 100 + 20 * wi + ((rq.sigma_wide ? 1 : 0) * 2 + (rq.delta_f64 ? 1 : 0)) * 2 +
                             (rq.semantics == GBC_BC_REFERENCE ? 1 : 0);
-            cudaGraphExec_t bwd;
-            GBC_TRY(get_graph(key, &bwd));
+            // the sweep runs levels maxlevel .. 1: graphs of lpg_ level kernels, then one of the
+            // power of two that covers the rest
+            const int nfull = maxlevel / lpg_, rest = maxlevel % lpg_;
+            const int nl = nfull + (rest ? 1 : 0);
+            cudaGraphExec_t bwd_full = nullptr, bwd_rest = nullptr;
+            if (nfull) GBC_TRY(get_graph(key, lpg_, &bwd_full));
+            if (rest) GBC_TRY(get_graph(key, pow2_at_least(rest), &bwd_rest));
             bw_begin_kernel<<<1, 1, 0, stream_>>>(A);
             res.kernel_launches++;
-            const int nl = (maxlevel + lpg_ - 1) / lpg_;
             GBC_TRY(ensure_events(2 * nl));
             for (int i = 0; i < nl; i++) {
+                const bool last_rest = rest && i == nfull;
+                const int cnt = last_rest ? pow2_at_least(rest) : lpg_;
                 GBC_CUDA(cudaEventRecord(ev_[2 * i], stream_));
-                GBC_CUDA(cudaGraphLaunch(bwd, stream_));
+                GBC_CUDA(cudaGraphLaunch(last_rest ? bwd_rest : bwd_full, stream_));
                 GBC_CUDA(cudaEventRecord(ev_[2 * i + 1], stream_));
                 res.graph_launches++;
-                res.kernel_launches += lpg_;
-                res.bwd_kernels += lpg_;
+                res.kernel_launches += cnt;
+                res.bwd_kernels += cnt;
             }
             GBC_CUDA(cudaStreamSynchronize(stream_));
             for (int i = 0; i < nl; i++) {
