@@ -72,7 +72,9 @@ typedef struct {
     int32_t lanes;            /* sources per batch, multiple of 32 in [32,1024]; 0 = autotune */
     int32_t sparse_lanes;     /* a frontier task with <= this many active lanes expands
                                  edge-parallel, otherwise lane-parallel; -1 = autotune */
-    int32_t levels_per_graph; /* level kernels per captured CUDA graph; 0 = default */
+    int32_t levels_per_graph; /* level kernels per captured CUDA graph; 0 = default (16, or 64 on
+                                 graphs deeper than 8-bit levels allow); a batch's first forward graph
+                                 and its sweep's last graph may be shorter, sized to the depth */
     int32_t source_order;     /* 0: group sources with similar BFS level profiles into the same
                                  lane group (results do not depend on it); 1: lanes in the order given */
     int32_t light_steps;      /* a frontier task with (active lanes x degree) <= this is expanded by a
