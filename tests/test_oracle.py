@@ -182,3 +182,34 @@ def test_oracle_rmat_generator_equals_product(gbc, orc, scale, ef, permute):
     b = gbc.gen_rmat(scale, ef, 0.57, 0.19, 0.19, seed=1, permute=permute)
     assert np.array_equal(a.row, b.row) and np.array_equal(a.col, b.col)
     assert np.array_equal(bench.sample_sources(a.row, 1024), bench.sample_sources(b.row, 1024))
+
+
+def test_reference_arm_line_without_the_library(tmp_path):
+    """bench.py --impl reference prints one JSON line with the fields the
+    measurement contract asks for, timing the oracle on the host cores, and
+    never maps libgbc.so into its process (it builds the R-MAT graph with the
+    oracle's restatement of the generator)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    probe = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--scale', '12', '--edge-factor', '8', "
+        "'--k', '256', '--steps', '1', '--warmup', '1']\n"
+        "try:\n"
+        "    runpy.run_path('bench.py', run_name='__main__')\n"
+        "except SystemExit:\n"
+        "    pass\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('LIBGBC_MAPPED' if 'libgbc.so' in maps else 'LIBGBC_ABSENT')\n")
+    r = subprocess.run([sys.executable, "-c", probe], cwd=root, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert lines[-1] == "LIBGBC_ABSENT"
+    line = json.loads(lines[-2])
+    assert line["impl"] == "reference" and line["unit"] == "GTEPS" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 1
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
